@@ -1,0 +1,161 @@
+/*
+ * nlse.h -- C ABI of the GB300 propagator library (libnlse.so).
+ *
+ * Axisymmetric split-step NLSE for femtosecond pulses in fused silica on one
+ * GB300 (sm_103a).  The caller owns every field buffer (device memory, e.g.
+ * torch tensors passed by data pointer); a context owns only constant tables
+ * and the workspace it allocates once in nlse_create.  No entry point
+ * allocates device memory after nlse_create returns.
+ *
+ * Layout of a field: row-major (Nr rows = radius, Nt columns = time), complex
+ * single precision interleaved (re, im) -- i.e. float2 / torch.complex64.
+ * Carrier densities: row-major float32 (Nr x Nt), cm^-3.
+ *
+ * Every function returns an nlse_status.  On failure the context keeps a
+ * message, readable with nlse_get_last_error.  Launches are asynchronous on
+ * the given stream (a cudaStream_t passed as void*; NULL = legacy default).
+ * A context is not thread-safe; use one context per host thread.
+ *
+ * Reference interfaces replaced (paths in omatousou/Rapport, relative to
+ * ".github/deliverable (3)/sim"):
+ *   nlse_create           build_grids + LinearOperator/NonlinearOperator
+ *                         constructors (grids.py:29-175, operators.py:35-87)
+ *   nlse_half_linear      LinearOperator.half_linear     (operators.py:47-53)
+ *   nlse_split            NonlinearOperator.split        (operators.py:89-146)
+ *   nlse_nonlinear_step   the alpha/2 + RK4 + alpha/2 block of
+ *                         Integrator.step                 (integrator.py:140-147)
+ *   nlse_update_plasma    NonlinearOperator.update_plasma + the
+ *                         solve_rate_equation_kernel      (operators.py:165-183,
+ *                                                          kernels.py:36-106)
+ *   nlse_step             Integrator.step                (integrator.py:138-149)
+ *   nlse_propagate        the z loop of Integrator.propagate: nsteps x
+ *                         (update_plasma, step)           (integrator.py:156-158)
+ *   nlse_destroy          (context teardown; the reference frees by GC)
+ */
+#ifndef NLSE_H
+#define NLSE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef struct nlse_ctx nlse_ctx;
+
+typedef enum {
+    NLSE_OK = 0,
+    NLSE_ERR_INVALID_ARG = 1,   /* bad pointer, size, alignment or value   */
+    NLSE_ERR_UNSUPPORTED = 2,   /* physics toggle / grid not built (yet)   */
+    NLSE_ERR_CUDA = 3,          /* a CUDA runtime call or launch failed    */
+    NLSE_ERR_DEVICE_FLAG = 4,   /* a kernel reported a device-side error   */
+    NLSE_ERR_TIMEOUT = 5        /* a bounded device wait gave up           */
+} nlse_status;
+
+/* Physics switches (Config field names, config.py:115-170). */
+enum {
+    NLSE_F_KERR_INSTANT   = 1 << 0,  /* enable_kerr_instantaneous   */
+    NLSE_F_PHOTO_LOSS     = 1 << 1,  /* enable_photoionization_loss */
+    NLSE_F_PLASMA_DEFOC   = 1 << 2,  /* enable_plasma_defocusing    */
+    NLSE_F_PLASMA_ABSORB  = 1 << 3,  /* enable_plasma_absorption    */
+    NLSE_F_KERR_RAMAN     = 1 << 4,  /* not built: rejected         */
+    NLSE_F_SELF_STEEP     = 1 << 5,  /* not built: rejected         */
+    NLSE_F_SPACE_TIME     = 1 << 6,  /* not built: rejected         */
+    NLSE_F_STE            = 1 << 7   /* not built: rejected         */
+};
+
+/* Linear-operator arithmetic used by nlse_step. */
+enum {
+    NLSE_MODE_PLAIN_F32 = 0,   /* FP32 SIMT Hankel products, reference order  */
+    NLSE_MODE_SPLIT_BF16 = 1   /* tcgen05 split-BF16 merged operator (I + E)  */
+};
+
+/*
+ * Everything the propagator needs, computed once on the host in FP64 by the
+ * caller (the Python layer's build_grids).  Pointers are HOST pointers; the
+ * arrays are copied during nlse_create and may be freed afterwards.
+ */
+typedef struct {
+    int Nr;                     /* radial points (Config.N - 1)             */
+    int Nt;                     /* time points, a power of two, 16..8192    */
+    int flags;                  /* NLSE_F_* bits                            */
+    double dt;                  /* time step [s]                             */
+    double komega;              /* k0 = n0 w0 / c [1/m]                      */
+    /* linear operator (grids.py:39-73) */
+    const double *Y;            /* Nr*Nr quasi-discrete Hankel matrix        */
+    const double *rho_modes;    /* Nr Hankel wavenumbers rho_m [1/m]         */
+    const double *delta_k;      /* Nt dispersion delta_k(Omega) [1/m]        */
+    const double *spec_mask;    /* Nt spectral band mask                     */
+    const double *mask_r;       /* Nr radial absorber                        */
+    double Rk_iRk;              /* Rk * iRk (mathematically 1)               */
+    /* nonlinear step (operators.py:60-68, 89-146) */
+    double invE2;               /* |u|^2 -> I [W/cm^2]                       */
+    double kerr_pref;           /* 3 chi3 w0^2 / (8 k0 c^2)                  */
+    double kerr_scale;          /* (1 - f_R) with the instantaneous Kerr on  */
+    double plasma_pref;         /* sigma(w0)/2 * 100                         */
+    double omega0_tau_c;        /* w0 tau_c (plasma phase 1 + i w0 tau_c)    */
+    double rho_max;             /* rho_nt [cm^-3]                            */
+    double photo_const;         /* 1e6 Ui / (n0 c eps0)                      */
+    /* PCHIP rate spline on I_k = 10^d (1 + 0.01 m) (grids.py:140-146)       */
+    int pchip_n;                /* number of knots (17 * 900 = 15300)        */
+    const double *pchip_x;      /* pchip_n knots                             */
+    const double *pchip_c;      /* 4 x (pchip_n - 1), scipy PPoly order      */
+    /* carrier-rate table (grids.py:152-161, kernels.py:14-26)               */
+    int lut_n;                  /* 4096                                      */
+    const double *lut;          /* W(10^logI) [cm^-3 s^-1]                   */
+    double lut_log_min, lut_inv_dlog, lut_Imin, lut_Imax;
+    double beta_g;              /* avalanche coefficient sigma/Ui            */
+    double inv_tau_r;           /* 1/tau_r (0 = recombination off)           */
+} nlse_grid_desc;
+
+/* Build a context on the current CUDA device. */
+int nlse_create(const nlse_grid_desc *desc, nlse_ctx **out);
+
+/* u <- half_linear(u, dz): iRk Y F^-1[e^{i phi} mask F(Rk Y u)], in place. */
+int nlse_half_linear(nlse_ctx *ctx, void *u, double dz, void *stream);
+
+/* (rhs, alpha) <- split(u, rho): RK right-hand side and absorption rate.
+ * rhs: complex64 Nr x Nt, alpha: float32 Nr x Nt (may be NULL). */
+int nlse_split(nlse_ctx *ctx, const void *u, const float *rho, void *rhs,
+               float *alpha, void *stream);
+
+/* u <- e^{-alpha dz/2} . RK4 . e^{-alpha dz/2} (u), rho frozen, in place. */
+int nlse_nonlinear_step(nlse_ctx *ctx, void *u, const float *rho, double dz,
+                        void *stream);
+
+/* rho[:,0] = 0, then march the carrier rate equation along t for every r.
+ * rho_s may be NULL; when given it is zeroed (the STE channel is off). */
+int nlse_update_plasma(nlse_ctx *ctx, const void *u, float *rho, float *rho_s,
+                       void *stream);
+
+/* Integrator.step(dz): half-linear, nonlinear block, half-linear, mask_r;
+ * u in place, rho read (frozen), rho_s unused (may be NULL). */
+int nlse_step(nlse_ctx *ctx, void *u, const float *rho, const float *rho_s,
+              double dz, int mode, void *stream);
+
+/* nsteps iterations of the z loop of Integrator.propagate:
+ * update_plasma(u, rho, rho_s) then step(dz).  On return u holds the field
+ * after the last step and rho the densities of the last update (computed from
+ * the field entering that step), exactly as after the reference loop. */
+int nlse_propagate(nlse_ctx *ctx, void *u, float *rho, float *rho_s, double dz,
+                   int nsteps, int mode, void *stream);
+
+/* Number of (row, call) pairs the carrier scan has re-marched sequentially
+ * since nlse_create (saturated or non-converging rows); synchronous read. */
+int nlse_scan_fallback_rows(nlse_ctx *ctx, int *out);
+
+/* Copy the last error message of ctx (or of the last failed nlse_create when
+ * ctx is NULL) into buf; returns the status of that error. */
+int nlse_get_last_error(const nlse_ctx *ctx, char *buf, size_t len);
+
+/* Free the context's tables and workspace. */
+void nlse_destroy(nlse_ctx *ctx);
+
+/* Library version string. */
+const char *nlse_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* NLSE_H */

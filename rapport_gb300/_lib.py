@@ -1,0 +1,231 @@
+"""ctypes binding of libnlse.so (the C ABI declared in include/nlse.h).
+
+The library is loaded from ``rapport_gb300/lib/libnlse.so`` (built in-tree by
+``rapport_gb300.build``).  There is no fallback: if the library is missing or
+a CUDA device is unavailable, constructing a Context raises.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "lib", "libnlse.so")
+
+NLSE_OK, NLSE_ERR_INVALID_ARG, NLSE_ERR_UNSUPPORTED, NLSE_ERR_CUDA, NLSE_ERR_DEVICE_FLAG, NLSE_ERR_TIMEOUT = range(6)
+F_KERR_INSTANT, F_PHOTO_LOSS, F_PLASMA_DEFOC, F_PLASMA_ABSORB = 1, 2, 4, 8
+F_KERR_RAMAN, F_SELF_STEEP, F_SPACE_TIME, F_STE = 16, 32, 64, 128
+MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
+
+# every symbol include/nlse.h declares (checked by the CPU test suite)
+EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_split", "nlse_nonlinear_step",
+           "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_scan_fallback_rows",
+           "nlse_get_last_error", "nlse_destroy", "nlse_version")
+
+_P = ctypes.c_void_p
+_D = ctypes.c_double
+_I = ctypes.c_int
+
+
+class GridDesc(ctypes.Structure):
+    """Mirror of nlse_grid_desc."""
+    _fields_ = [
+        ("Nr", _I), ("Nt", _I), ("flags", _I), ("dt", _D), ("komega", _D),
+        ("Y", _P), ("rho_modes", _P), ("delta_k", _P), ("spec_mask", _P), ("mask_r", _P),
+        ("Rk_iRk", _D),
+        ("invE2", _D), ("kerr_pref", _D), ("kerr_scale", _D), ("plasma_pref", _D),
+        ("omega0_tau_c", _D), ("rho_max", _D), ("photo_const", _D),
+        ("pchip_n", _I), ("pchip_x", _P), ("pchip_c", _P),
+        ("lut_n", _I), ("lut", _P), ("lut_log_min", _D), ("lut_inv_dlog", _D),
+        ("lut_Imin", _D), ("lut_Imax", _D), ("beta_g", _D), ("inv_tau_r", _D),
+    ]
+
+
+_lib = None
+
+
+def load():
+    """Load libnlse.so once and declare the C signatures."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise ImportError(f"{LIB_PATH} is not built: run `python -c \"import __graft_entry__ as g; g.build()\"`")
+    lib = ctypes.CDLL(LIB_PATH)
+    lib.nlse_create.argtypes = [ctypes.POINTER(GridDesc), ctypes.POINTER(_P)]
+    lib.nlse_half_linear.argtypes = [_P, _P, _D, _P]
+    lib.nlse_split.argtypes = [_P, _P, _P, _P, _P, _P]
+    lib.nlse_nonlinear_step.argtypes = [_P, _P, _P, _D, _P]
+    lib.nlse_update_plasma.argtypes = [_P, _P, _P, _P, _P]
+    lib.nlse_step.argtypes = [_P, _P, _P, _P, _D, _I, _P]
+    lib.nlse_propagate.argtypes = [_P, _P, _P, _P, _D, _I, _I, _P]
+    lib.nlse_scan_fallback_rows.argtypes = [_P, ctypes.POINTER(_I)]
+    lib.nlse_get_last_error.argtypes = [_P, ctypes.c_char_p, ctypes.c_size_t]
+    lib.nlse_destroy.argtypes = [_P]
+    lib.nlse_destroy.restype = None
+    lib.nlse_version.restype = ctypes.c_char_p
+    for name in EXPORTS:
+        if name not in ("nlse_destroy", "nlse_version"):
+            getattr(lib, name).restype = _I
+    _lib = lib
+    return lib
+
+
+class NLSEError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"libnlse status {status}: {msg}")
+        self.status = status
+
+
+def _check(lib, ctx, status):
+    if status != NLSE_OK:
+        buf = ctypes.create_string_buffer(512)
+        lib.nlse_get_last_error(ctx, buf, 512)
+        raise NLSEError(status, buf.value.decode(errors="replace"))
+
+
+def physics_flags(cfg):
+    f = 0
+    if cfg.enable_kerr_instantaneous:
+        f |= F_KERR_INSTANT
+    if cfg.enable_photoionization_loss:
+        f |= F_PHOTO_LOSS
+    if cfg.enable_plasma_defocusing:
+        f |= F_PLASMA_DEFOC
+    if cfg.enable_plasma_absorption:
+        f |= F_PLASMA_ABSORB
+    if cfg.enable_kerr_raman:
+        f |= F_KERR_RAMAN
+    if cfg.enable_self_steepening:
+        f |= F_SELF_STEEP
+    if cfg.enable_space_time_focusing:
+        f |= F_SPACE_TIME
+    if cfg.enable_ste:
+        f |= F_STE
+    return f
+
+
+def _arr(a, keep):
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    keep.append(a)
+    return a.ctypes.data
+
+
+def make_desc(cfg, g):
+    """Fill an nlse_grid_desc from a Config and its build_grids() dict.
+    Returns (desc, keep-alive list)."""
+    from scipy.constants import c, epsilon_0
+    keep = []
+    kel = g["keldysh"]
+    sp = kel["f_spline"]
+    Nr, Nt = g["Y"].shape[0], len(g["tlist"])
+    d = GridDesc()
+    d.Nr, d.Nt, d.flags = Nr, Nt, physics_flags(cfg)
+    d.dt, d.komega = g["dt"], g["komega"]
+    d.Y = _arr(g["Y"], keep)
+    d.rho_modes = _arr(g["rholist"], keep)
+    d.delta_k = _arr(g["delta_k"], keep)
+    d.spec_mask = _arr(g["spec_mask"], keep)
+    d.mask_r = _arr(g["mask_r"][:, 0], keep)
+    Rk = g["R"] ** 2 / g["j1last"]
+    iRk = g["j1last"] / g["R"] ** 2
+    d.Rk_iRk = Rk * iRk
+    d.invE2 = g["invE2"]
+    d.kerr_pref = 3 * cfg.chi3 * cfg.omega0**2 / (8 * g["komega"] * c**2)
+    d.kerr_scale = 1.0 - cfg.f_R
+    d.plasma_pref = (g["sigmaomega"] / 2.0) * 100.0
+    d.omega0_tau_c = cfg.omega0 * cfg.tau_c
+    d.rho_max = cfg.rho_max
+    d.photo_const = 1e6 * cfg.Ui / (cfg.n0 * c * epsilon_0)
+    d.pchip_n = len(kel["I_knots"])
+    d.pchip_x = _arr(kel["I_knots"], keep)
+    d.pchip_c = _arr(sp.c, keep)
+    d.lut_n = kel["NLUT"]
+    d.lut = _arr(kel["W_LUT"], keep)
+    d.lut_log_min, d.lut_inv_dlog = kel["logImin"], kel["inv_dlog"]
+    d.lut_Imin, d.lut_Imax = kel["Imin"], kel["Imax"]
+    d.beta_g = g["avalanche_coef"]
+    d.inv_tau_r = g["inv_taur_eff"]
+    return d, keep
+
+
+class Context:
+    """One libnlse context (tables + workspace on the current CUDA device).
+
+    Methods take torch CUDA tensors: fields complex64 (Nr, Nt) C-contiguous,
+    densities float32 (Nr, Nt).  Work is queued on torch's current stream."""
+
+    def __init__(self, cfg=None, g=None, desc=None):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("rapport_gb300 needs a CUDA device (no CPU path exists)")
+        self.lib = load()
+        torch.cuda.init()
+        if desc is None:
+            desc, keep = make_desc(cfg, g)
+        self.Nr, self.Nt = desc.Nr, desc.Nt
+        h = _P()
+        st = self.lib.nlse_create(ctypes.byref(desc), ctypes.byref(h))
+        _check(self.lib, None, st)
+        self.h = h
+        self.device = torch.cuda.current_device()
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.nlse_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+    # ---------------------------------------------------------- checks
+    def _stream(self):
+        import torch
+        return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+    def _field(self, t, name, dtype=None):
+        import torch
+        dtype = dtype or torch.complex64
+        if not isinstance(t, torch.Tensor) or not t.is_cuda:
+            raise TypeError(f"{name} must be a CUDA tensor")
+        if t.dtype != dtype or tuple(t.shape) != (self.Nr, self.Nt) or not t.is_contiguous():
+            raise ValueError(f"{name} must be a contiguous {dtype} tensor of shape {(self.Nr, self.Nt)}, "
+                             f"got {t.dtype} {tuple(t.shape)}")
+        return ctypes.c_void_p(t.data_ptr())
+
+    def _rho(self, t, name):
+        import torch
+        return self._field(t, name, torch.float32)
+
+    # ---------------------------------------------------------- ops
+    def half_linear(self, u, dz):
+        _check(self.lib, self.h, self.lib.nlse_half_linear(self.h, self._field(u, "u"), float(dz), self._stream()))
+
+    def split(self, u, rho, rhs, alpha):
+        a = self._rho(alpha, "alpha") if alpha is not None else None
+        _check(self.lib, self.h, self.lib.nlse_split(self.h, self._field(u, "u"), self._rho(rho, "rho"),
+                                                     self._field(rhs, "rhs"), a, self._stream()))
+
+    def nonlinear_step(self, u, rho, dz):
+        _check(self.lib, self.h, self.lib.nlse_nonlinear_step(self.h, self._field(u, "u"), self._rho(rho, "rho"),
+                                                              float(dz), self._stream()))
+
+    def update_plasma(self, u, rho, rho_s=None):
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
+        _check(self.lib, self.h, self.lib.nlse_update_plasma(self.h, self._field(u, "u"), self._rho(rho, "rho"),
+                                                             rs, self._stream()))
+
+    def step(self, u, rho, dz, mode=MODE_PLAIN_F32):
+        _check(self.lib, self.h, self.lib.nlse_step(self.h, self._field(u, "u"), self._rho(rho, "rho"), None,
+                                                    float(dz), int(mode), self._stream()))
+
+    def propagate(self, u, rho, rho_s, dz, nsteps, mode=MODE_PLAIN_F32):
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
+        _check(self.lib, self.h, self.lib.nlse_propagate(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs,
+                                                         float(dz), int(nsteps), int(mode), self._stream()))
+
+    def scan_fallback_rows(self):
+        v = _I(0)
+        _check(self.lib, self.h, self.lib.nlse_scan_fallback_rows(self.h, ctypes.byref(v)))
+        return v.value

@@ -1,0 +1,159 @@
+"""Config: every tunable of the propagator, with the reference's field names.
+
+Mirrors ``Config`` of the reference solver (``deliverable (3)/sim/config.py``,
+fields :54-200, derived constants :202-256) so that code written against the
+reference constructs this one unchanged.  Three fields are added for this
+implementation:
+
+* ``rate_model``: ``"keldysh"`` (the reference's default table source,
+  ``KeldyshSiO2.rate``) or ``"mpi"`` (the K-photon power law
+  ``sigma_K I^K rho_nt`` of the measured workloads);
+* ``sigma_K`` / ``K_photons``: the power-law constants;
+* ``linear_mode``: ``"plain"`` (FP32 reference-ordered Hankel products) or
+  ``"split_bf16"`` (tcgen05 split-BF16 merged operator).
+"""
+import datetime
+from dataclasses import dataclass
+from typing import Optional
+
+import numpy as np
+from scipy.constants import c, epsilon_0, m_e
+from scipy.constants import elementary_charge as q_e
+
+# Fused-silica Sellmeier coefficients (B_i, lambda_i in um), keldysh.py:22-23.
+SELLMEIER_B = (0.6961663, 0.4079426, 0.8974794)
+SELLMEIER_L = (0.0684043, 0.1162414, 9.896161)
+
+
+def n_sellmeier(lam_m):
+    """Refractive index of fused silica at vacuum wavelength lam_m [m] (keldysh.py:25-29)."""
+    x = (lam_m * 1e6) ** 2
+    s = 1.0
+    for b, l in zip(SELLMEIER_B, SELLMEIER_L):
+        s += b * x / (x - l * l)
+    return float(np.sqrt(s))
+
+
+@dataclass
+class Config:
+    # numerical grid
+    nz: int = 40000
+    Nt: int = 4096
+    N: int = 1025
+    begin: float = -600e-6
+    end: float = 7400e-6
+    R_factor: float = 40.0
+    save_stride: int = 1
+    ckpt_every: int = 500
+    verbose: bool = True
+    out_dir: Optional[str] = None
+    # laser
+    wavelength: float = 1030e-9
+    energy_uJ: float = 15.0
+    peak_power_W: Optional[float] = None
+    w0: float = 10e-6
+    delta_t: float = 263e-15
+    z_focus_air_um: Optional[float] = None
+    # material (fused silica, SI)
+    n2: float = 2.4e-20
+    Ui_eV: float = 9.0
+    meff_rel: float = 0.64
+    meff_drude_rel: float = 1.0
+    tau_c: float = 1.7e-15
+    tau_r: float = 330e-15
+    f_R: float = 0.18
+    tau_d: float = 32e-15
+    tau_s: float = 12e-15
+    rho_max: float = 2.1e22
+    # self-trapped excitons
+    Us_eV: float = 6.0
+    enable_ste: bool = True
+    tau_ste: Optional[float] = None
+    # field-equation switches
+    enable_kerr_instantaneous: bool = True
+    enable_kerr_raman: bool = True
+    enable_self_steepening: bool = True
+    enable_photoionization_loss: bool = True
+    enable_plasma_defocusing: bool = True
+    enable_plasma_absorption: bool = True
+    enable_space_time_focusing: bool = True
+    enable_spectral_filter: bool = True
+    enable_ste_index: bool = True
+    E_tr_eV: float = 4.2
+    # carrier-equation switches
+    enable_avalanche: bool = True
+    enable_recombination: bool = True
+    # probe / recording
+    lambda_probe: float = 490e-9
+    rho_t_stride: int = 15
+    rho_r_stride: int = 1
+    absorb_time_bins_fs: Optional[tuple] = None
+    rho_snapshot_t_fs: Optional[float] = None
+    # adaptive step (reserved in the reference too)
+    adaptive: bool = False
+    dphi_max: float = 0.05
+    drho_rel_max: float = 0.10
+    dz_min: float = 10e-9
+    dz_max: float = 200e-9
+    dz_init: Optional[float] = None
+    # additions of this implementation
+    rate_model: str = "keldysh"
+    sigma_K: float = 1e-71
+    K_photons: int = 6
+    linear_mode: str = "plain"
+
+    def __post_init__(self):
+        self.omega0 = 2 * np.pi * c / self.wavelength
+        self.omega_probe = 2 * np.pi * c / self.lambda_probe
+        self.n0_probe = n_sellmeier(self.lambda_probe)
+        self.nc_probe = (epsilon_0 * m_e * self.omega_probe**2 / q_e**2) * 1e-6
+        self.frequency = c / self.wavelength
+        self.n0 = n_sellmeier(self.wavelength)
+        if self.z_focus_air_um is not None:
+            self.begin = -self.n0 * self.z_focus_air_um * 1e-6
+        self.Ui = self.Ui_eV * q_e
+        self.Us = self.Us_eV * q_e
+        self.meff = self.meff_rel * m_e
+        self.meff_drude = self.meff_drude_rel * m_e
+        self.chi3 = 4 / 3 * epsilon_0 * self.n0**2 * c * self.n2
+        self.Omega_r2 = 1.0 / self.tau_s**2 + 1.0 / self.tau_d**2
+        self.komega = 2 * np.pi / self.wavelength * self.n0
+        self.dz = (self.end - self.begin) / self.nz
+        self.b = self.komega * self.w0**2
+        if self.dz_init is None:
+            self.dz_init = min(self.dz, self.dz_max)
+        if self.peak_power_W is not None:
+            I0 = 2.0 * self.peak_power_W / (np.pi * self.w0**2)
+        else:
+            tp = self.delta_t / np.sqrt(2 * np.log(2))
+            I0 = 2.0 * (self.energy_uJ * 1e-6 / (tp * np.sqrt(np.pi / 2))) / (np.pi * self.w0**2)
+        self.I0_Wcm2 = I0 * 1e-4
+        self.E0 = float(np.sqrt(2.0 * self.I0_Wcm2 * 1e4 / (self.n0 * c * epsilon_0)))
+        if self.out_dir is None:
+            self.out_dir = (f"sio2_{datetime.datetime.now():%Y%m%d_%H%M%S}"
+                            f"_E{self.energy_uJ * 1e3:.0f}nJ_{self.delta_t * 1e15:.0f}fs")
+        if self.rate_model not in ("keldysh", "mpi"):
+            raise ValueError(f"rate_model must be 'keldysh' or 'mpi', got {self.rate_model!r}")
+        if self.linear_mode not in ("plain", "split_bf16"):
+            raise ValueError(f"linear_mode must be 'plain' or 'split_bf16', got {self.linear_mode!r}")
+        pts = self.w0 / (self.R_factor * self.w0 / (self.N - 1))
+        if self.verbose:
+            if pts < 3:
+                print(f"[WARN] RADIAL UNDER-SAMPLING: {pts:.1f} pts/w0. Raise N.")
+            elif pts < 6:
+                print(f"[WARN] Radial sampling marginal: {pts:.1f} pts/w0.")
+
+
+def workload_config(Nr, Nt, R_max, w0, T_half, dz, nz, **over):
+    """Config of the measured workloads: 800 nm in fused silica, n2 = 3.2e-20,
+    K = 6 multiphoton ionisation (sigma_K = 1e-71), avalanche, recombination
+    (tau_rec = 150 fs); Raman, self-steepening, space-time focusing and the
+    exciton channel off; a +-T_half window (through delta_t, whose only other
+    uses are E0 -- unused with an explicit envelope -- and Raman, off)."""
+    d = dict(nz=nz, Nt=Nt, N=Nr + 1, begin=0.0, end=nz * dz, R_factor=R_max / w0, w0=w0,
+             wavelength=800e-9, delta_t=T_half * np.sqrt(2 * np.log(2)) / 5.0, n2=3.2e-20,
+             Ui_eV=9.0, rho_max=2.1e22, tau_r=150e-15, f_R=0.0, enable_kerr_raman=False,
+             enable_self_steepening=False, enable_space_time_focusing=False, enable_ste=False,
+             rate_model="mpi", verbose=False, out_dir="", rho_t_stride=0)
+    d.update(over)
+    return Config(**d)

@@ -1,0 +1,151 @@
+// Fused nonlinear step: absorption half-steps + RK4 (Kerr, plasma, photo-ionisation).
+//
+// Integrator.step (integrator.py:140-147) calls NonlinearOperator.split six
+// times per z-step -- one alpha evaluation, four RK4 stages, one more alpha --
+// and each split (operators.py:89-146) runs ~10^2 elementwise launches plus
+// four FFTs.  With Raman, self-steepening and space-time focusing off the
+// transforms are identities and split is pointwise in (r, t):
+//
+//   alpha = max(photo + pp*rho, 0),  photo = W(I) Kc / (|u|^2 + 1e-30) * depl
+//   rhs   = i kp |u|^2 u - pp (1 + i w0 tau_c) rho u - photo u + alpha u
+//         = i (kp |u|^2 - pp w0 tau_c rho) u            (when alpha is unclamped)
+//
+// so the whole block (e^{-alpha dz/2}, RK4, e^{-alpha dz/2}) is ONE pass over
+// u and rho: 8 B + 4 B read, 8 B written per point, HBM-bound.  The absorbed
+// photo term cancels exactly in rhs; the kernel keeps the (alpha - alpha_raw)
+// correction only where the clamp can fire (rho < 0 or a non-finite alpha).
+//
+// W(I) is the reference's PCHIP spline of the rate table (grids.py:140-146)
+// evaluated at clip(I, Imin, Imax).  Its knots are I = 10^d (1 + 0.01 m), so
+// the interval index is computed in closed form; each interval stores the
+// Hermite cubic in s = (I - x_i)/h_i pre-scaled by Kc*invE2/x_i, which keeps
+// every FP32 intermediate in range (W alone reaches 1e52 at Imax).
+#include "nlse_internal.cuh"
+
+__constant__ float c_pow10[18] = {1e0f,  1e1f,  1e2f,  1e3f,  1e4f,  1e5f,  1e6f,  1e7f,  1e8f,
+                                  1e9f,  1e10f, 1e11f, 1e12f, 1e13f, 1e14f, 1e15f, 1e16f, 1e17f};
+
+// photo-ionisation loss rate [1/m] before depletion, for a finite I >= 0.
+__device__ __forceinline__ float photo_rate(float I, const NLParams &p, const float4 *__restrict__ tab) {
+    float Ic = fminf(fmaxf(I, p.Imin), p.Imax);
+    int d = (int)floorf(log10f(Ic));
+    d = min(max(d, 0), 16);
+    if (Ic < c_pow10[d] && d > 0) --d;
+    else if (Ic >= c_pow10[d + 1] && d < 16) ++d;
+    int m = (int)((Ic / c_pow10[d] - 1.0f) * 100.0f);
+    m = min(max(m, 0), 899);
+    int i = min(900 * d + m, p.n_int - 1);
+    d = i / 900;
+    m = i - 900 * d;
+    const float p10 = c_pow10[d];
+    const float xi = p10 * (1.0f + 0.01f * (float)m);
+    const float s = (Ic - xi) / (0.01f * p10);
+    const float4 cf = __ldg(&tab[i]);
+    float V = fabsf(fmaf(s, fmaf(s, fmaf(s, cf.w, cf.z), cf.y), cf.x));
+    float r = V * (xi / (I + p.tiny_I));
+    return isfinite(r) ? r : 0.0f;
+}
+
+// alpha(u, rho) and the raw sum it clamps, as split() computes them.
+__device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p,
+                                          const float4 *__restrict__ tab, float *raw) {
+    float photo = 0.0f;
+    if (p.photo_on) {
+        float I = a2 * p.invE2;
+        if (isfinite(I)) {
+            float dep = fminf(fmaxf(1.0f - rho * p.inv_rho_max, 0.0f), 1.0f);
+            photo = photo_rate(I, p, tab) * dep;
+        } else if (isnan(I)) {
+            photo = I;  // NaN: split() turns the sum into alpha = 0 (nan_to_num)
+        }             // +Inf: W(Imax) / Inf = 0 in split()
+    }
+    float ar = photo + p.pp_abs * rho;
+    *raw = ar;
+    return isfinite(ar) ? fmaxf(ar, 0.0f) : 0.0f;
+}
+
+// RK right-hand side of split() for one point; rho frozen.
+__device__ __forceinline__ float2 nl_rhs(float2 u, float rho, const NLParams &p,
+                                         const float4 *__restrict__ tab) {
+    float a2 = fmaf(u.x, u.x, u.y * u.y);
+    if (!(a2 >= 1e-30f)) return make_float2(0.0f, 0.0f);  // also NaN
+    float w = fmaf(p.kp, a2, -p.pp_def * rho);             // i w u
+    float corr = 0.0f;
+    if (rho < 0.0f) {
+        float raw;
+        float al = alpha_of(a2, rho, p, tab, &raw);
+        corr = isfinite(raw) ? al - raw : 0.0f;
+    }
+    float2 r = make_float2(fmaf(corr, u.x, -w * u.y), fmaf(corr, u.y, w * u.x));
+    if (!isfinite(r.x) || !isfinite(r.y)) r = make_float2(0.0f, 0.0f);
+    return r;
+}
+
+__device__ __forceinline__ float2 nl_point(float2 u, float rho, float dz, const NLParams &p,
+                                           const float4 *__restrict__ tab) {
+    const float hdz = 0.5f * dz;
+    float raw;
+    float a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
+    u = c_scale(u, expf(-hdz * a));
+    float2 k1 = nl_rhs(u, rho, p, tab);
+    float2 k2 = nl_rhs(make_float2(fmaf(hdz, k1.x, u.x), fmaf(hdz, k1.y, u.y)), rho, p, tab);
+    float2 k3 = nl_rhs(make_float2(fmaf(hdz, k2.x, u.x), fmaf(hdz, k2.y, u.y)), rho, p, tab);
+    float2 k4 = nl_rhs(make_float2(fmaf(dz, k3.x, u.x), fmaf(dz, k3.y, u.y)), rho, p, tab);
+    const float s6 = dz * (1.0f / 6.0f);
+    u.x = fmaf(s6, k1.x + 2.0f * (k2.x + k3.x) + k4.x, u.x);
+    u.y = fmaf(s6, k1.y + 2.0f * (k2.y + k3.y) + k4.y, u.y);
+    a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
+    return c_scale(u, expf(-hdz * a));
+}
+
+// Two points per thread per iteration (16-byte field loads, 8-byte rho loads).
+__global__ void __launch_bounds__(256)
+k_nonlinear_step(float4 *__restrict__ u, const float2 *__restrict__ rho, size_t npair, float dz,
+                 NLParams p, const float4 *__restrict__ tab) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npair;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float4 v = u[i];
+        float2 r = __ldg(&rho[i]);
+        float2 a = nl_point(make_float2(v.x, v.y), r.x, dz, p, tab);
+        float2 b = nl_point(make_float2(v.z, v.w), r.y, dz, p, tab);
+        u[i] = make_float4(a.x, a.y, b.x, b.y);
+    }
+}
+
+__global__ void __launch_bounds__(256)
+k_split(const float2 *__restrict__ u, const float *__restrict__ rho, float2 *__restrict__ rhs,
+        float *__restrict__ alpha, size_t n, NLParams p, const float4 *__restrict__ tab) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
+         i += (size_t)gridDim.x * blockDim.x) {
+        float2 v = u[i];
+        float r = rho[i];
+        rhs[i] = nl_rhs(v, r, p, tab);
+        if (alpha) {
+            float raw;
+            alpha[i] = alpha_of(fmaf(v.x, v.x, v.y * v.y), r, p, tab, &raw);
+        }
+    }
+}
+
+static int grid_for(size_t n) {
+    int dev = 0, sms = 148;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    size_t want = (n + 255) / 256;
+    size_t cap = (size_t)sms * 8;
+    return (int)(want < cap ? want : cap);
+}
+
+cudaError_t launch_nonlinear_step(nlse_ctx *c, float2 *u, const float *rho, float dz, cudaStream_t stream) {
+    size_t npair = (size_t)c->Nr * c->Nt / 2;
+    k_nonlinear_step<<<grid_for(npair), 256, 0, stream>>>((float4 *)u, (const float2 *)rho, npair, dz,
+                                                         c->nl, c->d_pchip);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, float2 *rhs, float *alpha,
+                         cudaStream_t stream) {
+    size_t n = (size_t)c->Nr * c->Nt;
+    k_split<<<grid_for(n), 256, 0, stream>>>(u, rho, rhs, alpha, n, c->nl, c->d_pchip);
+    return cudaGetLastError();
+}

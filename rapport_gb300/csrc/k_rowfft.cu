@@ -1,0 +1,69 @@
+// Row FFT kernels: the spectral part of the linear half step.
+//
+// LinearOperator.half_linear (operators.py:47-53) applies, between the two
+// Hankel products, fft_t -> multiply by exp(i phase) * spec_mask -> ifft_t with
+// phase = (delta_k(Omega) - rho_m^2 / (2 k0)) dz / 2 (space-time focusing off,
+// so the phase separates into an Omega factor and a Hankel-mode factor).
+// Here one CTA owns one row (one Hankel mode m): it loads the row into shared
+// memory, runs the forward FFT, multiplies by Pr[m] * Pt[Omega], runs the
+// inverse FFT and stores the row -- one HBM read and one write per element.
+#include "nlse_internal.cuh"
+
+// Per-dz phase tables, computed in FP64 on the device and rounded once:
+//   Pt[k] = exp(i delta_k[k] dz/2) * spec_mask[k] * Rk*iRk / Nt   (1/Nt = ifft norm)
+//   Pr[m] = exp(-i rho_m^2 dz / (4 k0))
+__global__ void k_phase_tables(const double *__restrict__ delta_k, const double *__restrict__ spec_mask,
+                               const double *__restrict__ rho_modes, int Nt, int Nr, double dz,
+                               double komega, double scale, float2 *__restrict__ Pt,
+                               float2 *__restrict__ Pr) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < Nt) {
+        double s, c;
+        sincos(delta_k[i] * dz * 0.5, &s, &c);
+        double m = spec_mask[i] * scale / (double)Nt;
+        Pt[i] = make_float2((float)(c * m), (float)(s * m));
+    }
+    if (i < Nr) {
+        double s, c;
+        double r = rho_modes[i];
+        sincos(-r * r * dz / (4.0 * komega), &s, &c);
+        Pr[i] = make_float2((float)c, (float)s);
+    }
+}
+
+cudaError_t launch_phase_tables(nlse_ctx *c, double dz, cudaStream_t stream) {
+    int n = c->Nt > c->Nr ? c->Nt : c->Nr;
+    k_phase_tables<<<(n + 255) / 256, 256, 0, stream>>>(c->d_delta_k, c->d_spec_mask, c->d_rho_modes,
+                                                        c->Nt, c->Nr, dz, c->komega, c->Rk_iRk,
+                                                        c->d_Pt, c->d_Pr);
+    return cudaGetLastError();
+}
+
+// u[m, :] <- ifft( Pr[m] Pt * fft(u[m, :]) ), one CTA per row, in place.
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_fft_phase_ifft(float2 *__restrict__ u, int Nt, int logNt, const float2 *__restrict__ tw,
+                 const float2 *__restrict__ Pt, const float2 *__restrict__ Pr) {
+    extern __shared__ float2 smem[];
+    float2 *b0 = smem, *b1 = smem + Nt;
+    const size_t row = blockIdx.x;
+    float2 *g = u + row * (size_t)Nt;
+    for (int i = threadIdx.x; i < Nt; i += blockDim.x) b0[i] = g[i];
+    __syncthreads();
+    float2 *s = fft_row<false>(b0, b1, Nt, logNt, tw);
+    const float2 pr = Pr[row];
+    for (int i = threadIdx.x; i < Nt; i += blockDim.x) s[i] = c_mul(s[i], c_mul(pr, __ldg(&Pt[i])));
+    __syncthreads();
+    float2 *o = s == b0 ? b1 : b0;
+    float2 *r = fft_row<true>(s, o, Nt, logNt, tw);
+    for (int i = threadIdx.x; i < Nt; i += blockDim.x) g[i] = r[i];
+}
+
+cudaError_t launch_fft_phase_ifft(nlse_ctx *c, float2 *u, cudaStream_t stream) {
+    size_t smem = 2 * (size_t)c->Nt * sizeof(float2);
+    cudaError_t e = cudaFuncSetAttribute(k_fft_phase_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_fft_phase_ifft<<<c->Nr, NLSE_ROW_THREADS, smem, stream>>>(u, c->Nt, c->logNt, c->d_tw, c->d_Pt,
+                                                                c->d_Pr);
+    return cudaGetLastError();
+}

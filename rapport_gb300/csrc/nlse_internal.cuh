@@ -1,0 +1,214 @@
+// Internal declarations shared by the libnlse translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+#include <stdint.h>
+#include <stdio.h>
+
+#include "../../include/nlse.h"
+
+#define NLSE_MAX_NT 8192
+#define NLSE_ROW_THREADS 256
+
+// ---------------------------------------------------------------- errors
+struct nlse_error_slot {
+    int status;
+    char msg[512];
+};
+
+void nlse_set_error(nlse_error_slot *slot, int status, const char *fmt, ...);
+
+#define NLSE_CUDA_TRY(slot, call)                                                   \
+    do {                                                                            \
+        cudaError_t e_ = (call);                                                    \
+        if (e_ != cudaSuccess) {                                                    \
+            nlse_set_error((slot), NLSE_ERR_CUDA, "%s failed: %s (%s:%d)", #call,   \
+                           cudaGetErrorString(e_), __FILE__, __LINE__);             \
+            return NLSE_ERR_CUDA;                                                   \
+        }                                                                           \
+    } while (0)
+
+// ---------------------------------------------------------------- parameters
+// Nonlinear step constants, FP32 (derived from nlse_grid_desc in FP64).
+struct NLParams {
+    float invE2;        // |u|^2 -> I
+    float kp;           // kerr_pref * kerr_scale (0 if instantaneous Kerr off)
+    float pp_abs;       // plasma_pref if absorption on else 0
+    float pp_def;       // plasma_pref * w0 tau_c if defocusing on else 0
+    float inv_rho_max;  // 1 / rho_max
+    int photo_on;       // photo-ionisation loss on
+    float Imin, Imax;   // spline clip range
+    float tiny_I;       // 1e-30 * invE2 (the +1e-30 of the reference, in I units)
+    int n_int;          // spline intervals
+};
+
+// Carrier-rate scan constants.
+struct ScanParams {
+    float invE2;
+    float a_coef;       // beta_g * dt  (a_n = a_coef * I_avg)
+    float c_rec;        // dt / tau_r
+    float na;           // rho_max
+    float inv_na;
+    float lut_log_min, lut_inv_dlog, Imin, Imax;
+    int lut_n;
+};
+
+// ---------------------------------------------------------------- context
+struct nlse_ctx {
+    nlse_error_slot err;
+    int device;
+    int Nr, Nt, logNt, flags;
+    double dt, komega, Rk_iRk;
+    NLParams nl;
+    ScanParams sc;
+    // device tables
+    float2 *d_tw;          // Nt forward twiddles exp(-2 pi i k / Nt)
+    float *d_Y;            // Nr*Nr fp32 Hankel matrix (plain path)
+    double *d_Y64;         // Nr*Nr fp64 (operator builder)
+    double *d_rho_modes;   // Nr
+    double *d_delta_k;     // Nt
+    double *d_spec_mask;   // Nt
+    float *d_mask_r;       // Nr
+    float4 *d_pchip;       // n_int scaled Hermite coefficients
+    float *d_lut_dt;       // lut_n entries of W * dt
+    // per-dz tables (rebuilt on the stream when dz changes)
+    double cached_dz;
+    float2 *d_Pt;          // Nt  exp(i dk dz/2) mask Rk iRk / Nt
+    float2 *d_Pr;          // Nr  exp(-i rho^2 dz / (4 k0))
+    // workspace
+    float2 *d_work;        // Nr*Nt complex64
+    int *d_flag;           // device status word
+};
+
+// ---------------------------------------------------------------- launchers
+// (implemented in the k_*.cu units; all asynchronous on `stream`)
+cudaError_t launch_phase_tables(nlse_ctx *c, double dz, cudaStream_t stream);
+cudaError_t launch_gemm_f32(const float *A, const float *B, float *C, int M, int N, int K,
+                            const float *row_scale, cudaStream_t stream);
+cudaError_t launch_fft_phase_ifft(nlse_ctx *c, float2 *u, cudaStream_t stream);
+cudaError_t launch_nonlinear_step(nlse_ctx *c, float2 *u, const float *rho, float dz,
+                                  cudaStream_t stream);
+cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, float2 *rhs,
+                         float *alpha, cudaStream_t stream);
+cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s,
+                             int zero_first, cudaStream_t stream);
+
+// ---------------------------------------------------------------- complex
+__device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
+__device__ __forceinline__ float2 c_sub(float2 a, float2 b) { return make_float2(a.x - b.x, a.y - b.y); }
+__device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
+    return make_float2(fmaf(a.x, b.x, -a.y * b.y), fmaf(a.x, b.y, a.y * b.x));
+}
+__device__ __forceinline__ float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
+
+// multiply by the quarter-turn exp(-+ i pi/2): forward (-i), inverse (+i)
+template <bool INV>
+__device__ __forceinline__ float2 c_quarter(float2 a) {
+    return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// ---------------------------------------------------------------- small DFTs
+// Decimation-in-frequency butterflies with natural-order outputs:
+// V[k] = sum_r v[r] exp(-+ 2 pi i r k / R).
+template <bool INV>
+__device__ __forceinline__ void dft2(float2 *v) {
+    float2 a = v[0];
+    v[0] = c_add(a, v[1]);
+    v[1] = c_sub(a, v[1]);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft4(float2 *v) {
+    float2 y0 = c_add(v[0], v[2]), y1 = c_sub(v[0], v[2]);
+    float2 y2 = c_add(v[1], v[3]), y3 = c_quarter<INV>(c_sub(v[1], v[3]));
+    v[0] = c_add(y0, y2);
+    v[2] = c_sub(y0, y2);
+    v[1] = c_add(y1, y3);
+    v[3] = c_sub(y1, y3);
+}
+
+template <bool INV>
+__device__ __forceinline__ void dft8(float2 *v) {
+    const float h = 0.70710678118654752f;
+    float2 a[4], b[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        a[r] = c_add(v[r], v[r + 4]);
+        b[r] = c_sub(v[r], v[r + 4]);
+    }
+    // b_r *= w8^r, w8 = exp(-+ i pi / 4)
+    b[1] = INV ? make_float2(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y))
+               : make_float2(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));
+    b[2] = c_quarter<INV>(b[2]);
+    b[3] = INV ? make_float2(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y))
+               : make_float2(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));
+    dft4<INV>(a);
+    dft4<INV>(b);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        v[2 * m] = a[m];
+        v[2 * m + 1] = b[m];
+    }
+}
+
+template <int R, bool INV>
+__device__ __forceinline__ void dft_small(float2 *v) {
+    if (R == 2) dft2<INV>(v);
+    else if (R == 4) dft4<INV>(v);
+    else dft8<INV>(v);
+}
+
+// One Stockham autosort pass of radix R over a row of N points held in shared
+// memory: reads src, writes dst.  Ns = product of the radices already applied.
+// tw = forward twiddles exp(-2 pi i k / N), k < N (conjugated for INV).
+template <int R, bool INV>
+__device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                              int N, int Ns, const float2 *__restrict__ tw) {
+    const int nb = N / R;
+    const int tstride = N / (Ns * R);
+    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
+        const int k = j & (Ns - 1);
+        float2 v[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
+        if (Ns > 1) {
+#pragma unroll
+            for (int r = 1; r < R; ++r) {
+                float2 w = __ldg(&tw[r * k * tstride]);
+                if (INV) w.y = -w.y;
+                v[r] = c_mul(v[r], w);
+            }
+        }
+        dft_small<R, INV>(v);
+        const int d0 = (j - k) * R + k;
+#pragma unroll
+        for (int r = 0; r < R; ++r) dst[d0 + r * Ns] = v[r];
+    }
+}
+
+// Full in-CTA FFT of one row (N = 2^logN, 2 <= N <= NLSE_MAX_NT) using two
+// shared buffers; returns the buffer holding the (unnormalised) result.
+// Radix-8 passes first, then one radix-4 or radix-2 pass for the remainder.
+template <bool INV>
+__device__ float2 *fft_row(float2 *buf0, float2 *buf1, int N, int logN, const float2 *__restrict__ tw) {
+    float2 *src = buf0, *dst = buf1;
+    int Ns = 1;
+    int n8 = logN / 3, rem = logN % 3;
+    for (int p = 0; p < n8; ++p) {
+        stockham_pass<8, INV>(src, dst, N, Ns, tw);
+        __syncthreads();
+        Ns *= 8;
+        float2 *t = src; src = dst; dst = t;
+    }
+    if (rem == 2) {
+        stockham_pass<4, INV>(src, dst, N, Ns, tw);
+        __syncthreads();
+        float2 *t = src; src = dst; dst = t;
+    } else if (rem == 1) {
+        stockham_pass<2, INV>(src, dst, N, Ns, tw);
+        __syncthreads();
+        float2 *t = src; src = dst; dst = t;
+    }
+    return src;
+}

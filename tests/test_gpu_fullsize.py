@@ -1,0 +1,62 @@
+"""Parity at the measured grid (N_r = 1024, N_t = 2048, config 2) and
+size-independent properties of the operators."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+from gpu_util import CONFIG2, Case, dev, host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def c2():
+    return Case(**CONFIG2)
+
+
+def test_one_z_step_matches_oracle(c2):
+    u = dev(c2.u0)
+    rho = dev(np.zeros(c2.u0.shape))
+    rs = dev(np.zeros(c2.u0.shape))
+    c2.ctx.propagate(u, rho, rs, c2.dz, 1)
+    uo, rho_o, _ = c2.og.propagate(c2.u0.copy(), 1, c2.dz)
+    assert rel_l2(host(u), uo) < 2e-5
+    assert np.abs(host(rho) - rho_o).max() <= 1e-3 * max(rho_o.max(), 1e-30)
+
+
+def test_half_linear_is_linear(c2):
+    rng = np.random.default_rng(5)
+    v = c2.u0 * (0.3 + 0.1j) + rng.standard_normal(c2.u0.shape) * 1e6
+    a, b = 0.7 - 0.2j, -1.3 + 0.4j
+    hu = host(c2.lin.half_linear(dev(c2.u0), c2.dz))
+    hv = host(c2.lin.half_linear(dev(v), c2.dz))
+    huv = host(c2.lin.half_linear(dev(a * c2.u0 + b * v), c2.dz))
+    assert rel_l2(huv, a * hu + b * hv) < 1e-5
+
+
+def test_half_linear_conserves_energy_of_smooth_pulse(c2):
+    # spectral mask ~ 1 over the pulse band and no absorber inside half_linear:
+    # the QDHT-weighted energy sum |u|^2 / J1(j_k)^2 is invariant
+    from scipy.special import j1
+    w = 1.0 / j1(c2.og.jz[:c2.og.Nr]) ** 2
+    u = c2.u0
+    h = host(c2.lin.half_linear(dev(u), c2.dz))
+    e0 = np.sum(np.abs(u) ** 2 * w[:, None])
+    e1 = np.sum(np.abs(h) ** 2 * w[:, None])
+    assert abs(e1 / e0 - 1) < 1e-5
+
+
+def test_carrier_density_monotone_without_recombination(c2):
+    import rapport_gb300 as R
+    from gpu_util import O
+    cfg = R.workload_config(256, 2048, 2e-3, 150e-6, 800e-15, 2.5e-6, 1, enable_recombination=False)
+    g = R.build_grids(cfg)
+    lin = R.LinearOperator(cfg, g)
+    nl = R.NonlinearOperator(cfg, g, lin.ctx)
+    og = O.OracleGrid(O.workload_config(256, 2048, 2e-3, 150e-6, 800e-15))
+    u = O.lens_gaussian(og, 30e-6, 100e-15, 5.0, 0.1, 0)
+    rho = dev(np.zeros(u.shape))
+    nl.update_plasma(dev(u), rho, None)
+    r = host(rho)
+    assert np.all(np.diff(r, axis=1) >= -1e-6 * r.max())
+    assert r.max() > 0

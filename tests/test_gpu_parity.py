@@ -1,0 +1,173 @@
+"""CUDA path (through the C ABI) against the FP64 oracle and the reference fixtures.
+
+Tolerances (FP32 arithmetic against FP64):
+  half_linear / split / nonlinear block : relative L2 <= 2e-5
+  carrier densities                     : max |diff| <= 2e-4 * row peak (Newton scan, FP32)
+  full z-steps                          : relative L2 <= 1e-4 after 10 strongly ionising steps
+"""
+import numpy as np
+import pytest
+
+import nlse_oracle as O
+from conftest import rel_l2
+from gpu_util import Case, dev, host
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def tiny_case(tiny):
+    return Case.from_fixture(tiny)
+
+
+@pytest.fixture(scope="module")
+def c1_case(cfg1):
+    return Case.from_fixture(cfg1)
+
+
+def _case(name, tiny_case, c1_case):
+    return tiny_case if name == "tiny" else c1_case
+
+
+@pytest.mark.parametrize("name", ["tiny", "cfg1"])
+def test_half_linear(name, tiny_case, c1_case):
+    c = _case(name, tiny_case, c1_case)
+    out = host(c.lin.half_linear(dev(c.u0), c.dz))
+    ref = c.og.half_linear(c.u0, c.dz)
+    assert rel_l2(out, ref) < 2e-5
+
+
+def test_half_linear_matches_reference_fixture(tiny, tiny_case):
+    out = host(tiny_case.lin.half_linear(dev(tiny_case.u0), tiny_case.dz))
+    assert rel_l2(out[tiny["rows"]], tiny["hl_u0"]) < 2e-5
+
+
+@pytest.mark.parametrize("name", ["tiny", "cfg1"])
+def test_update_plasma(name, tiny_case, c1_case):
+    c = _case(name, tiny_case, c1_case)
+    rho_o = np.zeros(c.u0.shape)
+    c.og.update_plasma(c.u0, rho_o, np.zeros(c.u0.shape))
+    rho = dev(np.full(c.u0.shape, 7.0))
+    rho_s = dev(np.full(c.u0.shape, 3.0))
+    c.nl.update_plasma(dev(c.u0), rho, rho_s, c.og.dt, 1, 256)
+    r = host(rho)
+    peak = np.maximum(rho_o.max(axis=1, keepdims=True), 1e-30)
+    assert np.all(np.abs(r - rho_o) <= 2e-4 * peak + 1e-30)
+    assert np.all(host(rho_s) == 0.0)
+    assert np.all(r[:, 0] == 0.0)
+
+
+@pytest.mark.parametrize("name", ["tiny", "cfg1"])
+def test_split(name, tiny_case, c1_case):
+    c = _case(name, tiny_case, c1_case)
+    u = c.og.half_linear(c.u0, c.dz)
+    rho = np.zeros(u.shape)
+    c.og.update_plasma(c.u0, rho, np.zeros(u.shape))
+    rhs_o, al_o = c.og.split(u, rho)
+    rhs, al = c.nl.split(dev(u), dev(rho))
+    assert rel_l2(host(rhs), rhs_o) < 2e-5
+    assert rel_l2(host(al), al_o) < 2e-5
+
+
+def test_split_matches_reference_fixture(tiny, tiny_case):
+    # the fixture's split was taken on half_linear(u0) with rho from update_plasma(u0)
+    u = tiny_case.og.half_linear(tiny_case.u0, tiny_case.dz)
+    rhs, al = tiny_case.nl.split(dev(u), dev(tiny["rho_u0"]))
+    assert rel_l2(host(rhs), tiny["split_rhs"]) < 2e-5
+    assert rel_l2(host(al), tiny["split_alpha"]) < 2e-5
+
+
+@pytest.mark.parametrize("name", ["tiny", "cfg1"])
+def test_nonlinear_block(name, tiny_case, c1_case):
+    c = _case(name, tiny_case, c1_case)
+    u = c.og.half_linear(c.u0, c.dz)
+    rho = np.zeros(u.shape)
+    c.og.update_plasma(c.u0, rho, np.zeros(u.shape))
+    ref = c.oracle_nl_block(u, rho)
+    ud = dev(u)
+    c.nl.nonlinear_step(ud, dev(rho), c.dz)
+    assert rel_l2(host(ud), ref) < 2e-5
+
+
+@pytest.mark.parametrize("name,tol", [("tiny", 1e-4), ("cfg1", 2e-5)])
+def test_z_steps_match_reference_fixture(name, tol, tiny, cfg1, tiny_case, c1_case):
+    d = tiny if name == "tiny" else cfg1
+    c = _case(name, tiny_case, c1_case)
+    u = dev(c.u0)
+    rho = dev(np.zeros(c.u0.shape))
+    rs = dev(np.zeros(c.u0.shape))
+    kept = list(d["steps_kept"])
+    done = 0
+    for j, s in enumerate(kept):
+        c.ctx.propagate(u, rho, rs, c.dz, s - done)
+        done = s
+        assert rel_l2(host(u)[d["rows"]], d["u_steps"][j]) < tol, s
+        r = host(rho)[d["rows"]]
+        ro = d["rho_steps"][j]
+        assert np.abs(r - ro).max() <= 1e-3 * max(ro.max(), 1e-30), s
+
+
+def test_propagate_equals_update_plus_step(tiny_case):
+    c = tiny_case
+    u1, u2 = dev(c.u0), dev(c.u0)
+    r1, r2 = dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+    s1, s2 = dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+    c.ctx.propagate(u1, r1, s1, c.dz, 3)
+    for _ in range(3):
+        c.nl.update_plasma(u2, r2, s2)
+        c.ctx.step(u2, r2, c.dz)
+    assert np.array_equal(host(u1), host(u2))
+    assert np.array_equal(host(r1), host(r2))
+
+
+def _k1_ctx(k1edge):
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    Nr, Nt = k1edge["E"].shape
+    cfg = R.workload_config(Nr, Nt, 1e-4, 1e-5, 3e-13, 5e-6, 1)
+    g = R.build_grids(cfg)
+    desc, keep = _lib.make_desc(cfg, g)
+    lut = np.ascontiguousarray(k1edge["W_LUT"], dtype=np.float64)
+    keep.append(lut)
+    desc.lut = lut.ctypes.data
+    desc.dt, desc.invE2 = float(k1edge["dt"]), float(k1edge["invE2"])
+    desc.beta_g, desc.inv_tau_r, desc.rho_max = float(k1edge["beta_g"]), float(k1edge["inv_tau_r"]), float(k1edge["na"])
+    desc.lut_log_min, desc.lut_inv_dlog = float(k1edge["logImin"]), float(k1edge["inv_dlog"])
+    desc.lut_Imin, desc.lut_Imax = float(k1edge["Imin"]), float(k1edge["Imax"])
+    return _lib.Context(desc=desc)
+
+
+def test_rate_scan_edge_cases_match_reference_kernel(k1edge):
+    """NaN / Inf samples, zeros, saturation (x > na clamp) -- known answers
+    from the reference kernel itself (k1_edge.npz, 'zero' case)."""
+    ctx = _k1_ctx(k1edge)
+    E = k1edge["E"]
+    rho = dev(np.zeros(E.shape))
+    with np.errstate(invalid="ignore"):
+        ctx.update_plasma(dev(E), rho, None)
+    r = host(rho)
+    ref = k1edge["ne_zero"]
+    peak = np.maximum(ref.max(axis=1, keepdims=True), 1e-30)
+    assert np.all(np.abs(r - ref) <= 2e-4 * peak)
+    assert r[3, 40] == 0.0 and r[3, 41] == 0.0
+    assert ctx.scan_fallback_rows() >= 2          # the saturated rows were re-marched exactly
+
+
+def test_bad_arguments_raise(tiny_case):
+    import torch
+    from rapport_gb300._lib import NLSEError
+    c = tiny_case
+    with pytest.raises(ValueError):
+        c.lin.half_linear(dev(c.u0).to(torch.complex128), c.dz)
+    with pytest.raises(NLSEError):
+        c.ctx.half_linear(dev(c.u0), -1.0)
+    with pytest.raises(NLSEError):
+        c.ctx.step(dev(c.u0), dev(np.zeros(c.u0.shape)), c.dz, mode=7)
+
+
+def test_unsupported_physics_rejected():
+    import rapport_gb300 as R
+    from rapport_gb300._lib import NLSEError
+    cfg = R.workload_config(16, 64, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_kerr_raman=True, f_R=0.18)
+    with pytest.raises(NLSEError, match="Raman"):
+        R.LinearOperator(cfg, R.build_grids(cfg))

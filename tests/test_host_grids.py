@@ -1,0 +1,74 @@
+"""Host-side FP64 tables of the product (rapport_gb300.grids / config) against
+the reference fixtures and the reference's published physics numbers."""
+import numpy as np
+import pytest
+
+import rapport_gb300 as R
+from conftest import meta_case, rel_l2
+
+
+def _cfg(d):
+    m = meta_case(d)
+    return R.workload_config(m["Nr"], m["Nt"], m["R_max"], m["w0"], m["T_half"], m["dz"], m["nsteps"]), m
+
+
+def test_product_grids_match_reference(tiny):
+    cfg, m = _cfg(tiny)
+    g = R.build_grids(cfg)
+    assert rel_l2(g["Y"], tiny["Y"]) < 1e-14
+    assert rel_l2(g["delta_k"], tiny["delta_k"]) < 1e-11
+    assert rel_l2(g["spec_mask"], tiny["spec_mask"]) < 1e-14
+    assert rel_l2(g["mask_r"][:, 0], tiny["mask_r"]) < 1e-14
+    assert rel_l2(g["rlist"], tiny["rlist"]) < 1e-15
+    kel = g["keldysh"]
+    assert rel_l2(kel["W_LUT"], tiny["W_LUT"]) < 1e-14
+    assert rel_l2(kel["f_spline"](tiny["I_probe"]), tiny["W_probe"]) < 1e-14
+    for k in ("invE2", "sigmaomega", "avalanche_coef", "inv_taur_eff", "dt", "komega"):
+        assert g[k] == pytest.approx(float(tiny[k]), rel=1e-13), k
+    assert kel["logImin"] == tiny["logImin"] and kel["inv_dlog"] == pytest.approx(float(tiny["inv_dlog"]))
+
+
+def test_envelope_matches_reference(tiny):
+    cfg, m = _cfg(tiny)
+    g = R.build_grids(cfg)
+    fn = R.envelope_lens(m["w0"], m["fwhm"], m["E"], m["f"], m["seed"])
+    assert rel_l2(fn(g["rr"], g["tt"], cfg, g), tiny["u0"]) < 1e-14
+
+
+def test_published_material_numbers():
+    # n0(800 nm) = 1.4533 and k'' = 361.6 fs^2/cm (reference ANALYSE_CRITIQUE.md:58-59)
+    cfg = R.Config(wavelength=800e-9, verbose=False, out_dir="")
+    assert cfg.n0 == pytest.approx(1.4533, abs=5e-5)
+    from scipy.constants import c
+    n = R.n_sellmeier
+    w0 = cfg.omega0
+    k = lambda w: w / c * n(2 * np.pi * c / w)  # noqa: E731
+    h = w0 * 1e-3
+    k2 = (k(w0 + h) - 2 * k(w0) + k(w0 - h)) / h**2
+    assert k2 * 1e30 * 1e-2 == pytest.approx(361.6, rel=2e-3)
+
+
+def test_keldysh_multiphoton_limit():
+    # Couairon 2005: for weak fields the Keldysh rate approaches sigma_6 I^6 rho_at
+    # (sigma_6 = 9.6e-70, rho_at = 2.1e22); the reference asserts 0.8 < W/W_MPI < 1.25 at 1e12 W/cm^2
+    from scipy.constants import m_e
+    cfg = R.Config(wavelength=800e-9, verbose=False, out_dir="")
+    W = R.keldysh_rate(1e12, 800e-9, 9.0, 0.64 * m_e, cfg.n0)
+    ratio = W / (9.6e-70 * 1e12**6 * 2.1e22)
+    assert 0.8 < ratio < 1.25
+
+
+def test_config_validation():
+    with pytest.raises(ValueError):
+        R.Config(rate_model="tunnel", verbose=False, out_dir="")
+    with pytest.raises(ValueError):
+        R.Config(linear_mode="fp8", verbose=False, out_dir="")
+    cfg = R.Config(verbose=False, out_dir="", begin=0.0, end=1e-2, nz=2000)
+    assert cfg.dz == pytest.approx(5e-6)
+
+
+def test_mpi_rate_table():
+    cfg = R.workload_config(64, 128, 1e-4, 1e-5, 3e-13, 5e-6, 1)
+    g = R.build_grids(cfg)
+    I = np.array([1e10, 3e12, 5e13])
+    assert np.allclose(g["keldysh"]["f_spline"](I), 1e-71 * I**6 * 2.1e22, rtol=2e-4)
