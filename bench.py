@@ -1,0 +1,313 @@
+"""Benchmark: z-steps/s of the split-step NLSE propagator on one GB300.
+
+Workload (the measured grid): N_r = 1024 radial points (R_max = 2 mm),
+N_t = 2048 time points (+-800 fs), 800 nm, 5 uJ, 100 fs FWHM, w0 = 150 um,
+lens f = 10 cm, 1 % seeded noise (numpy default_rng(0)), fused silica with K=6
+MPI (sigma_K = 1e-71), avalanche, recombination (150 fs), dz = 2.5 um.
+Synthetic input of that shape; no dataset is involved.
+
+One bench step = Z z-steps (update_plasma + step each, the reference's z-loop
+iteration) advanced by one call of the C ABI (nlse_propagate); the metric is
+z-steps/s.  Between timed steps the L2 is flushed (256 MB write) outside the
+timed events; inside a step the field stays on-chip as in the reference's own
+loop, whose host syncs happen only at _record.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+--impl reference times the FP64 CPU restatement of the reference path (the
+oracle: numpy complex128 + the C carrier march with OpenMP) on this host's
+cores, one z-step per bench step; rank 0 only under torchrun.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+METRIC = "z-steps/s (1 GB300), split-BF16 batched vs plain FP32, at ≤1e-4 L2 err vs FP64"
+WORKLOAD = dict(Nr=1024, Nt=2048, R_max=2e-3, w0=150e-6, T_half=800e-15, fwhm=100e-15, E=5.0, f=0.1,
+                dz=2.5e-6, seed=0)
+CONFIG = {"workload": "single pulse, N_r=1024 (R_max 2 mm) x N_t=2048 (+-800 fs), 5 uJ, 100 fs, w0 150 um, "
+                      "f 10 cm, 1% noise seed 0, K=6 MPI + avalanche + recombination, dz 2.5 um",
+          "Nr": 1024, "Nt": 2048, "dz_um": 2.5}
+
+
+def peaks():
+    p = os.path.join(HERE, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return d.get("hbm_gbs", 6800.0), d.get("bf16_tflops", 1900.0), d.get("bf16_tflops_sustained", 1700.0), \
+            "measured"
+    return 6800.0, 1900.0, 1700.0, "fallback"
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", f"--query-gpu={self.Q}", "--format=csv,noheader,nounits",
+                                       "-lms", "100", "-i", str(device)], stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        self.f.seek(0)
+        rows = [r.split(",") for r in self.f.read().splitlines() if r.strip()]
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except (ValueError, IndexError):
+                continue
+            for n, v in zip(names, r[5:9]):
+                if v.strip().lower().startswith("active"):
+                    reasons.add(n)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ our arm
+def run_ours(args, rank, world, local_rank):
+    import torch
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    w = WORKLOAD
+    Z = args.zsteps
+    cfg = R.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], w["dz"], Z)
+    g = R.build_grids(cfg)
+    ctx = _lib.Context(cfg, g)
+    u0 = R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"])(g["rr"], g["tt"], cfg, g)
+    u0 = np.ascontiguousarray(u0.astype(np.complex64))
+    modes = {"plain": _lib.MODE_PLAIN_F32, "split_bf16": _lib.MODE_SPLIT_BF16}
+    want = ["split_bf16", "plain"] if args.mode == "auto" else [args.mode]
+
+    def barrier():
+        if world > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    results = {}
+    lead = None
+    for name in want:
+        mode = modes[name]
+        u = torch.from_numpy(u0).to(dev)
+        rho = torch.zeros(u.shape, dtype=torch.float32, device=dev)
+        rs = torch.zeros_like(rho)
+        try:
+            ctx.propagate(u, rho, rs, w["dz"], 1, mode)
+        except _lib.NLSEError as e:
+            if args.mode != "auto":
+                raise
+            results[name] = {"unavailable": str(e)}
+            continue
+        lead = lead or name
+        K = args.steps if name == lead else max(2, args.steps // 4)
+        for _ in range(args.warmup):
+            ctx.propagate(u, rho, rs, w["dz"], Z, mode)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        ctx.profile_start(K * Z * 16 + 64)
+        clk = ClockSampler(local_rank) if name == lead else None
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(K):
+            flush.fill_(float(i))
+            ev[i][0].record()
+            ctx.propagate(u, rho, rs, w["dz"], Z, mode)
+            ev[i][1].record()
+        torch.cuda.synchronize()
+        barrier()
+        clocks = clk.stop() if clk else None
+        prof = ctx.profile_read()
+        t_ms = sum(a.elapsed_time(b) for a, b in ev)
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([t_ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t_ms = float(tt.item())
+        results[name] = dict(K=K, t_ms=t_ms, zsteps_per_s=world * K * Z / (t_ms * 1e-3), prof=prof,
+                             clocks=clocks, finite=bool(torch.isfinite(u).all().item()))
+    head = next(n for n in want if "t_ms" in results.get(n, {}))
+    r = results[head]
+    mode = modes[head]
+
+    # ---------------------------------------------------------- e2e: host buffers through the C ABI
+    uh = torch.from_numpy(u0).pin_memory()
+    uo = torch.empty_like(uh).pin_memory()
+    rho_h = torch.empty(u0.shape, dtype=torch.float32).pin_memory()
+    ud = torch.empty(u0.shape, dtype=torch.complex64, device=dev)
+    rd = torch.zeros(u0.shape, dtype=torch.float32, device=dev)
+    sd = torch.zeros_like(rd)
+    e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(r["K"])]
+    for i in range(r["K"] + 1):
+        flush.fill_(float(i))
+        if i > 0:
+            e_ev[i - 1][0].record()
+        ud.copy_(uh, non_blocking=True)
+        ctx.propagate(ud, rd, sd, w["dz"], Z, mode)
+        uo.copy_(ud, non_blocking=True)
+        rho_h.copy_(rd, non_blocking=True)
+        if i > 0:
+            e_ev[i - 1][1].record()
+    torch.cuda.synchronize()
+    e_ms = sum(a.elapsed_time(b) for a, b in e_ev)
+    assert np.isfinite(uo.numpy()).all()
+    e2e = {"value": world * r["K"] * Z / (e_ms * 1e-3), "unit": "z-steps/s",
+           "h2d_bytes_per_step": int(uh.numel() * 8), "d2h_bytes_per_step": int(uo.numel() * 8 + rho_h.numel() * 4)}
+
+    # ---------------------------------------------------------- roofline of the dominant kernel
+    hbm, bf16, bf16_s, src = peaks()
+    prof = r["prof"]
+    top = max(prof, key=lambda k: prof[k][1])
+    n_launch, tot = prof[top]
+    avg_s = tot / n_launch * 1e-3
+    Nr, Nt = w["Nr"], w["Nt"]
+    traffic = None
+    tpath = os.path.join(HERE, "profiles", "traffic_per_launch.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get(top)
+    if top in ("k_gemm_tc", "k_gemm_f32"):
+        flops = (8.0 if top == "k_gemm_tc" else 4.0) * Nr * Nr * Nt   # per launch (algorithmic)
+        ach = flops / avg_s / 1e12
+        roof = {"kernel": top, "bound": "tensor", "achieved": ach, "peak": bf16_s, "unit": "TFLOP/s",
+                "frac": ach / bf16_s, "traffic": traffic, "peak_source": f"bf16_tflops_sustained ({src})",
+                "per_launch": f"{flops:.3e} algorithmic FLOPs, avg {avg_s * 1e6:.1f} us over {n_launch} launches"}
+    else:
+        byts = {"k_rate_scan": 12.0, "k_row_scan": 20.0, "k_row_nl": 36.0, "k_nonlinear_step": 20.0,
+                "k_fft_phase_ifft": 16.0}.get(top, 16.0) * Nr * Nt
+        ach = byts / avg_s / 1e9
+        roof = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
+                "traffic": traffic, "peak_source": f"hbm_gbs ({src})",
+                "per_launch": f"{byts:.3e} algorithmic bytes, avg {avg_s * 1e6:.1f} us over {n_launch} launches"}
+
+    line = {
+        "metric": METRIC, "value": r["zsteps_per_s"], "unit": "z-steps/s", "n_gpus": world, "steps": r["K"],
+        "warmup": args.warmup, "ms_per_step": r["t_ms"] / r["K"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "bf16x3-split + f32" if head == "split_bf16" else "f32",
+        "data": "synthetic (seeded lens-focused Gaussian pulse with 1% noise)",
+        "config": dict(CONFIG, form=head, z_steps_per_step=Z, parallelism=f"replicas{world}",
+                       l2="256 MB flush before each timed step (outside its events); inputs (24 MB) < L2"),
+        "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "clocks": r["clocks"],
+        "forms": {k: (round(v["zsteps_per_s"], 1) if "zsteps_per_s" in v else v) for k, v in results.items()},
+    }
+    if world == 1 and rank == 0 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(args.cpu_zsteps)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+# ------------------------------------------------------------------ CPU (oracle) arm
+def _oracle_setup():
+    sys.path.insert(0, os.path.join(HERE, "oracle"))
+    import nlse_oracle as O
+    w = WORKLOAD
+    og = O.OracleGrid(O.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"]))
+    u = O.lens_gaussian(og, w["w0"], w["fwhm"], w["E"], w["f"], w["seed"])
+    return og, u
+
+
+def cpu_baseline(nz):
+    og, u = _oracle_setup()
+    rho = np.zeros(u.shape)
+    rs = np.zeros(u.shape)
+    og.update_plasma(u, rho, rs)
+    t = time.perf_counter()
+    for _ in range(nz):
+        og.update_plasma(u, rho, rs)
+        u = og.step(u, rho, rs, WORKLOAD["dz"])
+    dt = time.perf_counter() - t
+    return {"value": nz / dt, "unit": "z-steps/s", "cores": os.cpu_count(), "kind": "port",
+            "sample": f"{nz} z-steps of the 1024x2048 workload (FP64 numpy/OpenBLAS + C carrier march, "
+                      f"OpenMP over r)"}
+
+
+def run_reference(args, rank):
+    if rank != 0:
+        return
+    og, u = _oracle_setup()
+    rho = np.zeros(u.shape)
+    rs = np.zeros(u.shape)
+    for _ in range(args.warmup):
+        og.update_plasma(u, rho, rs)
+        u = og.step(u, rho, rs, WORKLOAD["dz"])
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        og.update_plasma(u, rho, rs)
+        u = og.step(u, rho, rs, WORKLOAD["dz"])
+    dt = time.perf_counter() - t
+    v = args.steps / dt
+    cores = os.cpu_count()
+    print(json.dumps({
+        "metric": METRIC, "value": v, "unit": "z-steps/s", "n_gpus": 0, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic",
+        "config": dict(CONFIG, form="reference CPU path (FP64 restatement)", z_steps_per_step=1),
+        "impl": "reference",
+        "cpu_baseline": {"value": v, "unit": "z-steps/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} z-steps of the 1024x2048 workload"},
+        "e2e": {"value": v, "unit": "z-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--mode", default="auto", choices=["auto", "plain", "split_bf16"])
+    ap.add_argument("--zsteps", type=int, default=50, help="z-steps per bench step")
+    ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local_rank = int(os.environ.get("LOCAL_RANK", "0"))
+    if args.impl == "reference":
+        run_reference(args, rank)
+        return
+    run_ours(args, rank, world, local_rank)
+
+
+if __name__ == "__main__":
+    main()

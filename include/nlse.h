@@ -145,6 +145,17 @@ int nlse_propagate(nlse_ctx *ctx, void *u, float *rho, float *rho_s, double dz,
  * since nlse_create (saturated or non-converging rows); synchronous read. */
 int nlse_scan_fallback_rows(nlse_ctx *ctx, int *out);
 
+/* Per-launch profiling: bracket each of the next `capacity` kernel launches
+ * with CUDA events on its stream (host-side records, no device allocation). */
+int nlse_profile_start(nlse_ctx *ctx, int capacity);
+
+/* Synchronise on the last record, sum each kernel kind's launches and event
+ * time (ms) into launches[kind] / total_ms[kind] for kind < nkinds, and stop
+ * recording.  Kind names: nlse_kernel_name(kind) ("" for unused ids). */
+int nlse_profile_read(nlse_ctx *ctx, int *launches, double *total_ms, int nkinds,
+                      int *dropped);
+const char *nlse_kernel_name(int kind);
+
 /* Copy the last error message of ctx (or of the last failed nlse_create when
  * ctx is NULL) into buf; returns the status of that error. */
 int nlse_get_last_error(const nlse_ctx *ctx, char *buf, size_t len);

@@ -20,6 +20,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 # every symbol include/nlse.h declares (checked by the CPU test suite)
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_scan_fallback_rows",
+           "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
            "nlse_get_last_error", "nlse_destroy", "nlse_version")
 
 _P = ctypes.c_void_p
@@ -64,8 +65,12 @@ def load():
     lib.nlse_destroy.argtypes = [_P]
     lib.nlse_destroy.restype = None
     lib.nlse_version.restype = ctypes.c_char_p
+    lib.nlse_profile_start.argtypes = [_P, _I]
+    lib.nlse_profile_read.argtypes = [_P, ctypes.POINTER(_I), ctypes.POINTER(_D), _I, ctypes.POINTER(_I)]
+    lib.nlse_kernel_name.argtypes = [_I]
+    lib.nlse_kernel_name.restype = ctypes.c_char_p
     for name in EXPORTS:
-        if name not in ("nlse_destroy", "nlse_version"):
+        if name not in ("nlse_destroy", "nlse_version", "nlse_kernel_name"):
             getattr(lib, name).restype = _I
     _lib = lib
     return lib
@@ -224,6 +229,20 @@ class Context:
         rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
         _check(self.lib, self.h, self.lib.nlse_propagate(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs,
                                                          float(dz), int(nsteps), int(mode), self._stream()))
+
+    def profile_start(self, capacity):
+        _check(self.lib, self.h, self.lib.nlse_profile_start(self.h, int(capacity)))
+
+    def profile_read(self, nkinds=16):
+        """-> {kernel name: (launches, total ms)} of the records since profile_start."""
+        L = (_I * nkinds)()
+        T = (_D * nkinds)()
+        _check(self.lib, self.h, self.lib.nlse_profile_read(self.h, L, T, nkinds, None))
+        out = {}
+        for k in range(nkinds):
+            if L[k]:
+                out[self.lib.nlse_kernel_name(k).decode()] = (L[k], T[k])
+        return out
 
     def scan_fallback_rows(self):
         v = _I(0)

@@ -54,6 +54,22 @@ __device__ __forceinline__ float step_map(float x, float a, float b, const ScanP
                                           bool *clamped) {
     float d = fminf(fmaxf(1.0f - x * p.inv_na, 0.0f), 1.0f);
     float z = fmaf(a, d, -p.c_rec);
+    if (z > 80.0f) {
+        // e^z overflows FP32 but not FP64 (below z = 709.78): there the reference
+        // computes y = e^z x + b d (e^z - 1)/z, which exceeds na unless x and b d
+        // are tiny -- evaluate it in log space; beyond 709.78 FP64 overflows too
+        // and the reference's non-finite -> 0 rule resets the density.
+        *J = 0.0f;
+        if (z > 709.78f) return 0.0f;
+        float s = fmaf(b * d, 1.0f / z, x);
+        if (!(s > 0.0f)) return 0.0f;
+        float lg = z + logf(s);
+        if (lg > logf(p.na)) {
+            *clamped = true;
+            return p.na;
+        }
+        return expf(lg);
+    }
     float e = expf(z);
     float em1 = expm1f(z);
     float az = fabsf(z);

@@ -21,8 +21,21 @@ void nlse_set_error(nlse_error_slot *slot, int status, const char *fmt, ...) {
     va_end(ap);
 }
 
+static void prof_free(nlse_ctx *c) {
+    if (c->prof_ev) {
+        for (int i = 0; i < 2 * c->prof_cap; ++i)
+            if (c->prof_ev[i]) cudaEventDestroy(c->prof_ev[i]);
+        free(c->prof_ev);
+    }
+    free(c->prof_kid);
+    c->prof_ev = nullptr;
+    c->prof_kid = nullptr;
+    c->prof_on = c->prof_cap = c->prof_n = 0;
+}
+
 static void free_ctx(nlse_ctx *c) {
     if (!c) return;
+    prof_free(c);
     void *ptrs[] = {c->d_tw, c->d_Y, c->d_Y64, c->d_rho_modes, c->d_delta_k, c->d_spec_mask,
                     c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_Pt, c->d_Pr, c->d_work, c->d_flag};
     for (void *p : ptrs)
@@ -257,6 +270,24 @@ static int launched(nlse_ctx *c, cudaError_t e, const char *what) {
     return NLSE_OK;
 }
 
+// Bracket one launch with events on its stream when profiling is on.
+struct ProfScope {
+    nlse_ctx *c;
+    cudaStream_t st;
+    int slot;
+    ProfScope(nlse_ctx *c_, int kid, cudaStream_t s) : c(c_), st(s), slot(-1) {
+        if (c->prof_on && c->prof_n < c->prof_cap) {
+            slot = c->prof_n++;
+            c->prof_kid[slot] = kid;
+            cudaEventRecord(c->prof_ev[2 * slot], st);
+        }
+    }
+    ~ProfScope() {
+        if (slot >= 0) cudaEventRecord(c->prof_ev[2 * slot + 1], st);
+    }
+};
+#define PROF(kid) ProfScope prof_scope_##__LINE__(c, (kid), st)
+
 static int field_ok(nlse_ctx *c, const void *p, const char *name) {
     if (!p) {
         nlse_set_error(&c->err, NLSE_ERR_INVALID_ARG, "%s is NULL", name);
@@ -272,6 +303,7 @@ static int field_ok(nlse_ctx *c, const void *p, const char *name) {
 static int ensure_tables(nlse_ctx *c, double dz, cudaStream_t st) {
     if (!(dz > 0) || !isfinite(dz)) return bad(c, NLSE_ERR_INVALID_ARG, "dz must be positive and finite");
     if (dz == c->cached_dz) return NLSE_OK;
+    PROF(K_PHASE_TABLES);
     int s = launched(c, launch_phase_tables(c, dz, st), "phase tables");
     if (s == NLSE_OK) c->cached_dz = dz;
     return s;
@@ -281,11 +313,18 @@ static int half_linear_impl(nlse_ctx *c, float2 *u, double dz, const float *row_
     int s = ensure_tables(c, dz, st);
     if (s) return s;
     const int M = c->Nr, N = 2 * c->Nt;
-    s = launched(c, launch_gemm_f32(c->d_Y, (const float *)u, (float *)c->d_work, M, N, M, nullptr, st),
-                 "hankel gemm 1");
+    {
+        PROF(K_GEMM_F32);
+        s = launched(c, launch_gemm_f32(c->d_Y, (const float *)u, (float *)c->d_work, M, N, M, nullptr, st),
+                     "hankel gemm 1");
+    }
     if (s) return s;
-    s = launched(c, launch_fft_phase_ifft(c, c->d_work, st), "fft phase ifft");
+    {
+        PROF(K_FFT_PHASE);
+        s = launched(c, launch_fft_phase_ifft(c, c->d_work, st), "fft phase ifft");
+    }
     if (s) return s;
+    PROF(K_GEMM_F32);
     return launched(c, launch_gemm_f32(c->d_Y, (const float *)c->d_work, (float *)u, M, N, M, row_scale, st),
                     "hankel gemm 2");
 }
@@ -300,29 +339,35 @@ extern "C" int nlse_half_linear(nlse_ctx *c, void *u, double dz, void *stream) {
 extern "C" int nlse_split(nlse_ctx *c, const void *u, const float *rho, void *rhs, float *alpha, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !field_ok(c, rhs, "rhs")) return NLSE_ERR_INVALID_ARG;
-    return launched(c, launch_split(c, (const float2 *)u, rho, (float2 *)rhs, alpha, (cudaStream_t)stream),
-                    "split");
+    cudaStream_t st = (cudaStream_t)stream;
+    PROF(K_SPLIT);
+    return launched(c, launch_split(c, (const float2 *)u, rho, (float2 *)rhs, alpha, st), "split");
 }
 
 extern "C" int nlse_nonlinear_step(nlse_ctx *c, void *u, const float *rho, double dz, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
     if (!(dz > 0) || !isfinite(dz)) return bad(c, NLSE_ERR_INVALID_ARG, "dz must be positive and finite");
-    return launched(c, launch_nonlinear_step(c, (float2 *)u, rho, (float)dz, (cudaStream_t)stream),
-                    "nonlinear step");
+    cudaStream_t st = (cudaStream_t)stream;
+    PROF(K_NONLINEAR);
+    return launched(c, launch_nonlinear_step(c, (float2 *)u, rho, (float)dz, st), "nonlinear step");
 }
 
 extern "C" int nlse_update_plasma(nlse_ctx *c, const void *u, float *rho, float *rho_s, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
-    return launched(c, launch_rate_scan(c, (const float2 *)u, rho, rho_s, 1, (cudaStream_t)stream),
-                    "rate scan");
+    cudaStream_t st = (cudaStream_t)stream;
+    PROF(K_RATE_SCAN);
+    return launched(c, launch_rate_scan(c, (const float2 *)u, rho, rho_s, 1, st), "rate scan");
 }
 
 static int step_plain(nlse_ctx *c, float2 *u, const float *rho, double dz, cudaStream_t st) {
     int s = half_linear_impl(c, u, dz, nullptr, st);
     if (s) return s;
-    s = launched(c, launch_nonlinear_step(c, u, rho, (float)dz, st), "nonlinear step");
+    {
+        PROF(K_NONLINEAR);
+        s = launched(c, launch_nonlinear_step(c, u, rho, (float)dz, st), "nonlinear step");
+    }
     if (s) return s;
     return half_linear_impl(c, u, dz, c->d_mask_r, st);
 }
@@ -344,7 +389,11 @@ extern "C" int nlse_propagate(nlse_ctx *c, void *u, float *rho, float *rho_s, do
     if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_UNSUPPORTED, "mode not available in this build");
     cudaStream_t st = (cudaStream_t)stream;
     for (int i = 0; i < nsteps; ++i) {
-        int s = launched(c, launch_rate_scan(c, (const float2 *)u, rho, rho_s, 1, st), "rate scan");
+        int s;
+        {
+            PROF(K_RATE_SCAN);
+            s = launched(c, launch_rate_scan(c, (const float2 *)u, rho, rho_s, 1, st), "rate scan");
+        }
         if (s) return s;
         s = step_plain(c, (float2 *)u, rho, dz, st);
         if (s) return s;
@@ -358,4 +407,55 @@ extern "C" int nlse_scan_fallback_rows(nlse_ctx *c, int *out) {
     NLSE_CUDA_TRY(&c->err, cudaMemcpy(h, c->d_flag, sizeof(h), cudaMemcpyDeviceToHost));
     *out = h[1];
     return NLSE_OK;
+}
+
+// ---------------------------------------------------------------- profiling
+extern "C" int nlse_profile_start(nlse_ctx *c, int capacity) {
+    if (!c || capacity < 1) return NLSE_ERR_INVALID_ARG;
+    prof_free(c);
+    c->prof_ev = (cudaEvent_t *)calloc(2 * (size_t)capacity, sizeof(cudaEvent_t));
+    c->prof_kid = (int *)calloc(capacity, sizeof(int));
+    if (!c->prof_ev || !c->prof_kid) {
+        prof_free(c);
+        return bad(c, NLSE_ERR_INVALID_ARG, "out of host memory for profiling records");
+    }
+    c->prof_cap = capacity;
+    for (int i = 0; i < 2 * capacity; ++i) NLSE_CUDA_TRY(&c->err, cudaEventCreate(&c->prof_ev[i]));
+    c->prof_n = 0;
+    c->prof_on = 1;
+    return NLSE_OK;
+}
+
+extern "C" int nlse_profile_read(nlse_ctx *c, int *launches, double *total_ms, int nkinds, int *dropped) {
+    if (!c || !launches || !total_ms || nkinds < 1) return NLSE_ERR_INVALID_ARG;
+    for (int k = 0; k < nkinds; ++k) {
+        launches[k] = 0;
+        total_ms[k] = 0.0;
+    }
+    if (dropped) *dropped = 0;
+    if (!c->prof_ev) return NLSE_OK;
+    if (c->prof_n > 0) NLSE_CUDA_TRY(&c->err, cudaEventSynchronize(c->prof_ev[2 * c->prof_n - 1]));
+    for (int i = 0; i < c->prof_n; ++i) {
+        float ms = 0.0f;
+        NLSE_CUDA_TRY(&c->err, cudaEventElapsedTime(&ms, c->prof_ev[2 * i], c->prof_ev[2 * i + 1]));
+        int k = c->prof_kid[i];
+        if (k < nkinds) {
+            launches[k] += 1;
+            total_ms[k] += ms;
+        }
+    }
+    c->prof_on = 0;
+    return NLSE_OK;
+}
+
+extern "C" const char *nlse_kernel_name(int kid) {
+    switch (kid) {
+        case K_RATE_SCAN: return "k_rate_scan";
+        case K_GEMM_F32: return "k_gemm_f32";
+        case K_FFT_PHASE: return "k_fft_phase_ifft";
+        case K_NONLINEAR: return "k_nonlinear_step";
+        case K_SPLIT: return "k_split";
+        case K_PHASE_TABLES: return "k_phase_tables";
+        default: return "";
+    }
 }

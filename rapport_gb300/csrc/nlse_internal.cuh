@@ -79,6 +79,21 @@ struct nlse_ctx {
     // workspace
     float2 *d_work;        // Nr*Nt complex64
     int *d_flag;           // device status word
+    // per-launch event profiling (off unless nlse_profile_start was called)
+    int prof_on, prof_cap, prof_n;
+    cudaEvent_t *prof_ev;  // 2 * prof_cap events
+    int *prof_kid;         // kernel id per record
+};
+
+// kernel ids for the profiler (names in nlse_kernel_name)
+enum {
+    K_RATE_SCAN = 0,
+    K_GEMM_F32 = 1,
+    K_FFT_PHASE = 2,
+    K_NONLINEAR = 3,
+    K_SPLIT = 4,
+    K_PHASE_TABLES = 5,
+    K_NUM_KINDS = 16
 };
 
 // ---------------------------------------------------------------- launchers

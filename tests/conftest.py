@@ -20,6 +20,11 @@ def load_golden(name):
 
 @pytest.fixture(scope="session")
 def tiny():
+    return load_golden("tiny.npz")
+
+
+@pytest.fixture(scope="session")
+def hot():
     return load_golden("tiny_hot.npz")
 
 

@@ -34,16 +34,19 @@ def test_half_linear_is_linear(c2):
     assert rel_l2(huv, a * hu + b * hv) < 1e-5
 
 
-def test_half_linear_conserves_energy_of_smooth_pulse(c2):
-    # spectral mask ~ 1 over the pulse band and no absorber inside half_linear:
-    # the QDHT-weighted energy sum |u|^2 / J1(j_k)^2 is invariant
+def test_half_linear_energy_balance_matches_oracle(c2):
+    # the QDHT-weighted energy sum |u|^2 / J1(j_k)^2 changes only through the
+    # spectral band mask (it removes the out-of-band part of the 1 % noise:
+    # -2.65e-5 here); the GPU must lose exactly what the FP64 oracle loses
     from scipy.special import j1
     w = 1.0 / j1(c2.og.jz[:c2.og.Nr]) ** 2
     u = c2.u0
     h = host(c2.lin.half_linear(dev(u), c2.dz))
+    ho = c2.og.half_linear(u, c2.dz)
     e0 = np.sum(np.abs(u) ** 2 * w[:, None])
-    e1 = np.sum(np.abs(h) ** 2 * w[:, None])
-    assert abs(e1 / e0 - 1) < 1e-5
+    d_gpu = np.sum(np.abs(h) ** 2 * w[:, None]) / e0 - 1
+    d_ref = np.sum(np.abs(ho) ** 2 * w[:, None]) / e0 - 1
+    assert abs(d_gpu - d_ref) < 1e-6
 
 
 def test_carrier_density_monotone_without_recombination(c2):

@@ -3,7 +3,10 @@
 Tolerances (FP32 arithmetic against FP64):
   half_linear / split / nonlinear block : relative L2 <= 2e-5
   carrier densities                     : max |diff| <= 2e-4 * row peak (Newton scan, FP32)
-  full z-steps                          : relative L2 <= 1e-4 after 10 strongly ionising steps
+  full z-steps                          : relative L2 <= 1e-4 after 10 ionising steps
+The 5 uJ 'hot' fixture (66 % of rho_nt ionised) checks the carrier march and
+split() only: the reference's own RK4 is unstable at that density (plasma
+phase ~100 rad per step), so a propagation there has no meaningful parity.
 """
 import numpy as np
 import pytest
@@ -25,13 +28,19 @@ def c1_case(cfg1):
     return Case.from_fixture(cfg1)
 
 
-def _case(name, tiny_case, c1_case):
-    return tiny_case if name == "tiny" else c1_case
+@pytest.fixture(scope="module")
+def hot_case(hot):
+    return Case.from_fixture(hot)
+
+
+@pytest.fixture(scope="module")
+def cases(tiny_case, c1_case, hot_case):
+    return {"tiny": tiny_case, "cfg1": c1_case, "hot": hot_case}
 
 
 @pytest.mark.parametrize("name", ["tiny", "cfg1"])
-def test_half_linear(name, tiny_case, c1_case):
-    c = _case(name, tiny_case, c1_case)
+def test_half_linear(name, cases):
+    c = cases[name]
     out = host(c.lin.half_linear(dev(c.u0), c.dz))
     ref = c.og.half_linear(c.u0, c.dz)
     assert rel_l2(out, ref) < 2e-5
@@ -42,9 +51,9 @@ def test_half_linear_matches_reference_fixture(tiny, tiny_case):
     assert rel_l2(out[tiny["rows"]], tiny["hl_u0"]) < 2e-5
 
 
-@pytest.mark.parametrize("name", ["tiny", "cfg1"])
-def test_update_plasma(name, tiny_case, c1_case):
-    c = _case(name, tiny_case, c1_case)
+@pytest.mark.parametrize("name", ["tiny", "hot", "cfg1"])
+def test_update_plasma(name, cases):
+    c = cases[name]
     rho_o = np.zeros(c.u0.shape)
     c.og.update_plasma(c.u0, rho_o, np.zeros(c.u0.shape))
     rho = dev(np.full(c.u0.shape, 7.0))
@@ -57,9 +66,9 @@ def test_update_plasma(name, tiny_case, c1_case):
     assert np.all(r[:, 0] == 0.0)
 
 
-@pytest.mark.parametrize("name", ["tiny", "cfg1"])
-def test_split(name, tiny_case, c1_case):
-    c = _case(name, tiny_case, c1_case)
+@pytest.mark.parametrize("name", ["tiny", "hot", "cfg1"])
+def test_split(name, cases):
+    c = cases[name]
     u = c.og.half_linear(c.u0, c.dz)
     rho = np.zeros(u.shape)
     c.og.update_plasma(c.u0, rho, np.zeros(u.shape))
@@ -69,17 +78,19 @@ def test_split(name, tiny_case, c1_case):
     assert rel_l2(host(al), al_o) < 2e-5
 
 
-def test_split_matches_reference_fixture(tiny, tiny_case):
+@pytest.mark.parametrize("name", ["tiny", "hot"])
+def test_split_matches_reference_fixture(name, tiny, hot, cases):
     # the fixture's split was taken on half_linear(u0) with rho from update_plasma(u0)
-    u = tiny_case.og.half_linear(tiny_case.u0, tiny_case.dz)
-    rhs, al = tiny_case.nl.split(dev(u), dev(tiny["rho_u0"]))
-    assert rel_l2(host(rhs), tiny["split_rhs"]) < 2e-5
-    assert rel_l2(host(al), tiny["split_alpha"]) < 2e-5
+    d, c = (tiny if name == "tiny" else hot), cases[name]
+    u = c.og.half_linear(c.u0, c.dz)
+    rhs, al = c.nl.split(dev(u), dev(d["rho_u0"]))
+    assert rel_l2(host(rhs), d["split_rhs"]) < 2e-5
+    assert rel_l2(host(al), d["split_alpha"]) < 2e-5
 
 
 @pytest.mark.parametrize("name", ["tiny", "cfg1"])
-def test_nonlinear_block(name, tiny_case, c1_case):
-    c = _case(name, tiny_case, c1_case)
+def test_nonlinear_block(name, cases):
+    c = cases[name]
     u = c.og.half_linear(c.u0, c.dz)
     rho = np.zeros(u.shape)
     c.og.update_plasma(c.u0, rho, np.zeros(u.shape))
@@ -90,9 +101,9 @@ def test_nonlinear_block(name, tiny_case, c1_case):
 
 
 @pytest.mark.parametrize("name,tol", [("tiny", 1e-4), ("cfg1", 2e-5)])
-def test_z_steps_match_reference_fixture(name, tol, tiny, cfg1, tiny_case, c1_case):
+def test_z_steps_match_reference_fixture(name, tol, tiny, cfg1, cases):
     d = tiny if name == "tiny" else cfg1
-    c = _case(name, tiny_case, c1_case)
+    c = cases[name]
     u = dev(c.u0)
     rho = dev(np.zeros(c.u0.shape))
     rs = dev(np.zeros(c.u0.shape))

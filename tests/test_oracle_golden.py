@@ -28,9 +28,9 @@ def test_grid_tables_match_reference(tiny):
         assert getattr(g, k) == pytest.approx(float(tiny[k]), rel=1e-13), k
 
 
-@pytest.mark.parametrize("name", ["tiny", "cfg1"])
-def test_envelope_and_operators(name, tiny, cfg1):
-    d = tiny if name == "tiny" else cfg1
+@pytest.mark.parametrize("name", ["tiny", "hot", "cfg1"])
+def test_envelope_and_operators(name, tiny, hot, cfg1):
+    d = {"tiny": tiny, "hot": hot, "cfg1": cfg1}[name]
     g, m = _grid(d)
     rows = d["rows"]
     u0 = O.lens_gaussian(g, m["w0"], m["fwhm"], m["E"], m["f"], m["seed"])
