@@ -53,7 +53,7 @@ __device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p
     if (p.photo_on) {
         float I = a2 * p.invE2;
         if (isfinite(I)) {
-            float dep = fminf(fmaxf(1.0f - rho * p.inv_rho_max, 0.0f), 1.0f);
+            float dep = fminf(fmaxf((p.rho_max - rho) * p.inv_rho_max, 0.0f), 1.0f);
             photo = photo_rate(I, p, tab) * dep;
         } else if (isnan(I)) {
             photo = I;  // NaN: split() turns the sum into alpha = 0 (nan_to_num)

@@ -52,7 +52,8 @@ __device__ __forceinline__ float lut_rate_dt(float I, const float *__restrict__ 
 // One step of the march and its derivative d f / d x.
 __device__ __forceinline__ float step_map(float x, float a, float b, const ScanParams &p, float *J,
                                           bool *clamped) {
-    float d = fminf(fmaxf(1.0f - x * p.inv_na, 0.0f), 1.0f);
+    // (na - x) is exact near saturation, so d is exactly 0 at x = na as in FP64
+    float d = fminf(fmaxf((p.na - x) * p.inv_na, 0.0f), 1.0f);
     float z = fmaf(a, d, -p.c_rec);
     if (z > 80.0f) {
         // e^z overflows FP32 but not FP64 (below z = 709.78): there the reference

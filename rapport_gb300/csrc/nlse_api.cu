@@ -150,6 +150,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     nl.kp = (d->flags & NLSE_F_KERR_INSTANT) ? (float)(d->kerr_pref * d->kerr_scale) : 0.0f;
     nl.pp_abs = (d->flags & NLSE_F_PLASMA_ABSORB) ? (float)d->plasma_pref : 0.0f;
     nl.pp_def = (d->flags & NLSE_F_PLASMA_DEFOC) ? (float)(d->plasma_pref * d->omega0_tau_c) : 0.0f;
+    nl.rho_max = (float)d->rho_max;
     nl.inv_rho_max = (float)(1.0 / d->rho_max);
     nl.photo_on = (d->flags & NLSE_F_PHOTO_LOSS) ? 1 : 0;
     nl.Imin = (float)d->pchip_x[0];

@@ -36,6 +36,7 @@ struct NLParams {
     float kp;           // kerr_pref * kerr_scale (0 if instantaneous Kerr off)
     float pp_abs;       // plasma_pref if absorption on else 0
     float pp_def;       // plasma_pref * w0 tau_c if defocusing on else 0
+    float rho_max;      // rho_nt
     float inv_rho_max;  // 1 / rho_max
     int photo_on;       // photo-ionisation loss on
     float Imin, Imax;   // spline clip range
