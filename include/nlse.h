@@ -115,6 +115,11 @@ int nlse_create(const nlse_grid_desc *desc, nlse_ctx **out);
 /* u <- half_linear(u, dz): iRk Y F^-1[e^{i phi} mask F(Rk Y u)], in place. */
 int nlse_half_linear(nlse_ctx *ctx, void *u, double dz, void *stream);
 
+/* half_linear with an explicit arithmetic: NLSE_MODE_PLAIN_F32 (reference
+ * order: two FP32 Hankel products around the FFT pair) or NLSE_MODE_SPLIT_BF16
+ * (one tcgen05 product with the merged operator Y diag(P_r) Y = I + E). */
+int nlse_half_linear_ex(nlse_ctx *ctx, void *u, double dz, int mode, void *stream);
+
 /* (rhs, alpha) <- split(u, rho): RK right-hand side and absorption rate.
  * rhs: complex64 Nr x Nt, alpha: float32 Nr x Nt (may be NULL). */
 int nlse_split(nlse_ctx *ctx, const void *u, const float *rho, void *rhs,
@@ -140,6 +145,20 @@ int nlse_step(nlse_ctx *ctx, void *u, const float *rho, const float *rho_s,
  * the field entering that step), exactly as after the reference loop. */
 int nlse_propagate(nlse_ctx *ctx, void *u, float *rho, float *rho_s, double dz,
                    int nsteps, int mode, void *stream);
+
+/* Diagnostic: out = E' w for a planar FP32 field w (2Nr x Nt: Re rows then
+ * Im rows) through the tcgen05 product alone, E' = [[Re E, -Im E], [Im E, Re E]]
+ * with E = Y diag(e^{-i rho^2 dz / 4k0}) Y - I.  out: 2Nr x Nt FP32. */
+int nlse_debug_operator_product(nlse_ctx *ctx, const float *w, float *out, double dz,
+                                void *stream);
+
+/* Number of BF16 terms carrying E in the split mode: 3 (default; 4 MMAs per
+ * k-slice) or 2 (the plain hi/lo scheme, 3 MMAs). */
+int nlse_set_split_terms(nlse_ctx *ctx, int a_terms);
+
+/* Synchronise and read the device status word: NLSE_ERR_TIMEOUT if a kernel
+ * gave up a bounded wait since nlse_create (word receives the raw bits). */
+int nlse_device_status(nlse_ctx *ctx, int *word);
 
 /* Number of (row, call) pairs the carrier scan has re-marched sequentially
  * since nlse_create (saturated or non-converging rows); synchronous read. */

@@ -18,8 +18,9 @@ F_KERR_RAMAN, F_SELF_STEEP, F_SPACE_TIME, F_STE = 16, 32, 64, 128
 MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 
 # every symbol include/nlse.h declares (checked by the CPU test suite)
-EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_split", "nlse_nonlinear_step",
-           "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_scan_fallback_rows",
+EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
+           "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
+           "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
            "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
            "nlse_get_last_error", "nlse_destroy", "nlse_version")
 
@@ -55,6 +56,10 @@ def load():
     lib = ctypes.CDLL(LIB_PATH)
     lib.nlse_create.argtypes = [ctypes.POINTER(GridDesc), ctypes.POINTER(_P)]
     lib.nlse_half_linear.argtypes = [_P, _P, _D, _P]
+    lib.nlse_half_linear_ex.argtypes = [_P, _P, _D, _I, _P]
+    lib.nlse_set_split_terms.argtypes = [_P, _I]
+    lib.nlse_debug_operator_product.argtypes = [_P, _P, _P, _D, _P]
+    lib.nlse_device_status.argtypes = [_P, ctypes.POINTER(_I)]
     lib.nlse_split.argtypes = [_P, _P, _P, _P, _P, _P]
     lib.nlse_nonlinear_step.argtypes = [_P, _P, _P, _D, _P]
     lib.nlse_update_plasma.argtypes = [_P, _P, _P, _P, _P]
@@ -204,8 +209,26 @@ class Context:
         return self._field(t, name, torch.float32)
 
     # ---------------------------------------------------------- ops
-    def half_linear(self, u, dz):
-        _check(self.lib, self.h, self.lib.nlse_half_linear(self.h, self._field(u, "u"), float(dz), self._stream()))
+    def half_linear(self, u, dz, mode=MODE_PLAIN_F32):
+        _check(self.lib, self.h, self.lib.nlse_half_linear_ex(self.h, self._field(u, "u"), float(dz), int(mode),
+                                                              self._stream()))
+
+    def debug_operator_product(self, w, out, dz):
+        """out = E' w (planar FP32, 2Nr x Nt) through the tensor-core product alone."""
+        import torch
+        for t, nm in ((w, "w"), (out, "out")):
+            if t.dtype != torch.float32 or tuple(t.shape) != (2 * self.Nr, self.Nt) or not t.is_contiguous():
+                raise ValueError(f"{nm} must be a contiguous float32 tensor of shape {(2 * self.Nr, self.Nt)}")
+        _check(self.lib, self.h, self.lib.nlse_debug_operator_product(
+            self.h, ctypes.c_void_p(w.data_ptr()), ctypes.c_void_p(out.data_ptr()), float(dz), self._stream()))
+
+    def set_split_terms(self, n):
+        _check(self.lib, self.h, self.lib.nlse_set_split_terms(self.h, int(n)))
+
+    def device_status(self):
+        w = _I(0)
+        _check(self.lib, self.h, self.lib.nlse_device_status(self.h, ctypes.byref(w)))
+        return w.value
 
     def split(self, u, rho, rhs, alpha):
         a = self._rho(alpha, "alpha") if alpha is not None else None

@@ -1,0 +1,374 @@
+// Split-BF16 tcgen05 GEMM for the merged linear operator, and its builder.
+//
+// The reference's linear half step (operators.py:47-53) is
+//     iRk Y ifft_t( e^{i phi} mask fft_t( Rk Y u ) ),   phi = dk(W) dz/2 - rho_m^2 dz/(4 k0)
+// with two real Nr x Nr QDHT products around an FFT pair.  Y acts on r and the
+// FFT on t, so they commute, and the radial phase diag(P_r) is diagonal in the
+// Hankel basis: the half step is
+//     F^-1[ P_t . (M F[u]) ],   M = Y diag(P_r) Y = I + E     (Rk iRk = 1).
+// M is one complex Nr x Nr matrix per dz.  In the Omega domain the field is
+// stored planar, w' = [Re w; Im w] (2 Nr x Nt), and
+//     E' = [[Re E, -Im E], [Im E, Re E]]      (2 Nr x 2 Nr, real)
+// so E' w' is ONE real GEMM of M = K = 2 Nr, N = Nt (8 Nr^2 Nt flops, the same
+// as the reference's two complex-promoted products counted as real work).
+// The identity part of M is added exactly in FP32 by the row kernel that
+// consumes the product; only E -- |E| <= 0.15, typically |E w| ~ 1e-3 |w| --
+// goes through the tensor cores.
+//
+// Precision: E' is split into three BF16 terms (h + m + l, ~24 bits) and the
+// field into two (h + l, ~16 bits); the MMAs Eh.wh + Eh.wl + Em.wh + El.wh
+// accumulate in FP32 in TMEM (A_TERMS = 3; A_TERMS = 2 drops El.wh: the plain
+// hi/lo 3-MMA scheme).  E's own rounding is systematic and would accumulate
+// over thousands of steps; carrying it in three terms removes that drift.
+//
+// Kernel: one 128 x 256 output tile per CTA; warp 0 = TMA producer, warp 1 =
+// TMEM allocator + MMA issuer (one elected thread), warps 2-5 = epilogue
+// (tcgen05.ld of their 32-lane TMEM quadrant, FP32 rows to global).  Operands
+// are staged by TMA (128-byte swizzle) into a 2-stage mbarrier pipeline:
+// A tiles K-major (box 64 x 128), B tiles MN-major (4 boxes of 64 x 64).
+// Every wait is bounded by %globaltimer; on timeout the kernel raises an
+// error word, drains what it issued, frees TMEM and returns.
+#include <cuda.h>
+
+#include "nlse_internal.cuh"
+
+#define TC_BM 128
+#define TC_BN 256
+#define TC_BK 64
+#define TC_STAGES 2
+#define TC_THREADS 192
+#define TC_WAIT_NS 2000000000ull
+
+namespace {
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t global_ns() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)), "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Wait for the phase with the given parity to complete; false after ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+    if (mbar_try_wait(bar, parity)) return true;
+    const uint64_t t0 = global_ns();
+    for (uint32_t i = 1;; ++i) {
+        if (mbar_try_wait(bar, parity)) return true;
+        if ((i & 255u) == 0 && global_ns() - t0 > TC_WAIT_NS) return false;
+    }
+}
+
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, uint64_t *bar, int x, int y) {
+    asm volatile(
+        "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+        ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+        : "memory");
+}
+
+// Shared-memory matrix descriptor (tcgen05): start, leading/stride byte
+// offsets (>> 4), version 1, 128-byte swizzle.
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+    uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
+    d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
+    d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
+    d |= (uint64_t)1 << 46;
+    d |= (uint64_t)2 << 61;
+    return d;
+}
+
+__device__ __forceinline__ void umma_bf16(uint32_t d_tmem, uint64_t adesc, uint64_t bdesc, uint32_t idesc,
+                                          uint32_t accumulate) {
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "setp.ne.b32 p, %4, 0;\n\t"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}"
+        ::"r"(d_tmem), "l"(adesc), "l"(bdesc), "r"(idesc), "r"(accumulate)
+        : "memory");
+}
+
+__device__ __forceinline__ void umma_commit(uint64_t *bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+                     smem_u32(bar))
+                 : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 "
+        "{%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]),
+          "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]),
+          "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]),
+          "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+}  // namespace
+
+// Instruction descriptor, kind::f16: FP32 accumulate, BF16 A and B, A K-major,
+// B MN-major, N = 256, M = 128.
+constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((uint32_t)(TC_BN >> 3) << 17) |
+                            ((uint32_t)(TC_BM >> 4) << 24);
+
+template <int A_TERMS>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+          float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
+    constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;  // one term, 16 KB
+    constexpr uint32_t B_BYTES = TC_BK * TC_BN * 2;  // one term, 32 KB
+    constexpr uint32_t B_BOX = 64 * TC_BK * 2;       // one 64-column box, 8 KB
+    constexpr uint32_t STAGE = A_TERMS * A_BYTES + 2 * B_BYTES;
+    extern __shared__ uint8_t smem_raw[];
+    uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+    __shared__ __align__(8) uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], acc_bar;
+    __shared__ uint32_t tmem_base;
+    __shared__ int abort_flag, issued;
+
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n_tiles = N / TC_BN;
+    const int m0 = (blockIdx.x / n_tiles) * TC_BM, n0 = (blockIdx.x % n_tiles) * TC_BN;
+    const int KB = K / TC_BK;
+
+    if (threadIdx.x == 0) {
+        for (int s = 0; s < TC_STAGES; ++s) {
+            mbar_init(&full_bar[s], 1);
+            mbar_init(&empty_bar[s], 1);
+        }
+        mbar_init(&acc_bar, 1);
+        abort_flag = 0;
+        issued = 0;
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    if (warp == 1) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&tmem_base)),
+                     "r"(TC_BN));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = tmem_base;
+
+    if (warp == 0 && lane == 0) {
+        // ------------------------------------------------ TMA producer
+        for (int kb = 0; kb < KB; ++kb) {
+            const int s = kb % TC_STAGES;
+            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            if (!mbar_wait(&empty_bar[s], ph ^ 1u) || *(volatile int *)&abort_flag) {
+                atomicOr(err, 1);
+                abort_flag = 1;
+                break;
+            }
+            uint8_t *st = smem + (size_t)s * STAGE;
+            mbar_expect_tx(&full_bar[s], STAGE);
+#pragma unroll
+            for (int t = 0; t < A_TERMS; ++t) tma_load_2d(st + t * A_BYTES, &tmA, &full_bar[s], kb * TC_BK, t * M + m0);
+#pragma unroll
+            for (int t = 0; t < 2; ++t)
+#pragma unroll
+                for (int j = 0; j < TC_BN / 64; ++j)
+                    tma_load_2d(st + A_TERMS * A_BYTES + t * B_BYTES + j * B_BOX, &tmB, &full_bar[s], n0 + 64 * j,
+                                t * K + kb * TC_BK);
+            issued = kb + 1;
+        }
+    } else if (warp == 1 && lane == 0) {
+        // ------------------------------------------------ MMA issuer
+        // term pairs (a, b): Eh.wh, Eh.wl, Em.wh [, El.wh]
+        const int pa[4] = {0, 0, 1, 2}, pb[4] = {0, 1, 0, 0};
+        constexpr int NPAIR = A_TERMS == 3 ? 4 : 3;
+        for (int kb = 0; kb < KB; ++kb) {
+            const int s = kb % TC_STAGES;
+            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
+            if (!mbar_wait(&full_bar[s], ph) || *(volatile int *)&abort_flag) {
+                atomicOr(err, 2);
+                abort_flag = 1;
+                break;
+            }
+            tc_fence_after();
+            const uint32_t a0 = smem_u32(smem + (size_t)s * STAGE);
+            const uint32_t b0 = a0 + A_TERMS * A_BYTES;
+#pragma unroll
+            for (int kk = 0; kk < TC_BK / 16; ++kk) {
+#pragma unroll
+                for (int p = 0; p < NPAIR; ++p) {
+                    const uint64_t ad = smem_desc(a0 + pa[p] * A_BYTES + kk * 32, 16, 1024);
+                    const uint64_t bd = smem_desc(b0 + pb[p] * B_BYTES + kk * 2048, B_BOX, 1024);
+                    umma_bf16(tmem, ad, bd, kIdesc, (kb | kk | p) != 0);
+                }
+            }
+            umma_commit(&empty_bar[s]);
+        }
+        umma_commit(&acc_bar);  // always: the epilogue / teardown waits on it
+    } else if (warp >= 2) {
+        // ------------------------------------------------ epilogue
+        const int q = warp & 3;
+        const bool ok = mbar_wait(&acc_bar, 0);
+        if (!ok) atomicOr(err, 4);
+        if (ok && !*(volatile int *)&abort_flag) {
+            tc_fence_after();
+            float *row = D + (size_t)(m0 + q * 32 + lane) * N + n0;
+#pragma unroll 1
+            for (int c = 0; c < TC_BN / 32; ++c) {
+                uint32_t r[32];
+                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), r);
+                float4 *dst = reinterpret_cast<float4 *>(row + c * 32);
+#pragma unroll
+                for (int v = 0; v < 8; ++v)
+                    dst[v] = make_float4(__uint_as_float(r[4 * v]), __uint_as_float(r[4 * v + 1]),
+                                         __uint_as_float(r[4 * v + 2]), __uint_as_float(r[4 * v + 3]));
+            }
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (abort_flag && threadIdx.x == 0) {
+        // drain: the last loads this CTA issued must land before it exits
+        for (int kb = issued - TC_STAGES; kb < issued; ++kb)
+            if (kb >= 0) mbar_wait(&full_bar[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u);
+    }
+    if (warp == 1) {
+        if (abort_flag && lane == 0) mbar_wait(&acc_bar, 0);  // MMAs done before TMEM is released
+        __syncwarp();
+        tc_fence_after();
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+    }
+}
+
+static size_t tc_smem_bytes(int a_terms) {
+    return (size_t)TC_STAGES * (a_terms * TC_BM * TC_BK * 2 + 2 * TC_BK * TC_BN * 2) + 1024;
+}
+
+cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
+                           int a_terms, int *err, cudaStream_t stream) {
+    if (M % TC_BM || N % TC_BN || K % TC_BK) return cudaErrorInvalidValue;
+    const dim3 grid((M / TC_BM) * (N / TC_BN));
+    const size_t smem = tc_smem_bytes(a_terms);
+    cudaError_t e;
+    if (a_terms == 3) {
+        e = cudaFuncSetAttribute(k_gemm_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gemm_tc<3><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
+    } else {
+        e = cudaFuncSetAttribute(k_gemm_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gemm_tc<2><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
+    }
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ operator builder (FP64)
+// Er + i Ei = Y diag(e^{i theta}) Y - I,  theta_k = -rho_k^2 dz / (4 k0).
+// 32 x 32 output tiles, 16-deep k slices through shared memory; each thread
+// accumulates a 2 x 2 block of (Er, Ei) pairs.  Runs once per dz.
+__global__ void __launch_bounds__(256)
+k_build_E(const double *__restrict__ Y, const double *__restrict__ rho, int Nr, double dz, double komega,
+          double *__restrict__ Er, double *__restrict__ Ei) {
+    __shared__ double As[32][17], Bc[16][33], Bs[16][33];
+    const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+    const int row0 = blockIdx.y * 32, col0 = blockIdx.x * 32;
+    double ar[2][2] = {{0, 0}, {0, 0}}, ai[2][2] = {{0, 0}, {0, 0}};
+    for (int k0 = 0; k0 < Nr; k0 += 16) {
+        for (int i = threadIdx.x; i < 32 * 16; i += 256) {
+            int r = i / 16, k = i % 16;
+            int gr = row0 + r, gk = k0 + k;
+            As[r][k] = (gr < Nr && gk < Nr) ? Y[(size_t)gr * Nr + gk] : 0.0;
+        }
+        for (int i = threadIdx.x; i < 16 * 32; i += 256) {
+            int k = i / 32, cc = i % 32;
+            int gk = k0 + k, gc = col0 + cc;
+            double y = (gk < Nr && gc < Nr) ? Y[(size_t)gk * Nr + gc] : 0.0;
+            double s = 0.0, c = 0.0;
+            if (gk < Nr) {
+                double rr = rho[gk];
+                sincos(-rr * rr * dz / (4.0 * komega), &s, &c);
+            }
+            Bc[k][cc] = c * y;
+            Bs[k][cc] = s * y;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int k = 0; k < 16; ++k) {
+#pragma unroll
+            for (int i = 0; i < 2; ++i) {
+                double a = As[ty * 2 + i][k];
+#pragma unroll
+                for (int j = 0; j < 2; ++j) {
+                    ar[i][j] = fma(a, Bc[k][tx * 2 + j], ar[i][j]);
+                    ai[i][j] = fma(a, Bs[k][tx * 2 + j], ai[i][j]);
+                }
+            }
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int i = 0; i < 2; ++i)
+#pragma unroll
+        for (int j = 0; j < 2; ++j) {
+            int r = row0 + ty * 2 + i, cc = col0 + tx * 2 + j;
+            if (r < Nr && cc < Nr) {
+                Er[(size_t)r * Nr + cc] = ar[i][j] - (r == cc ? 1.0 : 0.0);
+                Ei[(size_t)r * Nr + cc] = ai[i][j];
+            }
+        }
+}
+
+// E' = [[Er, -Ei], [Ei, Er]] split into a_terms BF16 terms, stacked as
+// A[t][2Nr][2Nr] (term-major): h = bf16(v), m = bf16(v - h), l = bf16(v - h - m).
+__global__ void k_split_E(const double *__restrict__ Er, const double *__restrict__ Ei, int Nr, int a_terms,
+                          __nv_bfloat16 *__restrict__ A) {
+    const size_t K2 = 2 * (size_t)Nr;
+    const size_t total = K2 * K2;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t m = i / K2, k = i % K2;
+        size_t mr = m % Nr, kr = k % Nr;
+        bool mi = m >= (size_t)Nr, ki = k >= (size_t)Nr;
+        double v = (mi == ki) ? Er[mr * Nr + kr] : (mi ? Ei[mr * Nr + kr] : -Ei[mr * Nr + kr]);
+        double rem = v;
+        for (int t = 0; t < a_terms; ++t) {
+            __nv_bfloat16 b = __double2bfloat16(rem);
+            A[(size_t)t * total + i] = b;
+            rem -= (double)__bfloat162float(b);
+        }
+    }
+}
+
+cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
+                                  double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, cudaStream_t stream) {
+    dim3 grid((Nr + 31) / 32, (Nr + 31) / 32);
+    k_build_E<<<grid, 256, 0, stream>>>(Y64, rho, Nr, dz, komega, Er, Ei);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_split_E<<<1024, 256, 0, stream>>>(Er, Ei, Nr, a_terms, A);
+    return cudaGetLastError();
+}

@@ -20,83 +20,7 @@
 // the interval index is computed in closed form; each interval stores the
 // Hermite cubic in s = (I - x_i)/h_i pre-scaled by Kc*invE2/x_i, which keeps
 // every FP32 intermediate in range (W alone reaches 1e52 at Imax).
-#include "nlse_internal.cuh"
-
-__constant__ float c_pow10[18] = {1e0f,  1e1f,  1e2f,  1e3f,  1e4f,  1e5f,  1e6f,  1e7f,  1e8f,
-                                  1e9f,  1e10f, 1e11f, 1e12f, 1e13f, 1e14f, 1e15f, 1e16f, 1e17f};
-
-// photo-ionisation loss rate [1/m] before depletion, for a finite I >= 0.
-__device__ __forceinline__ float photo_rate(float I, const NLParams &p, const float4 *__restrict__ tab) {
-    float Ic = fminf(fmaxf(I, p.Imin), p.Imax);
-    int d = (int)floorf(log10f(Ic));
-    d = min(max(d, 0), 16);
-    if (Ic < c_pow10[d] && d > 0) --d;
-    else if (Ic >= c_pow10[d + 1] && d < 16) ++d;
-    int m = (int)((Ic / c_pow10[d] - 1.0f) * 100.0f);
-    m = min(max(m, 0), 899);
-    int i = min(900 * d + m, p.n_int - 1);
-    d = i / 900;
-    m = i - 900 * d;
-    const float p10 = c_pow10[d];
-    const float xi = p10 * (1.0f + 0.01f * (float)m);
-    const float s = (Ic - xi) / (0.01f * p10);
-    const float4 cf = __ldg(&tab[i]);
-    float V = fabsf(fmaf(s, fmaf(s, fmaf(s, cf.w, cf.z), cf.y), cf.x));
-    float r = V * (xi / (I + p.tiny_I));
-    return isfinite(r) ? r : 0.0f;
-}
-
-// alpha(u, rho) and the raw sum it clamps, as split() computes them.
-__device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p,
-                                          const float4 *__restrict__ tab, float *raw) {
-    float photo = 0.0f;
-    if (p.photo_on) {
-        float I = a2 * p.invE2;
-        if (isfinite(I)) {
-            float dep = fminf(fmaxf((p.rho_max - rho) * p.inv_rho_max, 0.0f), 1.0f);
-            photo = photo_rate(I, p, tab) * dep;
-        } else if (isnan(I)) {
-            photo = I;  // NaN: split() turns the sum into alpha = 0 (nan_to_num)
-        }             // +Inf: W(Imax) / Inf = 0 in split()
-    }
-    float ar = photo + p.pp_abs * rho;
-    *raw = ar;
-    return isfinite(ar) ? fmaxf(ar, 0.0f) : 0.0f;
-}
-
-// RK right-hand side of split() for one point; rho frozen.
-__device__ __forceinline__ float2 nl_rhs(float2 u, float rho, const NLParams &p,
-                                         const float4 *__restrict__ tab) {
-    float a2 = fmaf(u.x, u.x, u.y * u.y);
-    if (!(a2 >= 1e-30f)) return make_float2(0.0f, 0.0f);  // also NaN
-    float w = fmaf(p.kp, a2, -p.pp_def * rho);             // i w u
-    float corr = 0.0f;
-    if (rho < 0.0f) {
-        float raw;
-        float al = alpha_of(a2, rho, p, tab, &raw);
-        corr = isfinite(raw) ? al - raw : 0.0f;
-    }
-    float2 r = make_float2(fmaf(corr, u.x, -w * u.y), fmaf(corr, u.y, w * u.x));
-    if (!isfinite(r.x) || !isfinite(r.y)) r = make_float2(0.0f, 0.0f);
-    return r;
-}
-
-__device__ __forceinline__ float2 nl_point(float2 u, float rho, float dz, const NLParams &p,
-                                           const float4 *__restrict__ tab) {
-    const float hdz = 0.5f * dz;
-    float raw;
-    float a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
-    u = c_scale(u, expf(-hdz * a));
-    float2 k1 = nl_rhs(u, rho, p, tab);
-    float2 k2 = nl_rhs(make_float2(fmaf(hdz, k1.x, u.x), fmaf(hdz, k1.y, u.y)), rho, p, tab);
-    float2 k3 = nl_rhs(make_float2(fmaf(hdz, k2.x, u.x), fmaf(hdz, k2.y, u.y)), rho, p, tab);
-    float2 k4 = nl_rhs(make_float2(fmaf(dz, k3.x, u.x), fmaf(dz, k3.y, u.y)), rho, p, tab);
-    const float s6 = dz * (1.0f / 6.0f);
-    u.x = fmaf(s6, k1.x + 2.0f * (k2.x + k3.x) + k4.x, u.x);
-    u.y = fmaf(s6, k1.y + 2.0f * (k2.y + k3.y) + k4.y, u.y);
-    a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
-    return c_scale(u, expf(-hdz * a));
-}
+#include "nl_impl.cuh"
 
 // Two points per thread per iteration (16-byte field loads, 8-byte rho loads).
 __global__ void __launch_bounds__(256)

@@ -10,18 +10,23 @@
 #include "nlse_internal.cuh"
 
 // Per-dz phase tables, computed in FP64 on the device and rounded once:
-//   Pt[k] = exp(i delta_k[k] dz/2) * spec_mask[k] * Rk*iRk / Nt   (1/Nt = ifft norm)
-//   Pr[m] = exp(-i rho_m^2 dz / (4 k0))
+//   Pt[k]  = exp(i delta_k[k] dz/2) * spec_mask[k] * Rk*iRk / Nt   (1/Nt = ifft norm)
+//   Ptf[k] = the same without 1/Nt (split-BF16 path; may be NULL)
+//   Pr[m]  = exp(-i rho_m^2 dz / (4 k0))
 __global__ void k_phase_tables(const double *__restrict__ delta_k, const double *__restrict__ spec_mask,
                                const double *__restrict__ rho_modes, int Nt, int Nr, double dz,
                                double komega, double scale, float2 *__restrict__ Pt,
-                               float2 *__restrict__ Pr) {
+                               float2 *__restrict__ Pr, float2 *__restrict__ Ptf) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < Nt) {
         double s, c;
         sincos(delta_k[i] * dz * 0.5, &s, &c);
         double m = spec_mask[i] * scale / (double)Nt;
         Pt[i] = make_float2((float)(c * m), (float)(s * m));
+        if (Ptf) {
+            double mf = spec_mask[i] * scale;
+            Ptf[i] = make_float2((float)(c * mf), (float)(s * mf));
+        }
     }
     if (i < Nr) {
         double s, c;
@@ -35,7 +40,7 @@ cudaError_t launch_phase_tables(nlse_ctx *c, double dz, cudaStream_t stream) {
     int n = c->Nt > c->Nr ? c->Nt : c->Nr;
     k_phase_tables<<<(n + 255) / 256, 256, 0, stream>>>(c->d_delta_k, c->d_spec_mask, c->d_rho_modes,
                                                         c->Nt, c->Nr, dz, c->komega, c->Rk_iRk,
-                                                        c->d_Pt, c->d_Pr);
+                                                        c->d_Pt, c->d_Pr, c->d_Ptf);
     return cudaGetLastError();
 }
 

@@ -12,6 +12,25 @@
 
 static thread_local nlse_error_slot g_create_err;
 
+// cuTensorMapEncodeTiled, resolved through the runtime so that the library
+// itself does not link libcuda (it must load on hosts without a driver).
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *, const cuuint64_t *,
+                                  const cuuint64_t *, const cuuint32_t *, const cuuint32_t *, CUtensorMapInterleave,
+                                  CUtensorMapSwizzle, CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn encode_tiled() {
+    static EncodeTiledFn fn = nullptr;
+    if (!fn) {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = (EncodeTiledFn)p;
+    }
+    return fn;
+}
+
 void nlse_set_error(nlse_error_slot *slot, int status, const char *fmt, ...) {
     if (!slot) return;
     slot->status = status;
@@ -36,8 +55,9 @@ static void prof_free(nlse_ctx *c) {
 static void free_ctx(nlse_ctx *c) {
     if (!c) return;
     prof_free(c);
-    void *ptrs[] = {c->d_tw, c->d_Y, c->d_Y64, c->d_rho_modes, c->d_delta_k, c->d_spec_mask,
-                    c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_Pt, c->d_Pr, c->d_work, c->d_flag};
+    void *ptrs[] = {c->d_tw,    c->d_Y,   c->d_Y64, c->d_rho_modes, c->d_delta_k, c->d_spec_mask,
+                    c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_Pt,   c->d_Pr,     c->d_work,
+                    c->d_flag,  c->d_Er,  c->d_Ei,  c->d_A,  c->d_F32, c->d_Fb,  c->d_D,   c->d_Ptf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free(c);
@@ -123,7 +143,8 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     int s = check_desc(d, gerr);
     if (s != NLSE_OK) return s;
 
-    nlse_ctx *c = (nlse_ctx *)calloc(1, sizeof(nlse_ctx));
+    nlse_ctx *c = nullptr;  // 64-byte aligned: it embeds CUtensorMap objects
+    if (posix_memalign((void **)&c, 64, sizeof(nlse_ctx)) == 0) memset(c, 0, sizeof(nlse_ctx));
     if (!c) {
         nlse_set_error(gerr, NLSE_ERR_INVALID_ARG, "out of host memory");
         return NLSE_ERR_INVALID_ARG;
@@ -229,6 +250,57 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     NLSE_TRY(dev_upload<float2>(err, &c->d_Pr, nullptr, Nr));
     NLSE_TRY(dev_upload<float2>(err, &c->d_work, nullptr, (size_t)Nr * Nt));
     NLSE_TRY(dev_upload<int>(err, &c->d_flag, nullptr, 4));
+    // split-BF16 path: operator terms, Omega-domain state, tensor maps
+    c->a_terms = 3;
+    c->cached_dz_op = NAN;
+    c->split_ok = (Nr % 64 == 0) && (Nt % 256 == 0);
+    if (c->split_ok) {
+        const size_t K2 = 2 * (size_t)Nr;
+        NLSE_TRY(dev_upload(err, &c->d_Y64, d->Y, (size_t)Nr * Nr));
+        NLSE_TRY(dev_upload<double>(err, &c->d_Er, nullptr, (size_t)Nr * Nr));
+        NLSE_TRY(dev_upload<double>(err, &c->d_Ei, nullptr, (size_t)Nr * Nr));
+        NLSE_TRY(dev_upload<__nv_bfloat16>(err, &c->d_A, nullptr, 3 * K2 * K2));
+        NLSE_TRY(dev_upload<float>(err, &c->d_F32, nullptr, K2 * Nt));
+        NLSE_TRY(dev_upload<__nv_bfloat16>(err, &c->d_Fb, nullptr, 2 * K2 * Nt));
+        NLSE_TRY(dev_upload<float>(err, &c->d_D, nullptr, K2 * Nt));
+        NLSE_TRY(dev_upload<float2>(err, &c->d_Ptf, nullptr, Nt));
+        alignas(64) CUtensorMap m;
+        cuuint32_t estr[2] = {1, 1};
+        EncodeTiledFn cuTensorMapEncodeTiled = encode_tiled();
+        if (!cuTensorMapEncodeTiled) {
+            nlse_set_error(err, NLSE_ERR_CUDA, "cuTensorMapEncodeTiled is not available from the driver");
+            free_ctx(c);
+            return NLSE_ERR_CUDA;
+        }
+        {
+            cuuint64_t dims[2] = {K2, 3 * K2};
+            cuuint64_t strides[1] = {K2 * 2};
+            cuuint32_t box[2] = {64, 128};
+            CUresult r = cuTensorMapEncodeTiled(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, c->d_A, dims, strides, box,
+                                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) {
+                nlse_set_error(err, NLSE_ERR_CUDA, "cuTensorMapEncodeTiled(A) failed: %d", (int)r);
+                free_ctx(c);
+                return NLSE_ERR_CUDA;
+            }
+            memcpy(&c->tmA, &m, sizeof(m));
+        }
+        {
+            cuuint64_t dims[2] = {(cuuint64_t)Nt, 2 * K2};
+            cuuint64_t strides[1] = {(cuuint64_t)Nt * 2};
+            cuuint32_t box[2] = {64, 64};
+            CUresult r = cuTensorMapEncodeTiled(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, c->d_Fb, dims, strides, box,
+                                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) {
+                nlse_set_error(err, NLSE_ERR_CUDA, "cuTensorMapEncodeTiled(B) failed: %d", (int)r);
+                free_ctx(c);
+                return NLSE_ERR_CUDA;
+            }
+            memcpy(&c->tmB, &m, sizeof(m));
+        }
+    }
     ce = cudaMemset(c->d_flag, 0, 4 * sizeof(int));
     if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
     if (ce != cudaSuccess) {
@@ -330,10 +402,114 @@ static int half_linear_impl(nlse_ctx *c, float2 *u, double dz, const float *row_
                     "hankel gemm 2");
 }
 
+// ---------------------------------------------------------------- split-BF16 path
+static int split_ready(nlse_ctx *c, double dz, cudaStream_t st) {
+    if (!c->split_ok)
+        return bad(c, NLSE_ERR_UNSUPPORTED,
+                   "split-BF16 mode needs Nr % 64 == 0 and Nt % 256 == 0 (this grid: use the plain mode)");
+    int s = ensure_tables(c, dz, st);
+    if (s) return s;
+    if (dz == c->cached_dz_op) return NLSE_OK;
+    PROF(K_BUILD_OP);
+    s = launched(c, launch_build_operator(c->d_Y64, c->d_rho_modes, c->Nr, dz, c->komega, c->d_Er, c->d_Ei, 3,
+                                          c->d_A, st),
+                 "operator build");
+    if (s == NLSE_OK) c->cached_dz_op = dz;
+    return s;
+}
+
+static RowFusedArgs row_args(nlse_ctx *c, double dz) {
+    RowFusedArgs a;
+    a.Nr = c->Nr;
+    a.Nt = c->Nt;
+    a.logNt = c->logNt;
+    a.tw = c->d_tw;
+    a.Pt = c->d_Ptf;
+    a.mask_r = c->d_mask_r;
+    a.lut = c->d_lut_dt;
+    a.pchip = c->d_pchip;
+    a.nl = c->nl;
+    a.sc = c->sc;
+    a.dz = (float)dz;
+    a.stats = c->d_flag;
+    return a;
+}
+
+static int tc_gemm(nlse_ctx *c, cudaStream_t st) {
+    const int K2 = 2 * c->Nr;
+    PROF(K_GEMM_TC);
+    return launched(c, launch_gemm_tc(&c->tmA, &c->tmB, c->d_D, K2, c->Nt, K2, c->a_terms, c->d_flag, st),
+                    "tcgen05 gemm");
+}
+
+static int row_entry(nlse_ctx *c, const RowFusedArgs &a, const float2 *u, float *rho, int scan, cudaStream_t st) {
+    PROF(K_ROW_ENTRY);
+    return launched(c, launch_row_entry(a, u, c->d_F32, c->d_Fb, rho, scan, st), "row entry");
+}
+
+static int row_nl(nlse_ctx *c, const RowFusedArgs &a, const float *rho, cudaStream_t st) {
+    PROF(K_ROW_NL);
+    return launched(c, launch_row_nl(a, c->d_F32, c->d_Fb, c->d_D, rho, st), "row nonlinear");
+}
+
+static int row_next(nlse_ctx *c, const RowFusedArgs &a, float *rho, float2 *u_out, int write_state, int scan,
+                    int mask, cudaStream_t st) {
+    PROF(K_ROW_NEXT);
+    return launched(c, launch_row_next(a, c->d_F32, c->d_Fb, c->d_D, rho, u_out, write_state, scan, mask, st),
+                    "row next");
+}
+
+#define NLSE_SEQ(x)              \
+    do {                         \
+        int s_ = (x);            \
+        if (s_) return s_;       \
+    } while (0)
+
+static int half_linear_split(nlse_ctx *c, float2 *u, double dz, cudaStream_t st) {
+    NLSE_SEQ(split_ready(c, dz, st));
+    RowFusedArgs a = row_args(c, dz);
+    NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
+    NLSE_SEQ(tc_gemm(c, st));
+    return row_next(c, a, nullptr, u, 0, 0, 0, st);
+}
+
+static int step_split(nlse_ctx *c, float2 *u, const float *rho, double dz, cudaStream_t st) {
+    NLSE_SEQ(split_ready(c, dz, st));
+    RowFusedArgs a = row_args(c, dz);
+    NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
+    NLSE_SEQ(tc_gemm(c, st));
+    NLSE_SEQ(row_nl(c, a, rho, st));
+    NLSE_SEQ(tc_gemm(c, st));
+    return row_next(c, a, nullptr, u, 0, 0, 1, st);
+}
+
+static int propagate_split(nlse_ctx *c, float2 *u, float *rho, float *rho_s, double dz, int n, cudaStream_t st) {
+    if (n == 0) return NLSE_OK;
+    NLSE_SEQ(split_ready(c, dz, st));
+    RowFusedArgs a = row_args(c, dz);
+    if (rho_s)
+        NLSE_SEQ(launched(c, cudaMemsetAsync(rho_s, 0, (size_t)c->Nr * c->Nt * sizeof(float), st), "rho_s memset"));
+    NLSE_SEQ(row_entry(c, a, u, rho, 1, st));
+    for (int i = 0; i < n; ++i) {
+        const bool last = i == n - 1;
+        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(row_nl(c, a, rho, st));
+        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(row_next(c, a, rho, last ? u : nullptr, last ? 0 : 1, last ? 0 : 1, 1, st));
+    }
+    return NLSE_OK;
+}
+
 // ---------------------------------------------------------------- entry points
 extern "C" int nlse_half_linear(nlse_ctx *c, void *u, double dz, void *stream) {
+    return nlse_half_linear_ex(c, u, dz, NLSE_MODE_PLAIN_F32, stream);
+}
+
+extern "C" int nlse_half_linear_ex(nlse_ctx *c, void *u, double dz, int mode, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u")) return NLSE_ERR_INVALID_ARG;
+    if (mode == NLSE_MODE_SPLIT_BF16) return half_linear_split(c, (float2 *)u, dz, (cudaStream_t)stream);
+    if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
     return half_linear_impl(c, (float2 *)u, dz, nullptr, (cudaStream_t)stream);
 }
 
@@ -378,7 +554,8 @@ extern "C" int nlse_step(nlse_ctx *c, void *u, const float *rho, const float *rh
     (void)rho_s;
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
-    if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_UNSUPPORTED, "mode not available in this build");
+    if (mode == NLSE_MODE_SPLIT_BF16) return step_split(c, (float2 *)u, rho, dz, (cudaStream_t)stream);
+    if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
     return step_plain(c, (float2 *)u, rho, dz, (cudaStream_t)stream);
 }
 
@@ -387,8 +564,9 @@ extern "C" int nlse_propagate(nlse_ctx *c, void *u, float *rho, float *rho_s, do
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
     if (nsteps < 0) return bad(c, NLSE_ERR_INVALID_ARG, "nsteps < 0");
-    if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_UNSUPPORTED, "mode not available in this build");
     cudaStream_t st = (cudaStream_t)stream;
+    if (mode == NLSE_MODE_SPLIT_BF16) return propagate_split(c, (float2 *)u, rho, rho_s, dz, nsteps, st);
+    if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
     for (int i = 0; i < nsteps; ++i) {
         int s;
         {
@@ -398,6 +576,36 @@ extern "C" int nlse_propagate(nlse_ctx *c, void *u, float *rho, float *rho_s, do
         if (s) return s;
         s = step_plain(c, (float2 *)u, rho, dz, st);
         if (s) return s;
+    }
+    return NLSE_OK;
+}
+
+extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *out, double dz, void *stream) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    if (!field_ok(c, w, "w") || !field_ok(c, out, "out")) return NLSE_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    NLSE_SEQ(split_ready(c, dz, st));
+    const size_t n = 2 * (size_t)c->Nr * c->Nt;
+    NLSE_SEQ(launched(c, launch_split_field(w, c->d_Fb, n, st), "split field"));
+    NLSE_SEQ(tc_gemm(c, st));
+    return launched(c, cudaMemcpyAsync(out, c->d_D, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+}
+
+extern "C" int nlse_set_split_terms(nlse_ctx *c, int a_terms) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    if (a_terms != 2 && a_terms != 3) return bad(c, NLSE_ERR_INVALID_ARG, "a_terms must be 2 or 3");
+    c->a_terms = a_terms;
+    return NLSE_OK;
+}
+
+extern "C" int nlse_device_status(nlse_ctx *c, int *word) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    int h[4];
+    NLSE_CUDA_TRY(&c->err, cudaMemcpy(h, c->d_flag, sizeof(h), cudaMemcpyDeviceToHost));
+    if (word) *word = h[0];
+    if (h[0]) {
+        nlse_set_error(&c->err, NLSE_ERR_TIMEOUT, "a bounded device wait gave up (status word 0x%x)", h[0]);
+        return NLSE_ERR_TIMEOUT;
     }
     return NLSE_OK;
 }
@@ -457,6 +665,11 @@ extern "C" const char *nlse_kernel_name(int kid) {
         case K_NONLINEAR: return "k_nonlinear_step";
         case K_SPLIT: return "k_split";
         case K_PHASE_TABLES: return "k_phase_tables";
+        case K_GEMM_TC: return "k_gemm_tc";
+        case K_ROW_ENTRY: return "k_row_entry";
+        case K_ROW_NL: return "k_row_nl";
+        case K_ROW_NEXT: return "k_row_next";
+        case K_BUILD_OP: return "k_build_operator";
         default: return "";
     }
 }

@@ -1,6 +1,7 @@
 // Internal declarations shared by the libnlse translation units.
 #pragma once
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 #include <stdint.h>
@@ -55,6 +56,20 @@ struct ScanParams {
     int lut_n;
 };
 
+// Arguments of the fused row kernels (k_rowfused.cu).
+struct RowFusedArgs {
+    int Nr, Nt, logNt;
+    const float2 *tw;     // forward twiddles
+    const float2 *Pt;     // e^{i dk dz/2} spec_mask (no 1/Nt)
+    const float *mask_r;  // Nr
+    const float *lut;     // W * dt table for the march
+    const float4 *pchip;  // photo-ionisation spline
+    NLParams nl;
+    ScanParams sc;
+    float dz;
+    int *stats;
+};
+
 // ---------------------------------------------------------------- context
 struct nlse_ctx {
     nlse_error_slot err;
@@ -80,6 +95,17 @@ struct nlse_ctx {
     // workspace
     float2 *d_work;        // Nr*Nt complex64
     int *d_flag;           // device status word
+    // split-BF16 path (allocated when Nr % 64 == 0 and Nt % 256 == 0)
+    int split_ok, a_terms;
+    double cached_dz_op;   // dz of the operator currently in d_A
+    double *d_Er, *d_Ei;   // Nr*Nr FP64 scratch of the builder
+    __nv_bfloat16 *d_A;    // 3 x (2Nr x 2Nr) BF16 terms of E'
+    float *d_F32;          // 2Nr x Nt planar Omega-domain state
+    __nv_bfloat16 *d_Fb;   // 2 x (2Nr x Nt) BF16 hi/lo of the state
+    float *d_D;            // 2Nr x Nt tensor-core product
+    float2 *d_Ptf;         // Nt  exp(i dk dz/2) mask Rk iRk  (no 1/Nt)
+    CUtensorMap tmA;       // A operand: d_A as [3 * 2Nr][2Nr], box 64 x 128
+    CUtensorMap tmB;       // B operand: d_Fb as [2 * 2Nr][Nt], box 64 x 64
     // per-launch event profiling (off unless nlse_profile_start was called)
     int prof_on, prof_cap, prof_n;
     cudaEvent_t *prof_ev;  // 2 * prof_cap events
@@ -94,6 +120,11 @@ enum {
     K_NONLINEAR = 3,
     K_SPLIT = 4,
     K_PHASE_TABLES = 5,
+    K_GEMM_TC = 6,
+    K_ROW_ENTRY = 7,
+    K_ROW_NL = 8,
+    K_ROW_NEXT = 9,
+    K_BUILD_OP = 10,
     K_NUM_KINDS = 16
 };
 
@@ -109,6 +140,18 @@ cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, float2 
                          float *alpha, cudaStream_t stream);
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s,
                              int zero_first, cudaStream_t stream);
+cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
+                           int a_terms, int *err, cudaStream_t stream);
+cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
+                                  double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, cudaStream_t stream);
+
+cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st);
+cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
+                             int do_scan, cudaStream_t st);
+cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,
+                          cudaStream_t st);
+cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, float *rho,
+                            float2 *u_out, int write_state, int do_scan, int apply_mask, cudaStream_t st);
 
 // ---------------------------------------------------------------- complex
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
