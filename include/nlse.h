@@ -175,6 +175,27 @@ int nlse_profile_read(nlse_ctx *ctx, int *launches, double *total_ms, int nkinds
                       int *dropped);
 const char *nlse_kernel_name(int kind);
 
+/*
+ * Allocation-free variant of the plain half step, for callers that cannot
+ * call cudaMalloc (a host application that owns all device memory through
+ * its own pool, a real-time loop that must not reach the allocator, code
+ * that cannot create an nlse_ctx).  No counterpart in the reference: it is an
+ * addition of this library.  It needs no context and allocates nothing:
+ *   Y   device, Nr x Nr float32 row-major (the QDHT matrix),
+ *   Pt  device, Nt complex64: exp(i delta_k dz/2) spec_mask Rk iRk / Nt,
+ *   Pr  device, Nr complex64: exp(-i rho_m^2 dz / (4 k0)),
+ *   u   device, Nr x Nt complex64, transformed in place (16-byte aligned).
+ * Its intermediate field and twiddles live in a static device array of
+ * 4 MiB + 64 KiB that each GPU loading the library holds until exit, so
+ * Nr * Nt must not exceed 524288 (larger sizes are rejected with
+ * NLSE_ERR_INVALID_ARG).  The array's address is looked up on the first call
+ * on each device (make that call before any stream capture); all calls share
+ * the array, so calls that overlap on the GPU race.  Errors are read with
+ * nlse_get_last_error(NULL, ...).
+ */
+int nlse_half_linear_noalloc(const float *Y, const void *Pt, const void *Pr, void *u,
+                             int Nr, int Nt, void *stream);
+
 /* Copy the last error message of ctx (or of the last failed nlse_create when
  * ctx is NULL) into buf; returns the status of that error. */
 int nlse_get_last_error(const nlse_ctx *ctx, char *buf, size_t len);

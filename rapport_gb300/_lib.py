@@ -21,6 +21,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
+           "nlse_half_linear_noalloc",
            "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
            "nlse_get_last_error", "nlse_destroy", "nlse_version")
 
@@ -58,6 +59,7 @@ def load():
     lib.nlse_half_linear.argtypes = [_P, _P, _D, _P]
     lib.nlse_half_linear_ex.argtypes = [_P, _P, _D, _I, _P]
     lib.nlse_set_split_terms.argtypes = [_P, _I]
+    lib.nlse_half_linear_noalloc.argtypes = [_P, _P, _P, _P, _I, _I, _P]
     lib.nlse_debug_operator_product.argtypes = [_P, _P, _P, _D, _P]
     lib.nlse_device_status.argtypes = [_P, ctypes.POINTER(_I)]
     lib.nlse_split.argtypes = [_P, _P, _P, _P, _P, _P]

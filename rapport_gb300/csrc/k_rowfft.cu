@@ -72,3 +72,14 @@ cudaError_t launch_fft_phase_ifft(nlse_ctx *c, float2 *u, cudaStream_t stream) {
                                                                 c->d_Pr);
     return cudaGetLastError();
 }
+
+// The same row kernel on caller-provided tables (used by the allocation-free entry point).
+cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, const float2 *tw, const float2 *Pt,
+                                         const float2 *Pr, cudaStream_t stream) {
+    size_t smem = 2 * (size_t)Nt * sizeof(float2);
+    cudaError_t e = cudaFuncSetAttribute(k_fft_phase_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         (int)smem);
+    if (e != cudaSuccess) return e;
+    k_fft_phase_ifft<<<Nr, NLSE_ROW_THREADS, smem, stream>>>(u, Nt, logNt, tw, Pt, Pr);
+    return cudaGetLastError();
+}

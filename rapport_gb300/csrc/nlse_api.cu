@@ -31,6 +31,9 @@ static EncodeTiledFn encode_tiled() {
     return fn;
 }
 
+// Error of a context-free entry point, readable with nlse_get_last_error(NULL, ...).
+void nlse_set_thread_error(int status, const char *msg) { nlse_set_error(&g_create_err, status, "%s", msg); }
+
 void nlse_set_error(nlse_error_slot *slot, int status, const char *fmt, ...) {
     if (!slot) return;
     slot->status = status;

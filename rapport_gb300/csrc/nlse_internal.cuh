@@ -145,6 +145,9 @@ cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float
 cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
                                   double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, cudaStream_t stream);
 
+cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, const float2 *tw, const float2 *Pt,
+                                         const float2 *Pr, cudaStream_t stream);
+void nlse_set_thread_error(int status, const char *msg);
 cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st);
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
                              int do_scan, cudaStream_t st);
