@@ -1,0 +1,84 @@
+"""Long-run accuracy against FP64: the metric's "<= 1e-4 L2 field error after 1 cm".
+
+* test_fp64_gpu_reference_is_pinned: the FP64 GPU restatement (oracle/fp64_gpu.py)
+  reproduces the numpy oracle (which reproduces the reference bit for bit) to
+  1e-11 over several steps -- only then is it used as the long-run reference.
+* test_one_cm_accuracy (set NLSE_LONG=1; ~3 min): the 1024 x 2048 workload
+  propagated 4000 z-steps of 2.5 um (1 cm) by the FP64 reference, the plain
+  FP32 form and the split-BF16 form (3-term and 2-term operator).  Reports the
+  relative L2 field error, peak-fluence error and peak-rho error at 0.125,
+  0.25, 0.5 and 1 cm, writes them to gpurun_out/accuracy_1cm.json when that
+  folder exists, and asserts the benchmark spec's bounds for the split-BF16 form:
+  L2 <= 1e-4 and peak-rho <= 1e-3 after 1 cm.
+"""
+import json
+import os
+
+import numpy as np
+import pytest
+
+import nlse_oracle as O
+from conftest import REPO, rel_l2
+from gpu_util import CONFIG2, Case, dev, host
+
+pytestmark = pytest.mark.gpu
+
+
+def test_fp64_gpu_reference_is_pinned():
+    import fp64_gpu
+    og = O.OracleGrid(O.workload_config(64, 256, 1e-4, 1e-5, 3e-13))
+    u0 = O.lens_gaussian(og, 1e-5, 100e-15, 2.0, 1e-2, 0)
+    ref_u, ref_rho, _ = og.propagate(u0.copy(), 5, 5e-6)
+    g = fp64_gpu.FP64GPU(og)
+    u, rho = g.propagate(u0, 5, 5e-6)
+    assert rel_l2(u.cpu().numpy(), ref_u) < 1e-11
+    assert np.abs(rho.cpu().numpy() - ref_rho).max() <= 1e-11 * ref_rho.max()
+
+
+def _metrics(u, rho, uref, rref, dt, invE2):
+    flu = (np.abs(u) ** 2).sum(axis=1) * dt * invE2
+    flu_r = (np.abs(uref) ** 2).sum(axis=1) * dt * invE2
+    return {"l2": rel_l2(u, uref), "peak_fluence": abs(flu.max() / flu_r.max() - 1),
+            "peak_rho": abs(rho.max() / max(rref.max(), 1e-300) - 1) if rref.max() > 0 else 0.0,
+            "peak_rho_value": float(rref.max())}
+
+
+@pytest.mark.skipif(os.environ.get("NLSE_LONG") != "1", reason="long run: set NLSE_LONG=1")
+def test_one_cm_accuracy():
+    import torch
+    import fp64_gpu
+    from rapport_gb300._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16
+
+    c = Case(**CONFIG2)
+    ref = fp64_gpu.FP64GPU(c.og)
+    forms = {"split_bf16_3term": (MODE_SPLIT_BF16, 3), "split_bf16_2term": (MODE_SPLIT_BF16, 2),
+             "plain_fp32": (MODE_PLAIN_F32, 3)}
+    state = {k: (dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))) for k in forms}
+    ur = torch.tensor(c.u0, dtype=torch.complex128, device="cuda")
+    rr = torch.zeros(c.u0.shape, dtype=torch.float64, device="cuda")
+    report = {"workload": "1024x2048, 5 uJ, w0 150 um, f 10 cm, dz 2.5 um", "checkpoints": {}}
+    done = 0
+    for stop in (500, 1000, 2000, 4000):
+        for _ in range(stop - done):
+            ref.update_plasma(ur, rr)
+            ur = ref.step(ur, rr, c.dz)
+        for name, (mode, terms) in forms.items():
+            c.ctx.set_split_terms(terms)
+            u, rho, rs = state[name]
+            c.ctx.propagate(u, rho, rs, c.dz, stop - done, mode)
+        c.ctx.set_split_terms(3)
+        done = stop
+        urn, rrn = ur.cpu().numpy(), rr.cpu().numpy()
+        entry = {}
+        for name in forms:
+            u, rho, _ = state[name]
+            entry[name] = _metrics(host(u), host(rho), urn, rrn, c.og.dt, c.og.invE2)
+        report["checkpoints"][f"{stop * c.dz * 100:.3f} cm"] = entry
+        print(stop, json.dumps(entry), flush=True)
+    assert c.ctx.device_status() == 0
+    out = os.path.join(REPO, "gpurun_out")
+    if os.path.isdir(out):
+        with open(os.path.join(out, "accuracy_1cm.json"), "w") as f:
+            json.dump(report, f, indent=1)
+    last = report["checkpoints"]["1.000 cm"]["split_bf16_3term"]
+    assert last["l2"] <= 1e-4 and last["peak_rho"] <= 1e-3, last
