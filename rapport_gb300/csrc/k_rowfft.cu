@@ -45,41 +45,43 @@ cudaError_t launch_phase_tables(nlse_ctx *c, double dz, cudaStream_t stream) {
 }
 
 // u[m, :] <- ifft( Pr[m] Pt * fft(u[m, :]) ), one CTA per row, in place.
+template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
-k_fft_phase_ifft(float2 *__restrict__ u, int Nt, int logNt, const float2 *__restrict__ tw,
-                 const float2 *__restrict__ Pt, const float2 *__restrict__ Pr) {
+k_fft_phase_ifft(float2 *__restrict__ u, const float2 *__restrict__ tw, const float2 *__restrict__ Pt,
+                 const float2 *__restrict__ Pr) {
     extern __shared__ float2 smem[];
-    float2 *b0 = smem, *b1 = smem + Nt;
+    float2 *b0 = smem, *b1 = smem + fft_slots(NT);
     const size_t row = blockIdx.x;
-    float2 *g = u + row * (size_t)Nt;
-    for (int i = threadIdx.x; i < Nt; i += blockDim.x) b0[i] = g[i];
+    float2 *g = u + row * (size_t)NT;
+    for (int i = threadIdx.x; i < NT; i += blockDim.x) b0[pidx(i)] = g[i];
     __syncthreads();
-    float2 *s = fft_row<false>(b0, b1, Nt, logNt, tw);
+    float2 *s = fft_row<NT, false>(b0, b1, tw);
     const float2 pr = Pr[row];
-    for (int i = threadIdx.x; i < Nt; i += blockDim.x) s[i] = c_mul(s[i], c_mul(pr, __ldg(&Pt[i])));
+    for (int i = threadIdx.x; i < NT; i += blockDim.x) s[pidx(i)] = c_mul(s[pidx(i)], c_mul(pr, __ldg(&Pt[i])));
     __syncthreads();
-    float2 *o = s == b0 ? b1 : b0;
-    float2 *r = fft_row<true>(s, o, Nt, logNt, tw);
-    for (int i = threadIdx.x; i < Nt; i += blockDim.x) g[i] = r[i];
+    float2 *r = fft_row<NT, true>(s, s == b0 ? b1 : b0, tw);
+    for (int i = threadIdx.x; i < NT; i += blockDim.x) g[i] = r[pidx(i)];
+}
+
+static cudaError_t fft_phase_ifft(float2 *u, int Nr, int logNt, const float2 *tw, const float2 *Pt,
+                                  const float2 *Pr, cudaStream_t stream) {
+    NLSE_DISPATCH_NT(logNt, {
+        const size_t smem = 2 * (size_t)fft_slots(NT) * sizeof(float2);
+        cudaError_t e = cudaFuncSetAttribute(k_fft_phase_ifft<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
+        if (e != cudaSuccess) return e;
+        k_fft_phase_ifft<NT><<<Nr, NLSE_ROW_THREADS, smem, stream>>>(u, tw, Pt, Pr);
+    });
+    return cudaGetLastError();
 }
 
 cudaError_t launch_fft_phase_ifft(nlse_ctx *c, float2 *u, cudaStream_t stream) {
-    size_t smem = 2 * (size_t)c->Nt * sizeof(float2);
-    cudaError_t e = cudaFuncSetAttribute(k_fft_phase_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    k_fft_phase_ifft<<<c->Nr, NLSE_ROW_THREADS, smem, stream>>>(u, c->Nt, c->logNt, c->d_tw, c->d_Pt,
-                                                                c->d_Pr);
-    return cudaGetLastError();
+    return fft_phase_ifft(u, c->Nr, c->logNt, c->d_tw, c->d_Pt, c->d_Pr, stream);
 }
 
 // The same row kernel on caller-provided tables (used by the allocation-free entry point).
 cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, const float2 *tw, const float2 *Pt,
                                          const float2 *Pr, cudaStream_t stream) {
-    size_t smem = 2 * (size_t)Nt * sizeof(float2);
-    cudaError_t e = cudaFuncSetAttribute(k_fft_phase_ifft, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                         (int)smem);
-    if (e != cudaSuccess) return e;
-    k_fft_phase_ifft<<<Nr, NLSE_ROW_THREADS, smem, stream>>>(u, Nt, logNt, tw, Pt, Pr);
-    return cudaGetLastError();
+    (void)Nt;
+    return fft_phase_ifft(u, Nr, logNt, tw, Pt, Pr, stream);
 }

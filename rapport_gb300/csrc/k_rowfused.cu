@@ -21,140 +21,176 @@
 #include "scan_impl.cuh"
 
 
-// FP32 planar rows + BF16 hi/lo terms of one complex row held in smem.
+// FP32 planar rows + BF16 hi/lo terms of one complex row held in smem
+// (padded indexing); two points per thread per iteration.
+template <int NT>
 __device__ __forceinline__ void store_state_row(const float2 *s, int r, const RowFusedArgs &a, float *F32,
                                                 __nv_bfloat16 *Fb) {
-    const size_t Nt = a.Nt, rows = 2 * (size_t)a.Nr;
-    float *re = F32 + (size_t)r * Nt, *im = F32 + ((size_t)a.Nr + r) * Nt;
-    __nv_bfloat16 *hre = Fb + (size_t)r * Nt, *him = Fb + ((size_t)a.Nr + r) * Nt;
-    __nv_bfloat16 *lre = hre + rows * Nt, *lim = him + rows * Nt;
-    for (int t = threadIdx.x; t < a.Nt; t += blockDim.x) {
-        float2 v = s[t];
-        re[t] = v.x;
-        im[t] = v.y;
-        __nv_bfloat16 hx = __float2bfloat16_rn(v.x), hy = __float2bfloat16_rn(v.y);
-        hre[t] = hx;
-        him[t] = hy;
-        lre[t] = __float2bfloat16_rn(v.x - __bfloat162float(hx));
-        lim[t] = __float2bfloat16_rn(v.y - __bfloat162float(hy));
+    const size_t rows = 2 * (size_t)a.Nr;
+    float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nr + r) * NT;
+    __nv_bfloat16 *hre = Fb + (size_t)r * NT, *him = Fb + ((size_t)a.Nr + r) * NT;
+    __nv_bfloat16 *lre = hre + rows * NT, *lim = him + rows * NT;
+    for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
+        const float2 v0 = s[pidx(t)], v1 = s[pidx(t + 1)];
+        *reinterpret_cast<float2 *>(re + t) = make_float2(v0.x, v1.x);
+        *reinterpret_cast<float2 *>(im + t) = make_float2(v0.y, v1.y);
+        const __nv_bfloat162 hx = __floats2bfloat162_rn(v0.x, v1.x), hy = __floats2bfloat162_rn(v0.y, v1.y);
+        *reinterpret_cast<__nv_bfloat162 *>(hre + t) = hx;
+        *reinterpret_cast<__nv_bfloat162 *>(him + t) = hy;
+        *reinterpret_cast<__nv_bfloat162 *>(lre + t) =
+            __floats2bfloat162_rn(v0.x - __low2float(hx), v1.x - __high2float(hx));
+        *reinterpret_cast<__nv_bfloat162 *>(lim + t) =
+            __floats2bfloat162_rn(v0.y - __low2float(hy), v1.y - __high2float(hy));
     }
 }
 
-// s[t] = scale * P_t[t] * ((F32 + D) row r as complex)
+// s[t] = scale * P_t[t] * ((F32 + D) row r as complex), padded indexing.
+template <int NT>
 __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs &a, const float *F32,
                                             const float *D, float scale) {
-    const size_t Nt = a.Nt;
-    const float *fr = F32 + (size_t)r * Nt, *fi = F32 + ((size_t)a.Nr + r) * Nt;
-    const float *dr = D + (size_t)r * Nt, *di = D + ((size_t)a.Nr + r) * Nt;
-    for (int t = threadIdx.x; t < a.Nt; t += blockDim.x) {
-        float2 z = make_float2(fr[t] + dr[t], fi[t] + di[t]);
-        s[t] = c_scale(c_mul(z, __ldg(&a.Pt[t])), scale);
+    const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nr + r) * NT;
+    const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nr + r) * NT;
+    for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
+        const float2 xr = *reinterpret_cast<const float2 *>(fr + t), xi = *reinterpret_cast<const float2 *>(fi + t);
+        const float2 yr = *reinterpret_cast<const float2 *>(dr + t), yi = *reinterpret_cast<const float2 *>(di + t);
+        const float4 pt = __ldg(reinterpret_cast<const float4 *>(a.Pt + t));
+        s[pidx(t)] = c_scale(c_mul(make_float2(xr.x + yr.x, xi.x + yi.x), make_float2(pt.x, pt.y)), scale);
+        s[pidx(t + 1)] = c_scale(c_mul(make_float2(xr.y + yr.y, xi.y + yi.y), make_float2(pt.z, pt.w)), scale);
     }
+}
+
+// Carrier march of the physical row held (unnormalised by inv) in R; scratch
+// in the other FFT buffer O and the extra float area X; writes rho row r.
+template <int NT>
+__device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float inv, int r, const RowFusedArgs &a,
+                                          float *rho) {
+    float *sI = reinterpret_cast<float *>(O), *sW = sI + NT;
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+        const float2 v = c_scale(R[pidx(t)], inv);
+        sI[t] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
+    }
+    __syncthreads();
+    float *sx = reinterpret_cast<float *>(R), *sJ = sx + NT;
+    scan_row(sI, sW, sx, sJ, X, NT, a.sc, a.lut, 0.0f, a.stats);
+    float *gr = rho + (size_t)r * NT;
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[t];
+}
+
+template <int NT>
+__host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
+    return 2 * (size_t)fft_slots(NT) * sizeof(float2) + (with_march ? (size_t)NT * sizeof(float) : 0);
 }
 
 // Entry: physical u (interleaved) -> w = F[u] (state); optionally rho = march(|u|^2).
+template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb,
             float *__restrict__ rho, int do_scan) {
     extern __shared__ float2 sm2[];
-    const int r = blockIdx.x, Nt = a.Nt;
-    float2 *b0 = sm2, *b1 = sm2 + Nt;
-    const float2 *g = u + (size_t)r * Nt;
-    for (int t = threadIdx.x; t < Nt; t += blockDim.x) b0[t] = g[t];
-    __syncthreads();
-    float2 *R = fft_row<false>(b0, b1, Nt, a.logNt, a.tw);
-    store_state_row(R, r, a, F32, Fb);
-    if (!do_scan) return;
-    __syncthreads();
-    float *sI = (float *)(R == b0 ? b1 : b0), *sW = sI + Nt;
-    float *sx = (float *)R, *sJ = sx + Nt, *sB = (float *)(sm2 + 2 * Nt);
-    for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
-        float2 v = g[t];
-        sI[t] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
+    const int r = blockIdx.x;
+    float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
+    const float2 *g = u + (size_t)r * NT;
+    for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
+        const float4 v = *reinterpret_cast<const float4 *>(g + t);
+        b0[pidx(t)] = make_float2(v.x, v.y);
+        b0[pidx(t + 1)] = make_float2(v.z, v.w);
     }
     __syncthreads();
-    scan_row(sI, sW, sx, sJ, sB, Nt, a.sc, a.lut, 0.0f, a.stats);
-    float *gr = rho + (size_t)r * Nt;
-    for (int t = threadIdx.x; t < Nt; t += blockDim.x) gr[t] = sx[t];
+    float2 *R = fft_row<NT, false>(b0, b1, a.tw);
+    store_state_row<NT>(R, r, a, F32, Fb);
+    if (!do_scan) return;
+    __syncthreads();
+    // the march needs the physical field: reload it into the free buffer
+    float2 *O = R == b0 ? b1 : b0;
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) O[pidx(t)] = g[t];
+    __syncthreads();
+    march_row<NT>(O, R, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), 1.0f, r, a, rho);
 }
 
 // First half step's spectral end + the nonlinear block + forward FFT.
+template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
          const float *__restrict__ rho) {
     extern __shared__ float2 sm2[];
-    const int r = blockIdx.x, Nt = a.Nt;
-    float2 *b0 = sm2, *b1 = sm2 + Nt;
-    load_mw_row(b0, r, a, F32, D, 1.0f / (float)Nt);
+    const int r = blockIdx.x;
+    float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
+    load_mw_row<NT>(b0, r, a, F32, D, 1.0f / (float)NT);
     __syncthreads();
-    float2 *R = fft_row<true>(b0, b1, Nt, a.logNt, a.tw);
-    const float *gr = rho + (size_t)r * Nt;
-    for (int t = threadIdx.x; t < Nt; t += blockDim.x) R[t] = nl_point(R[t], gr[t], a.dz, a.nl, a.pchip);
+    float2 *R = fft_row<NT, true>(b0, b1, a.tw);
+    const float *gr = rho + (size_t)r * NT;
+    for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
+        const float2 rr = *reinterpret_cast<const float2 *>(gr + t);
+        R[pidx(t)] = nl_point(R[pidx(t)], rr.x, a.dz, a.nl, a.pchip);
+        R[pidx(t + 1)] = nl_point(R[pidx(t + 1)], rr.y, a.dz, a.nl, a.pchip);
+    }
     __syncthreads();
-    float2 *O = R == b0 ? b1 : b0;
-    float2 *Y = fft_row<false>(R, O, Nt, a.logNt, a.tw);
-    store_state_row(Y, r, a, F32, Fb);
+    float2 *Y = fft_row<NT, false>(R, R == b0 ? b1 : b0, a.tw);
+    store_state_row<NT>(Y, r, a, F32, Fb);
 }
 
 // Second half step's spectral end + mask_r: the next state w', and optionally
 // the physical field (u_out) and the next carrier march (rho).
+template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
            float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask) {
     extern __shared__ float2 sm2[];
-    const int r = blockIdx.x, Nt = a.Nt;
-    float2 *b0 = sm2, *b1 = sm2 + Nt;
-    load_mw_row(b0, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f);
+    const int r = blockIdx.x;
+    float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
+    load_mw_row<NT>(b0, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f);
     __syncthreads();
-    if (write_state) store_state_row(b0, r, a, F32, Fb);
+    if (write_state) store_state_row<NT>(b0, r, a, F32, Fb);
     if (!do_scan && !u_out) return;
-    float2 *R = fft_row<true>(b0, b1, Nt, a.logNt, a.tw);
-    const float inv = 1.0f / (float)Nt;
+    float2 *R = fft_row<NT, true>(b0, b1, a.tw);
+    const float inv = 1.0f / (float)NT;
     if (u_out) {
-        float2 *g = u_out + (size_t)r * Nt;
-        for (int t = threadIdx.x; t < Nt; t += blockDim.x) g[t] = c_scale(R[t], inv);
+        float2 *g = u_out + (size_t)r * NT;
+        for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
+            const float2 v0 = c_scale(R[pidx(t)], inv), v1 = c_scale(R[pidx(t + 1)], inv);
+            *reinterpret_cast<float4 *>(g + t) = make_float4(v0.x, v0.y, v1.x, v1.y);
+        }
     }
     if (!do_scan) return;
-    float *sI = (float *)(R == b0 ? b1 : b0), *sW = sI + Nt;
-    for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
-        float2 v = c_scale(R[t], inv);
-        sI[t] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
-    }
-    __syncthreads();
-    float *sx = (float *)R, *sJ = sx + Nt, *sB = (float *)(sm2 + 2 * Nt);
-    scan_row(sI, sW, sx, sJ, sB, Nt, a.sc, a.lut, 0.0f, a.stats);
-    float *gr = rho + (size_t)r * Nt;
-    for (int t = threadIdx.x; t < Nt; t += blockDim.x) gr[t] = sx[t];
+    march_row<NT>(R, R == b0 ? b1 : b0, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), inv, r, a, rho);
 }
 
-static cudaError_t set_smem(const void *fn, size_t bytes) {
+template <typename K>
+static cudaError_t set_smem(K *fn, size_t bytes) {
     return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
                              int do_scan, cudaStream_t st) {
-    size_t smem = 20 * (size_t)a.Nt;  // 2 complex buffers + one float scan array
-    cudaError_t e = set_smem((const void *)k_row_entry, smem);
-    if (e != cudaSuccess) return e;
-    k_row_entry<<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, u, F32, Fb, rho, do_scan);
+    NLSE_DISPATCH_NT(a.logNt, {
+        const size_t smem = row_smem_bytes<NT>(true);
+        cudaError_t e = set_smem(k_row_entry<NT>, smem);
+        if (e != cudaSuccess) return e;
+        k_row_entry<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, u, F32, Fb, rho, do_scan);
+    });
     return cudaGetLastError();
 }
 
 cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,
                           cudaStream_t st) {
-    size_t smem = 16 * (size_t)a.Nt;
-    cudaError_t e = set_smem((const void *)k_row_nl, smem);
-    if (e != cudaSuccess) return e;
-    k_row_nl<<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho);
+    NLSE_DISPATCH_NT(a.logNt, {
+        const size_t smem = row_smem_bytes<NT>(false);
+        cudaError_t e = set_smem(k_row_nl<NT>, smem);
+        if (e != cudaSuccess) return e;
+        k_row_nl<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho);
+    });
     return cudaGetLastError();
 }
 
 cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, float *rho,
                             float2 *u_out, int write_state, int do_scan, int apply_mask, cudaStream_t st) {
-    size_t smem = 20 * (size_t)a.Nt;
-    cudaError_t e = set_smem((const void *)k_row_next, smem);
-    if (e != cudaSuccess) return e;
-    k_row_next<<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask);
+    NLSE_DISPATCH_NT(a.logNt, {
+        const size_t smem = row_smem_bytes<NT>(true);
+        cudaError_t e = set_smem(k_row_next<NT>, smem);
+        if (e != cudaSuccess) return e;
+        k_row_next<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan,
+                                                              apply_mask);
+    });
     return cudaGetLastError();
 }
 

@@ -7,25 +7,27 @@
 static __constant__ float c_pow10[18] = {1e0f,  1e1f,  1e2f,  1e3f,  1e4f,  1e5f,  1e6f,  1e7f,  1e8f,
                                   1e9f,  1e10f, 1e11f, 1e12f, 1e13f, 1e14f, 1e15f, 1e16f, 1e17f};
 
+static __constant__ float c_ipow10[18] = {1e0f,   1e-1f,  1e-2f,  1e-3f,  1e-4f,  1e-5f,  1e-6f,  1e-7f,  1e-8f,
+                                          1e-9f,  1e-10f, 1e-11f, 1e-12f, 1e-13f, 1e-14f, 1e-15f, 1e-16f, 1e-17f};
+
 // photo-ionisation loss rate [1/m] before depletion, for a finite I >= 0.
+// Interval of the knots 10^d (1 + 0.01 m) holding clip(I): the decade from a
+// fast log10 corrected against the exact powers, m by one multiply; the
+// position s in the interval; the per-interval Hermite cubic (pre-scaled by
+// Kc invE2 / x_i); times x_i / (I + 1e-30 invE2).
 __device__ __forceinline__ float photo_rate(float I, const NLParams &p, const float4 *__restrict__ tab) {
-    float Ic = fminf(fmaxf(I, p.Imin), p.Imax);
-    int d = (int)floorf(log10f(Ic));
-    d = min(max(d, 0), 16);
-    if (Ic < c_pow10[d] && d > 0) --d;
-    else if (Ic >= c_pow10[d + 1] && d < 16) ++d;
-    int m = (int)((Ic / c_pow10[d] - 1.0f) * 100.0f);
-    m = min(max(m, 0), 899);
-    int i = min(900 * d + m, p.n_int - 1);
-    d = i / 900;
-    m = i - 900 * d;
-    const float p10 = c_pow10[d];
-    const float xi = p10 * (1.0f + 0.01f * (float)m);
-    const float s = (Ic - xi) / (0.01f * p10);
-    const float4 cf = __ldg(&tab[i]);
-    float V = fabsf(fmaf(s, fmaf(s, fmaf(s, cf.w, cf.z), cf.y), cf.x));
-    float r = V * (xi / (I + p.tiny_I));
-    return isfinite(r) ? r : 0.0f;
+    const float Ic = fminf(fmaxf(I, p.Imin), p.Imax);
+    int d = min(max(__float2int_rd(__log10f(Ic)), 0), 16);
+    if (Ic < c_pow10[d]) d = max(d - 1, 0);
+    else if (Ic >= c_pow10[d + 1]) d = min(d + 1, 16);
+    const float p10 = c_pow10[d], ip10 = c_ipow10[d];
+    int m = __float2int_rz(fmaf(Ic, ip10, -1.0f) * 100.0f);
+    m = min(max(m, 0), min(899, p.n_int - 1 - 900 * d));
+    const float xi = p10 * fmaf(0.01f, (float)m, 1.0f);
+    const float s = (Ic - xi) * (100.0f * ip10);
+    const float4 cf = __ldg(&tab[900 * d + m]);
+    const float V = fabsf(fmaf(s, fmaf(s, fmaf(s, cf.w, cf.z), cf.y), cf.x));
+    return V * __fdividef(xi, I + p.tiny_I);
 }
 
 // alpha(u, rho) and the raw sum it clamps, as split() computes them.

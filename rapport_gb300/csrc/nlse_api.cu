@@ -188,6 +188,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     sc.c_rec = (float)(d->dt * d->inv_tau_r);
     sc.na = (float)d->rho_max;
     sc.inv_na = (float)(1.0 / d->rho_max);
+    sc.x_tiny = (float)(d->rho_max * 1.4901161193847656e-08);  // 2^-26
     sc.lut_log_min = (float)d->lut_log_min;
     sc.lut_inv_dlog = (float)d->lut_inv_dlog;
     sc.Imin = (float)d->lut_Imin;

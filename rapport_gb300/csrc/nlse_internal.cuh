@@ -52,6 +52,7 @@ struct ScanParams {
     float c_rec;        // dt / tau_r
     float na;           // rho_max
     float inv_na;
+    float x_tiny;       // na * 2^-26: below it the depletion factor is exactly 1 in FP32
     float lut_log_min, lut_inv_dlog, Imin, Imax;
     int lut_n;
 };
@@ -221,56 +222,80 @@ __device__ __forceinline__ void dft_small(float2 *v) {
     else dft8<INV>(v);
 }
 
-// One Stockham autosort pass of radix R over a row of N points held in shared
-// memory: reads src, writes dst.  Ns = product of the radices already applied.
-// tw = forward twiddles exp(-2 pi i k / N), k < N (conjugated for INV).
-template <int R, bool INV>
+// Padded shared-memory index of a row held as float2: one pad slot per 16
+// points makes every Stockham pass (loads and the strided stores) within
+// 1.12x of conflict-free for 64-bit accesses (unpadded: 8-way on the first
+// pass).  A row of N points occupies fft_slots(N) float2.
+__host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 4); }
+__host__ __device__ __forceinline__ constexpr int fft_slots(int n) { return n + (n >> 4); }
+
+// One Stockham autosort pass of radix R over a row of N points (compile-time
+// sizes): reads src, writes dst (padded indexing).  NS = product of the
+// radices already applied; tw = forward twiddles exp(-2 pi i k / N).
+template <int R, bool INV, int N, int NS, int T>
 __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
-                                              int N, int Ns, const float2 *__restrict__ tw) {
-    const int nb = N / R;
-    const int tstride = N / (Ns * R);
-    for (int j = threadIdx.x; j < nb; j += blockDim.x) {
-        const int k = j & (Ns - 1);
-        float2 v[R];
+                                              const float2 *__restrict__ tw) {
+    constexpr int nb = N / R;
+    constexpr int tstride = N / (NS * R);
 #pragma unroll
-        for (int r = 0; r < R; ++r) v[r] = src[j + r * nb];
-        if (Ns > 1) {
+    for (int jj = 0; jj < (nb + T - 1) / T; ++jj) {
+        const int j = (int)threadIdx.x + jj * T;
+        if (nb % T == 0 || j < nb) {
+            const int k = j & (NS - 1);
+            float2 v[R];
 #pragma unroll
-            for (int r = 1; r < R; ++r) {
-                float2 w = __ldg(&tw[r * k * tstride]);
-                if (INV) w.y = -w.y;
-                v[r] = c_mul(v[r], w);
+            for (int r = 0; r < R; ++r) v[r] = src[pidx(j + r * nb)];
+            if (NS > 1) {
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    float2 w = __ldg(&tw[r * k * tstride]);
+                    if (INV) w.y = -w.y;
+                    v[r] = c_mul(v[r], w);
+                }
             }
-        }
-        dft_small<R, INV>(v);
-        const int d0 = (j - k) * R + k;
+            dft_small<R, INV>(v);
+            const int d0 = (j - k) * R + k;
 #pragma unroll
-        for (int r = 0; r < R; ++r) dst[d0 + r * Ns] = v[r];
+            for (int r = 0; r < R; ++r) dst[pidx(d0 + r * NS)] = v[r];
+        }
     }
 }
 
-// Full in-CTA FFT of one row (N = 2^logN, 2 <= N <= NLSE_MAX_NT) using two
-// shared buffers; returns the buffer holding the (unnormalised) result.
-// Radix-8 passes first, then one radix-4 or radix-2 pass for the remainder.
-template <bool INV>
-__device__ float2 *fft_row(float2 *buf0, float2 *buf1, int N, int logN, const float2 *__restrict__ tw) {
-    float2 *src = buf0, *dst = buf1;
-    int Ns = 1;
-    int n8 = logN / 3, rem = logN % 3;
-    for (int p = 0; p < n8; ++p) {
-        stockham_pass<8, INV>(src, dst, N, Ns, tw);
+// Remaining passes from NS on; radix 8 while it divides, then 4 or 2.
+template <int N, int NS, bool INV, int T>
+__device__ __forceinline__ float2 *fft_passes(float2 *src, float2 *dst, const float2 *__restrict__ tw) {
+    if constexpr (NS >= N) {
+        return src;
+    } else {
+        constexpr int REM = N / NS;
+        constexpr int R = (REM % 8 == 0) ? 8 : ((REM % 4 == 0) ? 4 : 2);
+        stockham_pass<R, INV, N, NS, T>(src, dst, tw);
         __syncthreads();
-        Ns *= 8;
-        float2 *t = src; src = dst; dst = t;
+        return fft_passes<N, NS * R, INV, T>(dst, src, tw);
     }
-    if (rem == 2) {
-        stockham_pass<4, INV>(src, dst, N, Ns, tw);
-        __syncthreads();
-        float2 *t = src; src = dst; dst = t;
-    } else if (rem == 1) {
-        stockham_pass<2, INV>(src, dst, N, Ns, tw);
-        __syncthreads();
-        float2 *t = src; src = dst; dst = t;
-    }
-    return src;
 }
+
+// Full in-CTA FFT of one row of N points (power of two, 16..8192) held in
+// buf0 (padded indexing), buf1 = scratch of the same size; returns the buffer
+// holding the unnormalised result.  Every thread of the CTA (T of them) calls it.
+template <int N, bool INV, int T = NLSE_ROW_THREADS>
+__device__ __forceinline__ float2 *fft_row(float2 *buf0, float2 *buf1, const float2 *__restrict__ tw) {
+    return fft_passes<N, 1, INV, T>(buf0, buf1, tw);
+}
+
+// Dispatch a runtime power-of-two size to a kernel template instantiated for
+// N = 16 .. 8192 (the macro body sees the compile-time constant NT).
+#define NLSE_DISPATCH_NT(logn, ...)                          \
+    switch (logn) {                                          \
+        case 4: { constexpr int NT = 16; __VA_ARGS__; break; }    \
+        case 5: { constexpr int NT = 32; __VA_ARGS__; break; }    \
+        case 6: { constexpr int NT = 64; __VA_ARGS__; break; }    \
+        case 7: { constexpr int NT = 128; __VA_ARGS__; break; }   \
+        case 8: { constexpr int NT = 256; __VA_ARGS__; break; }   \
+        case 9: { constexpr int NT = 512; __VA_ARGS__; break; }   \
+        case 10: { constexpr int NT = 1024; __VA_ARGS__; break; } \
+        case 11: { constexpr int NT = 2048; __VA_ARGS__; break; } \
+        case 12: { constexpr int NT = 4096; __VA_ARGS__; break; } \
+        case 13: { constexpr int NT = 8192; __VA_ARGS__; break; } \
+        default: return cudaErrorInvalidValue;               \
+    }

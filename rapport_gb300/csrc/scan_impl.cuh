@@ -31,8 +31,9 @@ __device__ __forceinline__ float lut_rate_dt(float I, const float *__restrict__ 
 // One step of the march and its derivative d f / d x.
 __device__ __forceinline__ float step_map(float x, float a, float b, const ScanParams &p, float *J,
                                           bool *clamped) {
-    // (na - x) is exact near saturation, so d is exactly 0 at x = na as in FP64
-    float d = fminf(fmaxf((p.na - x) * p.inv_na, 0.0f), 1.0f);
+    // (na - x) is exact near saturation, so d is exactly 0 at x = na as in FP64;
+    // below x_tiny the FP32 depletion factor is exactly 1 (and constant)
+    float d = x < p.x_tiny ? 1.0f : fminf(fmaxf((p.na - x) * p.inv_na, 0.0f), 1.0f);
     float z = fmaf(a, d, -p.c_rec);
     if (z > 80.0f) {
         // e^z overflows FP32 but not FP64 (below z = 709.78): there the reference
@@ -55,7 +56,7 @@ __device__ __forceinline__ float step_map(float x, float a, float b, const ScanP
     float az = fabsf(z);
     float ph = az > 1e-4f ? em1 / z : fmaf(z, fmaf(z, fmaf(z, 1.0f / 24.0f, 1.0f / 6.0f), 0.5f), 1.0f);
     float y = fmaf(e, x, b * d * ph);
-    float dd = (x > 0.0f && x < p.na) ? -p.inv_na : 0.0f;
+    float dd = (x >= p.x_tiny && x < p.na) ? -p.inv_na : 0.0f;
     float dph;  // phi1'(z) = (z e^z - (e^z - 1)) / z^2
     if (az < 0.1f)
         dph = fmaf(z, fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.0f / 840.0f, 1.0f / 144.0f), 1.0f / 30.0f),
@@ -187,7 +188,10 @@ static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ
         block_reduce(dmax, xmax, f, red);
         clamp_any |= f;
         if (clamp_any) break;
-        if (dmax <= SCAN_TOL * xmax) {
+        // The first sweep starts from x = 0, where the depletion is frozen at
+        // d = 1 (J = e^z, B = b phi1(z)): if the whole solution stays below
+        // x_tiny the map is exactly that affine map, so the sweep is exact.
+        if (dmax <= SCAN_TOL * xmax || (it == 0 && xmax < p.x_tiny)) {
             converged = 1;
             break;
         }
