@@ -140,7 +140,6 @@ def run_ours(args, rank, world, local_rank):
             ctx.propagate(u, rho, rs, w["dz"], Z, mode)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
-        ctx.profile_start(K * Z * 16 + 64)
         clk = ClockSampler(local_rank) if name == lead else None
         barrier()
         torch.cuda.synchronize()
@@ -152,6 +151,12 @@ def run_ours(args, rank, world, local_rank):
         torch.cuda.synchronize()
         barrier()
         clocks = clk.stop() if clk else None
+        # second, identical pass with per-launch events on the launching stream
+        # (kept out of the timed pass: recording them costs a few percent)
+        ctx.profile_start(K * Z * 16 + 64)
+        for i in range(K):
+            flush.fill_(float(i))
+            ctx.propagate(u, rho, rs, w["dz"], Z, mode)
         prof = ctx.profile_read()
         t_ms = sum(a.elapsed_time(b) for a, b in ev)
         if world > 1:
@@ -189,6 +194,35 @@ def run_ours(args, rank, world, local_rank):
     e2e = {"value": world * r["K"] * Z / (e_ms * 1e-3), "unit": "z-steps/s",
            "h2d_bytes_per_step": int(uh.numel() * 8), "d2h_bytes_per_step": int(uo.numel() * 8 + rho_h.numel() * 4)}
 
+    # ---------------------------------------------------------- batched form: B pulses of the same grid
+    batched = None
+    if args.batch > 0 and head == "split_bf16":
+        B = args.batch
+        env = [R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"] + i)(g["rr"], g["tt"], cfg, g)
+               for i in range(B)]
+        bt = _lib.Batch([cfg] * B, [g] * B)
+        bu = [torch.from_numpy(np.ascontiguousarray(e.astype(np.complex64))).to(dev) for e in env]
+        br = [torch.zeros(u0.shape, dtype=torch.float32, device=dev) for _ in range(B)]
+        for _ in range(args.warmup):
+            bt.propagate(bu, br, None, w["dz"], Z)
+        torch.cuda.synchronize()
+        KB = max(2, args.steps // 2)
+        bev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(KB)]
+        for i in range(KB):
+            flush.fill_(float(i))
+            bev[i][0].record()
+            bt.propagate(bu, br, None, w["dz"], Z)
+            bev[i][1].record()
+        torch.cuda.synchronize()
+        bms = sum(a.elapsed_time(b_) for a, b_ in bev)
+        assert bt.device_status() == 0 and all(bool(torch.isfinite(x).all().item()) for x in bu)
+        bval = world * B * KB * Z / (bms * 1e-3)
+        batched = {"pulses": B, "grid": "1024x2048 each (seeds 0..B-1)", "value": bval,
+                   "unit": "pulse-z-steps/s", "ms_per_step": bms / KB, "steps": KB,
+                   "vs_single_pulse": bval / r["zsteps_per_s"],
+                   "vs_plain_fp32": (bval / results["plain"]["zsteps_per_s"]) if "zsteps_per_s" in results.get("plain", {}) else None}
+        del bt, bu, br
+
     # ---------------------------------------------------------- roofline of the dominant kernel
     hbm, bf16, bf16_s, src = peaks()
     prof = r["prof"]
@@ -221,11 +255,13 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None, "dtype": "bf16x3-split + f32" if head == "split_bf16" else "f32",
         "data": "synthetic (seeded lens-focused Gaussian pulse with 1% noise)",
         "config": dict(CONFIG, form=head, z_steps_per_step=Z, parallelism=f"replicas{world}",
-                       l2="256 MB flush before each timed step (outside its events); inputs (24 MB) < L2"),
+                       l2="256 MB flush before each timed step (outside its events); inputs (24 MB) < L2",
+                       kernel_times="second identical pass of K steps with per-launch events"),
         "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
         "clocks": r["clocks"],
         "forms": {k: (round(v["zsteps_per_s"], 1) if "zsteps_per_s" in v else v) for k, v in results.items()},
+        "batched": batched,
     }
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_zsteps)
@@ -299,6 +335,7 @@ def main():
     ap.add_argument("--zsteps", type=int, default=50, help="z-steps per bench step")
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batch", type=int, default=8, help="pulses in the batched measurement (0 = skip)")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))

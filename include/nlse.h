@@ -152,6 +152,24 @@ int nlse_propagate(nlse_ctx *ctx, void *u, float *rho, float *rho_s, double dz,
 int nlse_debug_operator_product(nlse_ctx *ctx, const float *w, float *out, double dz,
                                 void *stream);
 
+/*
+ * Batches: many pulses, each with its own grid (Nr % 64 == 0, Nt % 256 == 0)
+ * and tables, advanced together in the split-BF16 form: per z-step ONE
+ * grouped tensor-core launch per half step over every pulse's tiles, and one
+ * row-kernel launch per distinct Nt.  The batch owns one context per pulse.
+ */
+typedef struct nlse_batch nlse_batch;
+int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch **out);
+/* u[i], rho[i], rho_s[i]: device pointers of pulse i (rho_s may be NULL or
+ * hold NULLs); same semantics as nlse_propagate for every pulse. */
+int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const *rho,
+                         float *const *rho_s, double dz, int nsteps, void *stream);
+int nlse_batch_get_context(nlse_batch *b, int i, nlse_ctx **out);
+int nlse_batch_set_split_terms(nlse_batch *b, int a_terms);
+int nlse_batch_device_status(nlse_batch *b, int *word);
+int nlse_batch_get_last_error(const nlse_batch *b, char *buf, size_t len);
+void nlse_batch_destroy(nlse_batch *b);
+
 /* Number of BF16 terms carrying E in the split mode: 3 (default; 4 MMAs per
  * k-slice) or 2 (the plain hi/lo scheme, 3 MMAs). */
 int nlse_set_split_terms(nlse_ctx *ctx, int a_terms);

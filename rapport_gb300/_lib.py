@@ -21,7 +21,9 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
-           "nlse_half_linear_noalloc",
+           "nlse_half_linear_noalloc", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
+           "nlse_batch_set_split_terms", "nlse_batch_device_status", "nlse_batch_get_last_error",
+           "nlse_batch_destroy",
            "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
            "nlse_get_last_error", "nlse_destroy", "nlse_version")
 
@@ -76,8 +78,16 @@ def load():
     lib.nlse_profile_read.argtypes = [_P, ctypes.POINTER(_I), ctypes.POINTER(_D), _I, ctypes.POINTER(_I)]
     lib.nlse_kernel_name.argtypes = [_I]
     lib.nlse_kernel_name.restype = ctypes.c_char_p
+    lib.nlse_batch_create.argtypes = [ctypes.POINTER(GridDesc), _I, ctypes.POINTER(_P)]
+    lib.nlse_batch_propagate.argtypes = [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), _D, _I, _P]
+    lib.nlse_batch_get_context.argtypes = [_P, _I, ctypes.POINTER(_P)]
+    lib.nlse_batch_set_split_terms.argtypes = [_P, _I]
+    lib.nlse_batch_device_status.argtypes = [_P, ctypes.POINTER(_I)]
+    lib.nlse_batch_get_last_error.argtypes = [_P, ctypes.c_char_p, ctypes.c_size_t]
+    lib.nlse_batch_destroy.argtypes = [_P]
+    lib.nlse_batch_destroy.restype = None
     for name in EXPORTS:
-        if name not in ("nlse_destroy", "nlse_version", "nlse_kernel_name"):
+        if name not in ("nlse_destroy", "nlse_version", "nlse_kernel_name", "nlse_batch_destroy"):
             getattr(lib, name).restype = _I
     _lib = lib
     return lib
@@ -184,7 +194,7 @@ class Context:
 
     def __del__(self):
         h = getattr(self, "h", None)
-        if h is not None and h.value:
+        if h is not None and h.value and not getattr(self, "_borrowed", False):
             try:
                 self.lib.nlse_destroy(h)
             except Exception:
@@ -273,3 +283,81 @@ class Context:
         v = _I(0)
         _check(self.lib, self.h, self.lib.nlse_scan_fallback_rows(self.h, ctypes.byref(v)))
         return v.value
+
+
+class Batch:
+    """Many pulses (each its own Config / grid) advanced together in the split-BF16
+    form: nlse_batch_create / nlse_batch_propagate."""
+
+    def __init__(self, cfgs, grids):
+        import torch
+        if not torch.cuda.is_available():
+            raise RuntimeError("rapport_gb300 needs a CUDA device (no CPU path exists)")
+        self.lib = load()
+        torch.cuda.init()
+        descs = (GridDesc * len(cfgs))()
+        self._keep = []
+        self.shapes = []
+        for i, (c, g) in enumerate(zip(cfgs, grids)):
+            d, keep = make_desc(c, g)
+            descs[i] = d
+            self._keep.append(keep)
+            self.shapes.append((d.Nr, d.Nt))
+        h = _P()
+        st = self.lib.nlse_batch_create(descs, len(cfgs), ctypes.byref(h))
+        if st != NLSE_OK:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.nlse_batch_get_last_error(None, buf, 512)
+            raise NLSEError(st, buf.value.decode(errors="replace"))
+        self.h = h
+        self.n = len(cfgs)
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value:
+            try:
+                self.lib.nlse_batch_destroy(h)
+            except Exception:
+                pass
+            self.h = None
+
+    def _ptrs(self, ts, dtype, name, allow_none=False):
+        import torch
+        arr = (_P * self.n)()
+        for i, t in enumerate(ts):
+            if t is None and allow_none:
+                arr[i] = None
+                continue
+            if t.dtype != dtype or tuple(t.shape) != self.shapes[i] or not t.is_contiguous() or not t.is_cuda:
+                raise ValueError(f"{name}[{i}] must be a contiguous CUDA {dtype} tensor of shape {self.shapes[i]}")
+            arr[i] = t.data_ptr()
+        return arr
+
+    def propagate(self, us, rhos, rho_ss, dz, nsteps):
+        import torch
+        u = self._ptrs(us, torch.complex64, "u")
+        r = self._ptrs(rhos, torch.float32, "rho")
+        s = self._ptrs(rho_ss, torch.float32, "rho_s", allow_none=True) if rho_ss is not None else None
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        status = self.lib.nlse_batch_propagate(self.h, u, r, s, float(dz), int(nsteps), st)
+        if status != NLSE_OK:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.nlse_batch_get_last_error(self.h, buf, 512)
+            raise NLSEError(status, buf.value.decode(errors="replace"))
+
+    def set_split_terms(self, n):
+        _check(self.lib, None, self.lib.nlse_batch_set_split_terms(self.h, int(n)))
+
+    def device_status(self):
+        w = _I(0)
+        self.lib.nlse_batch_device_status(self.h, ctypes.byref(w))
+        return w.value
+
+    def context_profile(self):
+        """The first pulse's context (the batch records its launches there)."""
+        c = _P()
+        _check(self.lib, None, self.lib.nlse_batch_get_context(self.h, 0, ctypes.byref(c)))
+        ctx = Context.__new__(Context)
+        ctx.lib, ctx.h, ctx.Nr, ctx.Nt = self.lib, c, self.shapes[0][0], self.shapes[0][1]
+        ctx._borrowed = True
+        return ctx

@@ -140,10 +140,12 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((uint32_t)(TC_BN >> 3) << 17) |
                             ((uint32_t)(TC_BM >> 4) << 24);
 
+// One 128 x 256 output tile at (m0, n0) of D[M x N] = A[M x K] B[K x N]; every
+// thread of the CTA calls it.  tmA / tmB: generic addresses of the tensor maps
+// (kernel-parameter or global memory).
 template <int A_TERMS>
-__global__ void __launch_bounds__(TC_THREADS, 1)
-k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-          float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
+__device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensorMap *tmB, float *__restrict__ D,
+                                          int M, int N, int K, int m0, int n0, int *__restrict__ err) {
     constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;  // one term, 16 KB
     constexpr uint32_t B_BYTES = TC_BK * TC_BN * 2;  // one term, 32 KB
     constexpr uint32_t B_BOX = 64 * TC_BK * 2;       // one 64-column box, 8 KB
@@ -155,8 +157,6 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
     __shared__ int abort_flag, issued;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n_tiles = N / TC_BN;
-    const int m0 = (blockIdx.x / n_tiles) * TC_BM, n0 = (blockIdx.x % n_tiles) * TC_BN;
     const int KB = K / TC_BK;
 
     if (threadIdx.x == 0) {
@@ -193,12 +193,12 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
             uint8_t *st = smem + (size_t)s * STAGE;
             mbar_expect_tx(&full_bar[s], STAGE);
 #pragma unroll
-            for (int t = 0; t < A_TERMS; ++t) tma_load_2d(st + t * A_BYTES, &tmA, &full_bar[s], kb * TC_BK, t * M + m0);
+            for (int t = 0; t < A_TERMS; ++t) tma_load_2d(st + t * A_BYTES, tmA, &full_bar[s], kb * TC_BK, t * M + m0);
 #pragma unroll
             for (int t = 0; t < 2; ++t)
 #pragma unroll
                 for (int j = 0; j < TC_BN / 64; ++j)
-                    tma_load_2d(st + A_TERMS * A_BYTES + t * B_BYTES + j * B_BOX, &tmB, &full_bar[s], n0 + 64 * j,
+                    tma_load_2d(st + A_TERMS * A_BYTES + t * B_BYTES + j * B_BOX, tmB, &full_bar[s], n0 + 64 * j,
                                 t * K + kb * TC_BK);
             issued = kb + 1;
         }
@@ -265,8 +265,44 @@ k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUten
     }
 }
 
+template <int A_TERMS>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+          float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
+    const int n_tiles = N / TC_BN;
+    gemm_tile<A_TERMS>(&tmA, &tmB, D, M, N, K, (blockIdx.x / n_tiles) * TC_BM, (blockIdx.x % n_tiles) * TC_BN, err);
+}
+
+// Grouped product over many pulses: CTA b computes tiles[b] of pulse tiles[b].pulse,
+// whose A / B tensor maps are maps[2 p] / maps[2 p + 1] (global memory, written
+// by the host before the launch).
+template <int A_TERMS>
+__global__ void __launch_bounds__(TC_THREADS, 1)
+k_gemm_tc_grouped(const CUtensorMap *__restrict__ maps, const BatchPulse *__restrict__ P,
+                  const GemmTile *__restrict__ tiles, int *__restrict__ err) {
+    const GemmTile t = tiles[blockIdx.x];
+    const BatchPulse &q = P[t.pulse];
+    gemm_tile<A_TERMS>(maps + 2 * t.pulse, maps + 2 * t.pulse + 1, q.D, q.M, q.N, q.K, t.m0, t.n0, err);
+}
+
 static size_t tc_smem_bytes(int a_terms) {
     return (size_t)TC_STAGES * (a_terms * TC_BM * TC_BK * 2 + 2 * TC_BK * TC_BN * 2) + 1024;
+}
+
+cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
+                                   int a_terms, int *err, cudaStream_t stream) {
+    const size_t smem = tc_smem_bytes(a_terms);
+    cudaError_t e;
+    if (a_terms == 3) {
+        e = cudaFuncSetAttribute(k_gemm_tc_grouped<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gemm_tc_grouped<3><<<ntiles, TC_THREADS, smem, stream>>>(maps, P, tiles, err);
+    } else {
+        e = cudaFuncSetAttribute(k_gemm_tc_grouped<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        k_gemm_tc_grouped<2><<<ntiles, TC_THREADS, smem, stream>>>(maps, P, tiles, err);
+    }
+    return cudaGetLastError();
 }
 
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,

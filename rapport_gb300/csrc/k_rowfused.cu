@@ -83,11 +83,10 @@ __host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
 
 // Entry: physical u (interleaved) -> w = F[u] (state); optionally rho = march(|u|^2).
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
-k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb,
-            float *__restrict__ rho, int do_scan) {
+__device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, const float2 *__restrict__ u,
+                                               float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb,
+                                               float *__restrict__ rho, int do_scan) {
     extern __shared__ float2 sm2[];
-    const int r = blockIdx.x;
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
     const float2 *g = u + (size_t)r * NT;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
@@ -109,11 +108,10 @@ k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F3
 
 // First half step's spectral end + the nonlinear block + forward FFT.
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
-k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-         const float *__restrict__ rho) {
+__device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
+                                            __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+                                            const float *__restrict__ rho) {
     extern __shared__ float2 sm2[];
-    const int r = blockIdx.x;
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
     load_mw_row<NT>(b0, r, a, F32, D, 1.0f / (float)NT);
     __syncthreads();
@@ -132,11 +130,11 @@ k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb
 // Second half step's spectral end + mask_r: the next state w', and optionally
 // the physical field (u_out) and the next carrier march (rho).
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
-k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-           float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask) {
+__device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
+                                              __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+                                              float *__restrict__ rho, float2 *__restrict__ u_out, int write_state,
+                                              int do_scan, int apply_mask) {
     extern __shared__ float2 sm2[];
-    const int r = blockIdx.x;
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
     load_mw_row<NT>(b0, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f);
     __syncthreads();
@@ -153,6 +151,53 @@ k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ 
     }
     if (!do_scan) return;
     march_row<NT>(R, R == b0 ? b1 : b0, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), inv, r, a, rho);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb,
+            float *__restrict__ rho, int do_scan) {
+    row_entry_body<NT>(a, blockIdx.x, u, F32, Fb, rho, do_scan);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+         const float *__restrict__ rho) {
+    row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+           float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask) {
+    row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask);
+}
+
+// ------------------------------------------------------------------ batched (many pulses, one time-grid class)
+// work[b] = (pulse, row) for CTA b; every pulse of the class has the same N_t.
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int do_scan) {
+    const int2 w = work[blockIdx.x];
+    const BatchPulse &q = P[w.x];
+    row_entry_body<NT>(q.a, w.y, q.u, q.F32, q.Fb, q.rho, do_scan);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work) {
+    const int2 w = work[blockIdx.x];
+    const BatchPulse &q = P[w.x];
+    row_nl_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last) {
+    const int2 w = work[blockIdx.x];
+    const BatchPulse &q = P[w.x];
+    row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1);
 }
 
 template <typename K>
@@ -190,6 +235,28 @@ cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb
         if (e != cudaSuccess) return e;
         k_row_next<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan,
                                                               apply_mask);
+    });
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
+                             cudaStream_t st) {
+    NLSE_DISPATCH_NT(logNt, {
+        const size_t smem = row_smem_bytes<NT>(kind != 1);
+        cudaError_t e;
+        if (kind == 0) {
+            e = set_smem(k_row_entry_b<NT>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_entry_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, flag);
+        } else if (kind == 1) {
+            e = set_smem(k_row_nl_b<NT>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_nl_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work);
+        } else {
+            e = set_smem(k_row_next_b<NT>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_next_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, flag);
+        }
     });
     return cudaGetLastError();
 }

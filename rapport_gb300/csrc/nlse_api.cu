@@ -677,3 +677,230 @@ extern "C" const char *nlse_kernel_name(int kid) {
         default: return "";
     }
 }
+
+// ---------------------------------------------------------------- batches of pulses
+struct nlse_batch {
+    nlse_error_slot err;
+    int n, a_terms;
+    nlse_ctx **ctx;          // one context per pulse (tables, operator, state buffers)
+    BatchPulse *h_pulses;    // pinned staging of the per-pulse table
+    BatchPulse *d_pulses;
+    CUtensorMap *d_maps;     // 2 per pulse: A, B
+    GemmTile *d_tiles;
+    int ntiles;
+    struct Class {
+        int logNt, nblocks;
+        int2 *d_work;
+    } cls[16];
+    int ncls;
+    int *d_flag;
+    cudaEvent_t staged;      // the last upload of h_pulses has been consumed
+    double last_dz;
+    void *last_ptrs[3];      // u[0], rho[0] of the last upload (cheap change check)
+    int uploaded;
+};
+
+static void batch_free(nlse_batch *b) {
+    if (!b) return;
+    if (b->ctx)
+        for (int i = 0; i < b->n; ++i) nlse_destroy(b->ctx[i]);
+    free(b->ctx);
+    if (b->h_pulses) cudaFreeHost(b->h_pulses);
+    void *ptrs[] = {b->d_pulses, b->d_maps, b->d_tiles, b->d_flag};
+    for (void *p : ptrs)
+        if (p) cudaFree(p);
+    for (int c = 0; c < b->ncls; ++c)
+        if (b->cls[c].d_work) cudaFree(b->cls[c].d_work);
+    if (b->staged) cudaEventDestroy(b->staged);
+    free(b);
+}
+
+extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch **out) {
+    nlse_error_slot *gerr = &g_create_err;
+    if (!out || !descs || n < 1) {
+        nlse_set_error(gerr, NLSE_ERR_INVALID_ARG, "batch: descs/out NULL or n < 1");
+        return NLSE_ERR_INVALID_ARG;
+    }
+    *out = nullptr;
+    nlse_batch *b = (nlse_batch *)calloc(1, sizeof(nlse_batch));
+    if (!b) return NLSE_ERR_INVALID_ARG;
+    b->n = n;
+    b->a_terms = 3;
+    b->last_dz = NAN;
+    b->ctx = (nlse_ctx **)calloc(n, sizeof(nlse_ctx *));
+#define BATCH_FAIL(st, ...)                       \
+    do {                                         \
+        nlse_set_error(gerr, (st), __VA_ARGS__); \
+        batch_free(b);                           \
+        return (st);                             \
+    } while (0)
+    for (int i = 0; i < n; ++i) {
+        int st = nlse_create(&descs[i], &b->ctx[i]);
+        if (st != NLSE_OK) {
+            char msg[400];
+            snprintf(msg, sizeof(msg), "%s", gerr->msg);
+            BATCH_FAIL(st, "pulse %d: %s", i, msg);
+        }
+        if (!b->ctx[i]->split_ok)
+            BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: batches run the split-BF16 form, which needs Nr %% 64 == 0 "
+                                             "and Nt %% 256 == 0",
+                       i);
+    }
+    std::vector<GemmTile> tiles;
+    std::vector<CUtensorMap> maps(2 * (size_t)n);
+    int logs[16], nlog = 0;
+    std::vector<std::vector<int2>> work(16);
+    for (int i = 0; i < n; ++i) {
+        nlse_ctx *c = b->ctx[i];
+        memcpy(&maps[2 * i], &c->tmA, sizeof(CUtensorMap));
+        memcpy(&maps[2 * i + 1], &c->tmB, sizeof(CUtensorMap));
+        const int M = 2 * c->Nr;
+        for (int m0 = 0; m0 < M; m0 += 128)
+            for (int n0 = 0; n0 < c->Nt; n0 += 256) tiles.push_back(GemmTile{i, m0, n0, 0});
+        int k = 0;
+        while (k < nlog && logs[k] != c->logNt) ++k;
+        if (k == nlog) logs[nlog++] = c->logNt;
+        for (int r = 0; r < c->Nr; ++r) work[k].push_back(make_int2(i, r));
+    }
+    // large tiles first: the big pulses' tiles start in the first waves
+    b->ntiles = (int)tiles.size();
+    cudaError_t e = cudaMalloc((void **)&b->d_tiles, tiles.size() * sizeof(GemmTile));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_maps, maps.size() * sizeof(CUtensorMap));
+    if (e == cudaSuccess)
+        e = cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pulses, n * sizeof(BatchPulse));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_pulses, n * sizeof(BatchPulse));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_flag, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(b->d_flag, 0, 4 * sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
+    b->ncls = nlog;
+    for (int k = 0; k < nlog && e == cudaSuccess; ++k) {
+        b->cls[k].logNt = logs[k];
+        b->cls[k].nblocks = (int)work[k].size();
+        e = cudaMalloc((void **)&b->cls[k].d_work, work[k].size() * sizeof(int2));
+        if (e == cudaSuccess)
+            e = cudaMemcpy(b->cls[k].d_work, work[k].data(), work[k].size() * sizeof(int2), cudaMemcpyHostToDevice);
+    }
+    if (e != cudaSuccess) BATCH_FAIL(NLSE_ERR_CUDA, "batch set-up: %s", cudaGetErrorString(e));
+#undef BATCH_FAIL
+    *out = b;
+    return NLSE_OK;
+}
+
+extern "C" void nlse_batch_destroy(nlse_batch *b) {
+    if (!b) return;
+    cudaDeviceSynchronize();
+    batch_free(b);
+}
+
+extern "C" int nlse_batch_get_context(nlse_batch *b, int i, nlse_ctx **out) {
+    if (!b || !out || i < 0 || i >= b->n) return NLSE_ERR_INVALID_ARG;
+    *out = b->ctx[i];
+    return NLSE_OK;
+}
+
+extern "C" int nlse_batch_set_split_terms(nlse_batch *b, int a_terms) {
+    if (!b || (a_terms != 2 && a_terms != 3)) return NLSE_ERR_INVALID_ARG;
+    b->a_terms = a_terms;
+    return NLSE_OK;
+}
+
+extern "C" int nlse_batch_device_status(nlse_batch *b, int *word) {
+    if (!b) return NLSE_ERR_INVALID_ARG;
+    int h[4];
+    NLSE_CUDA_TRY(&b->err, cudaMemcpy(h, b->d_flag, sizeof(h), cudaMemcpyDeviceToHost));
+    if (word) *word = h[0];
+    return h[0] ? NLSE_ERR_TIMEOUT : NLSE_OK;
+}
+
+extern "C" int nlse_batch_get_last_error(const nlse_batch *b, char *buf, size_t len) {
+    const nlse_error_slot *e = b ? &b->err : &g_create_err;
+    if (buf && len) {
+        strncpy(buf, e->msg, len - 1);
+        buf[len - 1] = 0;
+    }
+    return e->status;
+}
+
+extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const *rho, float *const *rho_s, double dz,
+                                    int nsteps, void *stream) {
+    if (!b || !u || !rho) return NLSE_ERR_INVALID_ARG;
+    if (nsteps < 0) {
+        nlse_set_error(&b->err, NLSE_ERR_INVALID_ARG, "nsteps < 0");
+        return NLSE_ERR_INVALID_ARG;
+    }
+    if (nsteps == 0) return NLSE_OK;
+    cudaStream_t st = (cudaStream_t)stream;
+    nlse_ctx *c = b->ctx[0];  // profiling records go to the first pulse's context
+    bool changed = !(dz == b->last_dz) || !b->uploaded;
+    for (int i = 0; i < b->n; ++i) {
+        if (!field_ok(b->ctx[i], u[i], "u") || !field_ok(b->ctx[i], rho[i], "rho")) {
+            nlse_set_error(&b->err, NLSE_ERR_INVALID_ARG, "pulse %d: %s", i, b->ctx[i]->err.msg);
+            return NLSE_ERR_INVALID_ARG;
+        }
+        int s = split_ready(b->ctx[i], dz, st);
+        if (s) {
+            nlse_set_error(&b->err, s, "pulse %d: %s", i, b->ctx[i]->err.msg);
+            return s;
+        }
+        if (b->uploaded && (b->h_pulses[i].u != (float2 *)u[i] || b->h_pulses[i].rho != rho[i])) changed = true;
+    }
+    if (changed) {
+        // the previous upload must be consumed before the staging buffer is rewritten
+        NLSE_CUDA_TRY(&b->err, cudaEventSynchronize(b->staged));
+        for (int i = 0; i < b->n; ++i) {
+            nlse_ctx *q = b->ctx[i];
+            BatchPulse &P = b->h_pulses[i];
+            P.a = row_args(q, dz);
+            P.F32 = q->d_F32;
+            P.Fb = q->d_Fb;
+            P.D = q->d_D;
+            P.rho = rho[i];
+            P.u = (float2 *)u[i];
+            P.M = 2 * q->Nr;
+            P.N = q->Nt;
+            P.K = 2 * q->Nr;
+        }
+        NLSE_CUDA_TRY(&b->err, cudaMemcpyAsync(b->d_pulses, b->h_pulses, b->n * sizeof(BatchPulse),
+                                               cudaMemcpyHostToDevice, st));
+        NLSE_CUDA_TRY(&b->err, cudaEventRecord(b->staged, st));
+        b->last_dz = dz;
+        b->uploaded = 1;
+    }
+    if (rho_s)
+        for (int i = 0; i < b->n; ++i)
+            if (rho_s[i])
+                NLSE_CUDA_TRY(&b->err, cudaMemsetAsync(rho_s[i], 0,
+                                                       (size_t)b->ctx[i]->Nr * b->ctx[i]->Nt * sizeof(float), st));
+#define BSEQ(kid, call, what)                                                          \
+    do {                                                                               \
+        PROF(kid);                                                                     \
+        cudaError_t e_ = (call);                                                       \
+        if (e_ != cudaSuccess) {                                                       \
+            nlse_set_error(&b->err, NLSE_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e_)); \
+            return NLSE_ERR_CUDA;                                                      \
+        }                                                                              \
+    } while (0)
+    for (int k = 0; k < b->ncls; ++k)
+        BSEQ(K_ROW_ENTRY,
+             launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, st),
+             "batch row entry");
+    for (int it = 0; it < nsteps; ++it) {
+        const int last = it == nsteps - 1;
+        BSEQ(K_GEMM_TC, launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, b->d_flag, st),
+             "batch gemm");
+        for (int k = 0; k < b->ncls; ++k)
+            BSEQ(K_ROW_NL, launch_row_batch(1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 0, st),
+                 "batch row nonlinear");
+        BSEQ(K_GEMM_TC, launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, b->d_flag, st),
+             "batch gemm");
+        for (int k = 0; k < b->ncls; ++k)
+            BSEQ(K_ROW_NEXT,
+                 launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last, st),
+                 "batch row next");
+    }
+#undef BSEQ
+    return NLSE_OK;
+}

@@ -71,6 +71,22 @@ struct RowFusedArgs {
     int *stats;
 };
 
+// One pulse of a batch, as the batched kernels see it (device memory).
+struct BatchPulse {
+    RowFusedArgs a;
+    float *F32;
+    __nv_bfloat16 *Fb;
+    float *D;
+    float *rho;
+    float2 *u;
+    int M, N, K;  // GEMM sizes: 2Nr, Nt, 2Nr
+};
+
+// One 128 x 256 tile of the grouped tensor-core product.
+struct GemmTile {
+    int pulse, m0, n0, pad;
+};
+
 // ---------------------------------------------------------------- context
 struct nlse_ctx {
     nlse_error_slot err;
@@ -150,6 +166,11 @@ cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, c
                                          const float2 *Pr, cudaStream_t stream);
 void nlse_set_thread_error(int status, const char *msg);
 cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st);
+// kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call)
+cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
+                             cudaStream_t st);
+cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
+                                   int a_terms, int *err, cudaStream_t stream);
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
                              int do_scan, cudaStream_t st);
 cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,

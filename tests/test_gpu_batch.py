@@ -1,0 +1,78 @@
+"""Batches of pulses with uneven grids (nlse_batch_*), split-BF16 form.
+
+A batch runs the same per-pulse arithmetic as a single-pulse context (grouped
+tensor-core launch over every pulse's tiles, one row launch per time-grid
+class), so every pulse must come out bit-identical to its single-context
+split-BF16 run, and within the parity tolerance of the FP64 oracle."""
+import numpy as np
+import pytest
+
+import nlse_oracle as O
+from conftest import rel_l2
+from gpu_util import dev, host
+
+pytestmark = pytest.mark.gpu
+
+# (Nr, Nt, R_max, w0, T_half, fwhm, E_uJ, f) -- three grids, two time classes
+PULSES = [(64, 256, 1e-4, 1e-5, 3e-13, 100e-15, 2.0, 1e-2),
+          (128, 512, 2e-4, 2e-5, 4e-13, 80e-15, 6.0, 2e-2),
+          (64, 512, 1.5e-4, 1.5e-5, 3e-13, 120e-15, 3.0, 1.5e-2)]
+DZ, STEPS = 5e-6, 6
+
+
+def _setup():
+    import rapport_gb300 as R
+    cfgs, grids, u0s, ogs = [], [], [], []
+    for i, (Nr, Nt, Rm, w0, Th, fw, E, f) in enumerate(PULSES):
+        cfg = R.workload_config(Nr, Nt, Rm, w0, Th, DZ, STEPS)
+        g = R.build_grids(cfg)
+        cfgs.append(cfg)
+        grids.append(g)
+        u0s.append(R.envelope_lens(w0, fw, E, f, i)(g["rr"], g["tt"], cfg, g))
+        ogs.append(O.OracleGrid(O.workload_config(Nr, Nt, Rm, w0, Th)))
+    return cfgs, grids, u0s, ogs
+
+
+def test_batch_matches_single_contexts_and_oracle():
+    from rapport_gb300 import _lib
+    cfgs, grids, u0s, ogs = _setup()
+    b = _lib.Batch(cfgs, grids)
+    us = [dev(u) for u in u0s]
+    rhos = [dev(np.zeros(u.shape)) for u in u0s]
+    rss = [dev(np.ones(u.shape)) for u in u0s]
+    b.propagate(us, rhos, rss, DZ, STEPS)
+    assert b.device_status() == 0
+    for i, (cfg, g, u0, og) in enumerate(zip(cfgs, grids, u0s, ogs)):
+        ctx = _lib.Context(cfg, g)
+        u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+        ctx.propagate(u, rho, rs, DZ, STEPS, _lib.MODE_SPLIT_BF16)
+        assert np.array_equal(host(us[i]), host(u)), i
+        assert np.array_equal(host(rhos[i]), host(rho)), i
+        assert np.all(host(rss[i]) == 0)
+        uo, rho_o, _ = og.propagate(u0.copy(), STEPS, DZ)
+        assert rel_l2(host(us[i]), uo) < 5e-5, i
+        assert np.abs(host(rhos[i]) - rho_o).max() <= 1e-3 * max(rho_o.max(), 1e-30), i
+
+
+def test_batch_two_calls_equal_one():
+    from rapport_gb300 import _lib
+    cfgs, grids, u0s, _ = _setup()
+    b = _lib.Batch(cfgs, grids)
+    a = [dev(u) for u in u0s]
+    ra = [dev(np.zeros(u.shape)) for u in u0s]
+    b.propagate(a, ra, None, DZ, STEPS)
+    c = [dev(u) for u in u0s]
+    rc = [dev(np.zeros(u.shape)) for u in u0s]
+    b.propagate(c, rc, None, DZ, STEPS // 2)
+    b.propagate(c, rc, None, DZ, STEPS - STEPS // 2)
+    for i in range(len(a)):
+        # a call boundary rounds the field through the physical domain once
+        assert rel_l2(host(c[i]), host(a[i])) < 1e-6
+
+
+def test_batch_rejects_untileable_grid():
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    cfg = R.workload_config(64, 128, 1e-4, 1e-5, 3e-13, DZ, 1)
+    with pytest.raises(_lib.NLSEError, match="split-BF16"):
+        _lib.Batch([cfg], [R.build_grids(cfg)])
