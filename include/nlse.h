@@ -170,6 +170,13 @@ int nlse_batch_device_status(nlse_batch *b, int *word);
 int nlse_batch_get_last_error(const nlse_batch *b, char *buf, size_t len);
 void nlse_batch_destroy(nlse_batch *b);
 
+/* Tensor-core pipeline of the split mode: 0 = 64-deep k slices x 2 stages,
+ * 1 = 32-deep x 4 stages, -1 = autotune (default: the first split-mode call
+ * times both on the live operands and keeps the faster; that call
+ * synchronises its stream, so make it before any stream capture). */
+int nlse_set_gemm_variant(nlse_ctx *ctx, int variant);
+int nlse_get_gemm_variant(const nlse_ctx *ctx);
+
 /* Number of BF16 terms carrying E in the split mode: 3 (default; 4 MMAs per
  * k-slice) or 2 (the plain hi/lo scheme, 3 MMAs). */
 int nlse_set_split_terms(nlse_ctx *ctx, int a_terms);

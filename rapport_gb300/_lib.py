@@ -21,7 +21,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
-           "nlse_half_linear_noalloc", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
+           "nlse_half_linear_noalloc", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
            "nlse_batch_set_split_terms", "nlse_batch_device_status", "nlse_batch_get_last_error",
            "nlse_batch_destroy",
            "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
@@ -78,6 +78,8 @@ def load():
     lib.nlse_profile_read.argtypes = [_P, ctypes.POINTER(_I), ctypes.POINTER(_D), _I, ctypes.POINTER(_I)]
     lib.nlse_kernel_name.argtypes = [_I]
     lib.nlse_kernel_name.restype = ctypes.c_char_p
+    lib.nlse_set_gemm_variant.argtypes = [_P, _I]
+    lib.nlse_get_gemm_variant.argtypes = [_P]
     lib.nlse_batch_create.argtypes = [ctypes.POINTER(GridDesc), _I, ctypes.POINTER(_P)]
     lib.nlse_batch_propagate.argtypes = [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), _D, _I, _P]
     lib.nlse_batch_get_context.argtypes = [_P, _I, ctypes.POINTER(_P)]
@@ -236,6 +238,12 @@ class Context:
 
     def set_split_terms(self, n):
         _check(self.lib, self.h, self.lib.nlse_set_split_terms(self.h, int(n)))
+
+    def set_gemm_variant(self, v):
+        _check(self.lib, self.h, self.lib.nlse_set_gemm_variant(self.h, int(v)))
+
+    def gemm_variant(self):
+        return self.lib.nlse_get_gemm_variant(self.h)
 
     def device_status(self):
         w = _I(0)

@@ -34,8 +34,6 @@
 
 #define TC_BM 128
 #define TC_BN 256
-#define TC_BK 64
-#define TC_STAGES 2
 #define TC_THREADS 192
 #define TC_WAIT_NS 2000000000ull
 
@@ -90,13 +88,13 @@ __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, u
 }
 
 // Shared-memory matrix descriptor (tcgen05): start, leading/stride byte
-// offsets (>> 4), version 1, 128-byte swizzle.
-__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo) {
+// offsets (>> 4), version 1, swizzle mode (2 = 128-byte, 4 = 64-byte).
+__device__ __forceinline__ uint64_t smem_desc(uint32_t saddr, uint32_t lbo, uint32_t sbo, uint32_t swz) {
     uint64_t d = (uint64_t)((saddr >> 4) & 0x3FFFu);
     d |= (uint64_t)((lbo >> 4) & 0x3FFFu) << 16;
     d |= (uint64_t)((sbo >> 4) & 0x3FFFu) << 32;
     d |= (uint64_t)1 << 46;
-    d |= (uint64_t)2 << 61;
+    d |= (uint64_t)swz << 61;
     return d;
 }
 
@@ -142,14 +140,18 @@ constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((
 
 // One 128 x 256 output tile at (m0, n0) of D[M x N] = A[M x K] B[K x N]; every
 // thread of the CTA calls it.  tmA / tmB: generic addresses of the tensor maps
-// (kernel-parameter or global memory).
-template <int A_TERMS>
+// (kernel-parameter or global memory).  TC_BK = k depth of one pipeline stage
+// (64: A rows of 128 B, 128-byte swizzle; 32: rows of 64 B, 64-byte swizzle),
+// TC_STAGES stages in the ring.
+template <int A_TERMS, int TC_BK, int TC_STAGES>
 __device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensorMap *tmB, float *__restrict__ D,
                                           int M, int N, int K, int m0, int n0, int *__restrict__ err) {
-    constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;  // one term, 16 KB
-    constexpr uint32_t B_BYTES = TC_BK * TC_BN * 2;  // one term, 32 KB
-    constexpr uint32_t B_BOX = 64 * TC_BK * 2;       // one 64-column box, 8 KB
+    constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;  // one term
+    constexpr uint32_t B_BYTES = TC_BK * TC_BN * 2;  // one term
+    constexpr uint32_t B_BOX = 64 * TC_BK * 2;       // one 64-column box
     constexpr uint32_t STAGE = A_TERMS * A_BYTES + 2 * B_BYTES;
+    constexpr uint32_t A_SWZ = TC_BK == 64 ? 2u : 4u;
+    constexpr uint32_t A_SBO = TC_BK * 2 * 8;        // 8 rows of one swizzle atom
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
     __shared__ __align__(8) uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], acc_bar;
@@ -222,8 +224,8 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensor
             for (int kk = 0; kk < TC_BK / 16; ++kk) {
 #pragma unroll
                 for (int p = 0; p < NPAIR; ++p) {
-                    const uint64_t ad = smem_desc(a0 + pa[p] * A_BYTES + kk * 32, 16, 1024);
-                    const uint64_t bd = smem_desc(b0 + pb[p] * B_BYTES + kk * 2048, B_BOX, 1024);
+                    const uint64_t ad = smem_desc(a0 + pa[p] * A_BYTES + kk * 32, 16, A_SBO, A_SWZ);
+                    const uint64_t bd = smem_desc(b0 + pb[p] * B_BYTES + kk * 2048, B_BOX, 1024, 2u);
                     umma_bf16(tmem, ad, bd, kIdesc, (kb | kk | p) != 0);
                 }
             }
@@ -265,61 +267,63 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensor
     }
 }
 
-template <int A_TERMS>
+template <int A_TERMS, int BK, int ST>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
           float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
     const int n_tiles = N / TC_BN;
-    gemm_tile<A_TERMS>(&tmA, &tmB, D, M, N, K, (blockIdx.x / n_tiles) * TC_BM, (blockIdx.x % n_tiles) * TC_BN, err);
+    gemm_tile<A_TERMS, BK, ST>(&tmA, &tmB, D, M, N, K, (blockIdx.x / n_tiles) * TC_BM,
+                               (blockIdx.x % n_tiles) * TC_BN, err);
 }
 
 // Grouped product over many pulses: CTA b computes tiles[b] of pulse tiles[b].pulse,
 // whose A / B tensor maps are maps[2 p] / maps[2 p + 1] (global memory, written
 // by the host before the launch).
-template <int A_TERMS>
+template <int A_TERMS, int BK, int ST>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc_grouped(const CUtensorMap *__restrict__ maps, const BatchPulse *__restrict__ P,
                   const GemmTile *__restrict__ tiles, int *__restrict__ err) {
     const GemmTile t = tiles[blockIdx.x];
     const BatchPulse &q = P[t.pulse];
-    gemm_tile<A_TERMS>(maps + 2 * t.pulse, maps + 2 * t.pulse + 1, q.D, q.M, q.N, q.K, t.m0, t.n0, err);
+    // maps of pulse p: [4p] A (box 64), [4p+1] B (box 64), [4p+2] A (box 32), [4p+3] B (box 32)
+    const CUtensorMap *m = maps + 4 * t.pulse + (BK == 32 ? 2 : 0);
+    gemm_tile<A_TERMS, BK, ST>(m, m + 1, q.D, q.M, q.N, q.K, t.m0, t.n0, err);
 }
 
-static size_t tc_smem_bytes(int a_terms) {
-    return (size_t)TC_STAGES * (a_terms * TC_BM * TC_BK * 2 + 2 * TC_BK * TC_BN * 2) + 1024;
+static size_t tc_smem_bytes(int a_terms, int bk, int stages) {
+    return (size_t)stages * (a_terms * TC_BM * bk * 2 + 2 * bk * TC_BN * 2) + 1024;
 }
+
+// variant: 0 = (BK 64, 2 stages), 1 = (BK 32, 4 stages)
+#define TC_DISPATCH(a_terms, variant, ...)                                                     \
+    if (a_terms == 3 && variant == 0) { constexpr int AT = 3, BK = 64, ST = 2; __VA_ARGS__; } \
+    else if (a_terms == 3) { constexpr int AT = 3, BK = 32, ST = 4; __VA_ARGS__; }            \
+    else if (variant == 0) { constexpr int AT = 2, BK = 64, ST = 2; __VA_ARGS__; }            \
+    else { constexpr int AT = 2, BK = 32, ST = 4; __VA_ARGS__; }
 
 cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
-                                   int a_terms, int *err, cudaStream_t stream) {
-    const size_t smem = tc_smem_bytes(a_terms);
-    cudaError_t e;
-    if (a_terms == 3) {
-        e = cudaFuncSetAttribute(k_gemm_tc_grouped<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+                                   int a_terms, int variant, int *err, cudaStream_t stream) {
+    TC_DISPATCH(a_terms, variant, {
+        const size_t smem = tc_smem_bytes(AT, BK, ST);
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc_grouped<AT, BK, ST>,
+                                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_gemm_tc_grouped<3><<<ntiles, TC_THREADS, smem, stream>>>(maps, P, tiles, err);
-    } else {
-        e = cudaFuncSetAttribute(k_gemm_tc_grouped<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_gemm_tc_grouped<2><<<ntiles, TC_THREADS, smem, stream>>>(maps, P, tiles, err);
-    }
+        k_gemm_tc_grouped<AT, BK, ST><<<ntiles, TC_THREADS, smem, stream>>>(maps, P, tiles, err);
+    })
     return cudaGetLastError();
 }
 
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
-                           int a_terms, int *err, cudaStream_t stream) {
-    if (M % TC_BM || N % TC_BN || K % TC_BK) return cudaErrorInvalidValue;
+                           int a_terms, int variant, int *err, cudaStream_t stream) {
+    if (M % TC_BM || N % TC_BN || K % 64) return cudaErrorInvalidValue;
     const dim3 grid((M / TC_BM) * (N / TC_BN));
-    const size_t smem = tc_smem_bytes(a_terms);
-    cudaError_t e;
-    if (a_terms == 3) {
-        e = cudaFuncSetAttribute(k_gemm_tc<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    TC_DISPATCH(a_terms, variant, {
+        const size_t smem = tc_smem_bytes(AT, BK, ST);
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<AT, BK, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)smem);
         if (e != cudaSuccess) return e;
-        k_gemm_tc<3><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
-    } else {
-        e = cudaFuncSetAttribute(k_gemm_tc<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        k_gemm_tc<2><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
-    }
+        k_gemm_tc<AT, BK, ST><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
+    })
     return cudaGetLastError();
 }
 

@@ -304,6 +304,34 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
             }
             memcpy(&c->tmB, &m, sizeof(m));
         }
+        {
+            cuuint64_t dims[2] = {K2, 3 * K2};
+            cuuint64_t strides[1] = {K2 * 2};
+            cuuint32_t box[2] = {32, 128};
+            CUresult r = cuTensorMapEncodeTiled(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, c->d_A, dims, strides, box,
+                                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_64B,
+                                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) {
+                nlse_set_error(err, NLSE_ERR_CUDA, "cuTensorMapEncodeTiled(A32) failed: %d", (int)r);
+                free_ctx(c);
+                return NLSE_ERR_CUDA;
+            }
+            memcpy(&c->tmA32, &m, sizeof(m));
+        }
+        {
+            cuuint64_t dims[2] = {(cuuint64_t)Nt, 2 * K2};
+            cuuint64_t strides[1] = {(cuuint64_t)Nt * 2};
+            cuuint32_t box[2] = {64, 32};
+            CUresult r = cuTensorMapEncodeTiled(&m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, c->d_Fb, dims, strides, box,
+                                                estr, CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                                                CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+            if (r != CUDA_SUCCESS) {
+                nlse_set_error(err, NLSE_ERR_CUDA, "cuTensorMapEncodeTiled(B32) failed: %d", (int)r);
+                free_ctx(c);
+                return NLSE_ERR_CUDA;
+            }
+            memcpy(&c->tmB32, &m, sizeof(m));
+        }
     }
     ce = cudaMemset(c->d_flag, 0, 4 * sizeof(int));
     if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
@@ -407,6 +435,8 @@ static int half_linear_impl(nlse_ctx *c, float2 *u, double dz, const float *row_
 }
 
 // ---------------------------------------------------------------- split-BF16 path
+static int autotune_gemm(nlse_ctx *c, cudaStream_t st);
+
 static int split_ready(nlse_ctx *c, double dz, cudaStream_t st) {
     if (!c->split_ok)
         return bad(c, NLSE_ERR_UNSUPPORTED,
@@ -414,11 +444,14 @@ static int split_ready(nlse_ctx *c, double dz, cudaStream_t st) {
     int s = ensure_tables(c, dz, st);
     if (s) return s;
     if (dz == c->cached_dz_op) return NLSE_OK;
-    PROF(K_BUILD_OP);
-    s = launched(c, launch_build_operator(c->d_Y64, c->d_rho_modes, c->Nr, dz, c->komega, c->d_Er, c->d_Ei, 3,
-                                          c->d_A, st),
-                 "operator build");
+    {
+        PROF(K_BUILD_OP);
+        s = launched(c, launch_build_operator(c->d_Y64, c->d_rho_modes, c->Nr, dz, c->komega, c->d_Er, c->d_Ei, 3,
+                                              c->d_A, st),
+                     "operator build");
+    }
     if (s == NLSE_OK) c->cached_dz_op = dz;
+    if (s == NLSE_OK) s = autotune_gemm(c, st);
     return s;
 }
 
@@ -439,11 +472,52 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
     return a;
 }
 
-static int tc_gemm(nlse_ctx *c, cudaStream_t st) {
+static cudaError_t tc_gemm_raw(nlse_ctx *c, int variant, cudaStream_t st) {
     const int K2 = 2 * c->Nr;
+    const CUtensorMap *a = variant ? &c->tmA32 : &c->tmA, *b = variant ? &c->tmB32 : &c->tmB;
+    return launch_gemm_tc(a, b, c->d_D, K2, c->Nt, K2, c->a_terms, variant, c->d_flag, st);
+}
+
+static int tc_gemm(nlse_ctx *c, cudaStream_t st) {
     PROF(K_GEMM_TC);
-    return launched(c, launch_gemm_tc(&c->tmA, &c->tmB, c->d_D, K2, c->Nt, K2, c->a_terms, c->d_flag, st),
-                    "tcgen05 gemm");
+    return launched(c, tc_gemm_raw(c, c->gemm_variant, st), "tcgen05 gemm");
+}
+
+// Pipeline autotuner: time each (k depth, stages) variant of the tensor-core
+// product on this context's live operands and keep the faster.  Runs once per
+// context, on its first split-mode call (it synchronises the stream).
+static int autotune_gemm(nlse_ctx *c, cudaStream_t st) {
+    if (c->tuned) return NLSE_OK;
+    cudaEvent_t e0, e1;
+    NLSE_CUDA_TRY(&c->err, cudaEventCreate(&e0));
+    NLSE_CUDA_TRY(&c->err, cudaEventCreate(&e1));
+    float best = 1e30f;
+    int pick = 0;
+    for (int v = 0; v < 2; ++v) {
+        cudaError_t e = tc_gemm_raw(c, v, st);  // warm-up
+        for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) {
+            if (rep == 1) e = cudaEventRecord(e0, st);
+            if (e == cudaSuccess) e = tc_gemm_raw(c, v, st);
+        }
+        if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+        if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+        float ms = 1e30f;
+        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+        if (e != cudaSuccess) {
+            cudaEventDestroy(e0);
+            cudaEventDestroy(e1);
+            return launched(c, e, "gemm autotune");
+        }
+        if (ms < best) {
+            best = ms;
+            pick = v;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    c->gemm_variant = pick;
+    c->tuned = 1;
+    return NLSE_OK;
 }
 
 static int row_entry(nlse_ctx *c, const RowFusedArgs &a, const float2 *u, float *rho, int scan, cudaStream_t st) {
@@ -595,6 +669,16 @@ extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *o
     return launched(c, cudaMemcpyAsync(out, c->d_D, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
 }
 
+extern "C" int nlse_set_gemm_variant(nlse_ctx *c, int variant) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    if (variant < -1 || variant > 1) return bad(c, NLSE_ERR_INVALID_ARG, "variant must be -1 (autotune), 0 or 1");
+    c->gemm_variant = variant < 0 ? 0 : variant;
+    c->tuned = variant >= 0;
+    return NLSE_OK;
+}
+
+extern "C" int nlse_get_gemm_variant(const nlse_ctx *c) { return c ? c->gemm_variant : -1; }
+
 extern "C" int nlse_set_split_terms(nlse_ctx *c, int a_terms) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (a_terms != 2 && a_terms != 3) return bad(c, NLSE_ERR_INVALID_ARG, "a_terms must be 2 or 3");
@@ -685,7 +769,7 @@ struct nlse_batch {
     nlse_ctx **ctx;          // one context per pulse (tables, operator, state buffers)
     BatchPulse *h_pulses;    // pinned staging of the per-pulse table
     BatchPulse *d_pulses;
-    CUtensorMap *d_maps;     // 2 per pulse: A, B
+    CUtensorMap *d_maps;     // 4 per pulse: A, B (k depth 64), A, B (k depth 32)
     GemmTile *d_tiles;
     int ntiles;
     struct Class {
@@ -747,13 +831,15 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
                        i);
     }
     std::vector<GemmTile> tiles;
-    std::vector<CUtensorMap> maps(2 * (size_t)n);
+    std::vector<CUtensorMap> maps(4 * (size_t)n);
     int logs[16], nlog = 0;
     std::vector<std::vector<int2>> work(16);
     for (int i = 0; i < n; ++i) {
         nlse_ctx *c = b->ctx[i];
-        memcpy(&maps[2 * i], &c->tmA, sizeof(CUtensorMap));
-        memcpy(&maps[2 * i + 1], &c->tmB, sizeof(CUtensorMap));
+        memcpy(&maps[4 * i], &c->tmA, sizeof(CUtensorMap));
+        memcpy(&maps[4 * i + 1], &c->tmB, sizeof(CUtensorMap));
+        memcpy(&maps[4 * i + 2], &c->tmA32, sizeof(CUtensorMap));
+        memcpy(&maps[4 * i + 3], &c->tmB32, sizeof(CUtensorMap));
         const int M = 2 * c->Nr;
         for (int m0 = 0; m0 < M; m0 += 128)
             for (int n0 = 0; n0 < c->Nt; n0 += 256) tiles.push_back(GemmTile{i, m0, n0, 0});
@@ -889,12 +975,16 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
              "batch row entry");
     for (int it = 0; it < nsteps; ++it) {
         const int last = it == nsteps - 1;
-        BSEQ(K_GEMM_TC, launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, b->d_flag, st),
+        BSEQ(K_GEMM_TC,
+             launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
+                                    b->d_flag, st),
              "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NL, launch_row_batch(1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 0, st),
                  "batch row nonlinear");
-        BSEQ(K_GEMM_TC, launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, b->d_flag, st),
+        BSEQ(K_GEMM_TC,
+             launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
+                                    b->d_flag, st),
              "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NEXT,

@@ -121,8 +121,12 @@ struct nlse_ctx {
     __nv_bfloat16 *d_Fb;   // 2 x (2Nr x Nt) BF16 hi/lo of the state
     float *d_D;            // 2Nr x Nt tensor-core product
     float2 *d_Ptf;         // Nt  exp(i dk dz/2) mask Rk iRk  (no 1/Nt)
-    CUtensorMap tmA;       // A operand: d_A as [3 * 2Nr][2Nr], box 64 x 128
+    CUtensorMap tmA;       // A operand: d_A as [3 * 2Nr][2Nr], box 64 x 128, 128-byte swizzle
     CUtensorMap tmB;       // B operand: d_Fb as [2 * 2Nr][Nt], box 64 x 64
+    CUtensorMap tmA32;     // A operand, box 32 x 128, 64-byte swizzle
+    CUtensorMap tmB32;     // B operand, box 64 x 32
+    int gemm_variant;      // 0 = BK 64 x 2 stages, 1 = BK 32 x 4 stages (autotuned)
+    int tuned;
     // per-launch event profiling (off unless nlse_profile_start was called)
     int prof_on, prof_cap, prof_n;
     cudaEvent_t *prof_ev;  // 2 * prof_cap events
@@ -158,7 +162,7 @@ cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, float2 
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s,
                              int zero_first, cudaStream_t stream);
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
-                           int a_terms, int *err, cudaStream_t stream);
+                           int a_terms, int variant, int *err, cudaStream_t stream);
 cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
                                   double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, cudaStream_t stream);
 
@@ -170,7 +174,7 @@ cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cuda
 cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
                              cudaStream_t st);
 cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
-                                   int a_terms, int *err, cudaStream_t stream);
+                                   int a_terms, int variant, int *err, cudaStream_t stream);
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
                              int do_scan, cudaStream_t st);
 cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,

@@ -35,10 +35,12 @@ def _operator(c):
     return np.block([[E.real, -E.imag], [E.imag, E.real]])
 
 
+@pytest.mark.parametrize("variant", [0, 1])
 @pytest.mark.parametrize("name", ["small", "c1"])
-def test_operator_product(name, small, c1):
+def test_operator_product(name, variant, small, c1):
     import torch
     c = small if name == "small" else c1
+    c.ctx.set_gemm_variant(variant)
     rng = np.random.default_rng(11)
     w = rng.standard_normal((2 * c.og.Nr, c.og.Nt)) * np.geomspace(1e3, 1e-2, c.og.Nt)[None, :]
     wd = torch.from_numpy(w.astype(np.float32)).cuda()
@@ -51,6 +53,22 @@ def test_operator_product(name, small, c1):
     assert np.all(np.abs(o - ref) <= 2e-5 * scale + 1e-30)
     assert rel_l2(o, ref) < 2e-5
     assert c.ctx.device_status() == 0
+    c.ctx.set_gemm_variant(-1)
+
+
+def test_gemm_variants_agree_bitwise(c1):
+    import torch
+    rng = np.random.default_rng(12)
+    w = torch.from_numpy(rng.standard_normal((2 * c1.og.Nr, c1.og.Nt)).astype(np.float32)).cuda()
+    outs = []
+    for v in (0, 1):
+        c1.ctx.set_gemm_variant(v)
+        o = torch.empty_like(w)
+        c1.ctx.debug_operator_product(w, o, c1.dz)
+        outs.append(o.cpu().numpy())
+    c1.ctx.set_gemm_variant(-1)
+    # same MMAs, same k order within the accumulator: identical results
+    assert np.array_equal(outs[0], outs[1])
 
 
 @pytest.mark.parametrize("name", ["small", "c1"])
