@@ -272,6 +272,94 @@ def run_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
+# ------------------------------------------------------------------ config 4: 64 mixed pulses
+def config4_pulses(n=64, seed=1):
+    """The batch workload: rng = default_rng(seed); per-parameter draws in this
+    order -- N_r in {512, 768, 1024}, N_t in {1024, 2048, 4096} (uniform),
+    energy log-uniform 1-20 uJ, FWHM uniform 50-200 fs, w0 uniform 80-200 um,
+    f uniform 5-20 cm -- then each pulse's noise.  R_max = 10 w0 and a +-4 FWHM
+    window (the ratios of the 256 x 512 CPU case); dz = 5 um."""
+    rng = np.random.default_rng(seed)
+    Nr = rng.choice([512, 768, 1024], n)
+    Nt = rng.choice([1024, 2048, 4096], n)
+    E = np.exp(rng.uniform(np.log(1.0), np.log(20.0), n))
+    fwhm = rng.uniform(50e-15, 200e-15, n)
+    w0 = rng.uniform(80e-6, 200e-6, n)
+    f = rng.uniform(0.05, 0.20, n)
+    return [dict(Nr=int(Nr[i]), Nt=int(Nt[i]), E=float(E[i]), fwhm=float(fwhm[i]), w0=float(w0[i]), f=float(f[i]),
+                 R_max=10 * float(w0[i]), T_half=4 * float(fwhm[i]), dz=5e-6, noise_seed=int(rng.integers(1 << 31)))
+            for i in range(n)]
+
+
+def run_config4(args, rank, world, local_rank):
+    import torch
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    from rapport_gb300.replicas import pulse_cost, shard_pulses
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=dev)
+    pulses = config4_pulses()
+    mine = shard_pulses([pulse_cost(p["Nr"], p["Nt"]) for p in pulses], world, rank)
+    cfgs, grids, us, rhos = [], [], [], []
+    for i in mine:
+        p = pulses[i]
+        cfg = R.workload_config(p["Nr"], p["Nt"], p["R_max"], p["w0"], p["T_half"], p["dz"], 2000)
+        g = R.build_grids(cfg)
+        u0 = R.envelope_lens(p["w0"], p["fwhm"], p["E"], p["f"], p["noise_seed"])(g["rr"], g["tt"], cfg, g)
+        cfgs.append(cfg)
+        grids.append(g)
+        us.append(torch.from_numpy(np.ascontiguousarray(u0.astype(np.complex64))).to(dev))
+        rhos.append(torch.zeros(u0.shape, dtype=torch.float32, device=dev))
+    bt = _lib.Batch(cfgs, grids)
+    Z = args.zsteps
+    for _ in range(args.warmup):
+        bt.propagate(us, rhos, None, 5e-6, Z)
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+    torch.cuda.synchronize()
+    for i in range(args.steps):
+        flush.fill_(float(i))
+        ev[i][0].record()
+        bt.propagate(us, rhos, None, 5e-6, Z)
+        ev[i][1].record()
+    torch.cuda.synchronize()
+    t_ms = sum(a.elapsed_time(b) for a, b in ev)
+    if world > 1:
+        import torch.distributed as dist
+        tt = torch.tensor([t_ms], device=dev)
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t_ms = float(tt.item())
+    prof_ctx = bt.context_profile()
+    prof_ctx.profile_start(args.steps * Z * 64 + 64)
+    for i in range(args.steps):
+        bt.propagate(us, rhos, None, 5e-6, Z)
+    prof = prof_ctx.profile_read()
+    ok = bt.device_status() == 0 and all(bool(torch.isfinite(u).all().item()) for u in us)
+    flops = sum(8.0 * pulses[i]["Nr"] ** 2 * pulses[i]["Nt"] for i in range(len(pulses)))
+    line = {
+        "metric": "pulse-z-steps/s (1 GB300), split-BF16 batched, 64 mixed pulses", "value":
+            len(pulses) * args.steps * Z / (t_ms * 1e-3), "unit": "pulse-z-steps/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "dtype": "bf16x3-split + f32", "data": "synthetic (config-4 draws, default_rng(1))",
+        "config": {"workload": "64 pulses, N_r in {512,768,1024} x N_t in {1024,2048,4096}, 1-20 uJ, 50-200 fs, "
+                               "w0 80-200 um, f 5-20 cm, dz 5 um", "z_steps_per_step": Z,
+                   "grids": sorted({(p["Nr"], p["Nt"]) for p in pulses}), "parallelism": f"replicas{world}"},
+        "tensor_tflops_algorithmic": 2 * flops * args.steps * Z / (sum(v[1] for k, v in prof.items()
+                                                                     if k == "k_gemm_tc") * 1e-3) / 1e12,
+        "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "finite": ok,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 # ------------------------------------------------------------------ CPU (oracle) arm
 def _oracle_setup():
     sys.path.insert(0, os.path.join(HERE, "oracle"))
@@ -336,12 +424,16 @@ def main():
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=8, help="pulses in the batched measurement (0 = skip)")
+    ap.add_argument("--workload", default="single", choices=["single", "config4"])
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
     if args.impl == "reference":
         run_reference(args, rank)
+        return
+    if args.workload == "config4":
+        run_config4(args, rank, world, local_rank)
         return
     run_ours(args, rank, world, local_rank)
 

@@ -185,6 +185,16 @@ int nlse_set_split_terms(nlse_ctx *ctx, int a_terms);
  * gave up a bounded wait since nlse_create (word receives the raw bits). */
 int nlse_device_status(nlse_ctx *ctx, int *word);
 
+/* Per-radius diagnostics of one saved plane (Integrator._record,
+ * integrator.py:179-224), FP64 reductions over t into out[r][6 + nbins]:
+ * sum |u|^2, max rho, max rho_s, max |u|^2, sum 2 photo |u|^2,
+ * sum 2 plasma |u|^2, then per time bin sum 2 (photo + plasma) |u|^2 with
+ * bin_of_t[t] in [0, nbins) or -1 (device int array; nbins <= 8).  photo and
+ * plasma are NonlinearOperator.loss_rates (operators.py:148-163).  out and
+ * bin_of_t are device pointers; rho_s may be NULL. */
+int nlse_record(nlse_ctx *ctx, const void *u, const float *rho, const float *rho_s,
+                const int *bin_of_t, int nbins, double *out, void *stream);
+
 /* Number of (row, call) pairs the carrier scan has re-marched sequentially
  * since nlse_create (saturated or non-converging rows); synchronous read. */
 int nlse_scan_fallback_rows(nlse_ctx *ctx, int *out);

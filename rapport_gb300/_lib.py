@@ -21,7 +21,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
-           "nlse_half_linear_noalloc", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
+           "nlse_half_linear_noalloc", "nlse_record", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
            "nlse_batch_set_split_terms", "nlse_batch_device_status", "nlse_batch_get_last_error",
            "nlse_batch_destroy",
            "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
@@ -79,6 +79,7 @@ def load():
     lib.nlse_kernel_name.argtypes = [_I]
     lib.nlse_kernel_name.restype = ctypes.c_char_p
     lib.nlse_set_gemm_variant.argtypes = [_P, _I]
+    lib.nlse_record.argtypes = [_P, _P, _P, _P, _P, _I, _P, _P]
     lib.nlse_get_gemm_variant.argtypes = [_P]
     lib.nlse_batch_create.argtypes = [ctypes.POINTER(GridDesc), _I, ctypes.POINTER(_P)]
     lib.nlse_batch_propagate.argtypes = [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), _D, _I, _P]
@@ -236,6 +237,16 @@ class Context:
         _check(self.lib, self.h, self.lib.nlse_debug_operator_product(
             self.h, ctypes.c_void_p(w.data_ptr()), ctypes.c_void_p(out.data_ptr()), float(dz), self._stream()))
 
+    def record(self, u, rho, rho_s, bin_of_t, nbins, out):
+        """Per-radius plane diagnostics into out (float64 CUDA tensor, Nr x (6 + nbins))."""
+        import torch
+        if out.dtype != torch.float64 or tuple(out.shape) != (self.Nr, 6 + nbins) or not out.is_contiguous():
+            raise ValueError("out must be a contiguous float64 CUDA tensor of shape (Nr, 6 + nbins)")
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
+        b = ctypes.c_void_p(bin_of_t.data_ptr()) if bin_of_t is not None else None
+        _check(self.lib, self.h, self.lib.nlse_record(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs, b,
+                                                      int(nbins), ctypes.c_void_p(out.data_ptr()), self._stream()))
+
     def set_split_terms(self, n):
         _check(self.lib, self.h, self.lib.nlse_set_split_terms(self.h, int(n)))
 
@@ -352,6 +363,16 @@ class Batch:
             buf = ctypes.create_string_buffer(512)
             self.lib.nlse_batch_get_last_error(self.h, buf, 512)
             raise NLSEError(status, buf.value.decode(errors="replace"))
+
+    def record(self, u, rho, rho_s, bin_of_t, nbins, out):
+        """Per-radius plane diagnostics into out (float64 CUDA tensor, Nr x (6 + nbins))."""
+        import torch
+        if out.dtype != torch.float64 or tuple(out.shape) != (self.Nr, 6 + nbins) or not out.is_contiguous():
+            raise ValueError("out must be a contiguous float64 CUDA tensor of shape (Nr, 6 + nbins)")
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
+        b = ctypes.c_void_p(bin_of_t.data_ptr()) if bin_of_t is not None else None
+        _check(self.lib, self.h, self.lib.nlse_record(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs, b,
+                                                      int(nbins), ctypes.c_void_p(out.data_ptr()), self._stream()))
 
     def set_split_terms(self, n):
         _check(self.lib, None, self.lib.nlse_batch_set_split_terms(self.h, int(n)))

@@ -669,6 +669,16 @@ extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *o
     return launched(c, cudaMemcpyAsync(out, c->d_D, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
 }
 
+extern "C" int nlse_record(nlse_ctx *c, const void *u, const float *rho, const float *rho_s, const int *bin_of_t,
+                           int nbins, double *out, void *stream) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !field_ok(c, out, "out")) return NLSE_ERR_INVALID_ARG;
+    if (nbins < 0 || nbins > 8 || (nbins && !bin_of_t)) return bad(c, NLSE_ERR_INVALID_ARG, "nbins must be 0..8");
+    cudaStream_t st = (cudaStream_t)stream;
+    PROF(K_RECORD);
+    return launched(c, launch_record(c, (const float2 *)u, rho, rho_s, bin_of_t, nbins, out, st), "record");
+}
+
 extern "C" int nlse_set_gemm_variant(nlse_ctx *c, int variant) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (variant < -1 || variant > 1) return bad(c, NLSE_ERR_INVALID_ARG, "variant must be -1 (autotune), 0 or 1");
@@ -758,6 +768,7 @@ extern "C" const char *nlse_kernel_name(int kid) {
         case K_ROW_NL: return "k_row_nl";
         case K_ROW_NEXT: return "k_row_next";
         case K_BUILD_OP: return "k_build_operator";
+        case K_RECORD: return "k_record";
         default: return "";
     }
 }

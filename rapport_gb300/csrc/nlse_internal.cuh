@@ -146,6 +146,7 @@ enum {
     K_ROW_NL = 8,
     K_ROW_NEXT = 9,
     K_BUILD_OP = 10,
+    K_RECORD = 11,
     K_NUM_KINDS = 16
 };
 
@@ -169,6 +170,8 @@ cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, 
 cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, const float2 *tw, const float2 *Pt,
                                          const float2 *Pr, cudaStream_t stream);
 void nlse_set_thread_error(int status, const char *msg);
+cudaError_t launch_record(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, const int *bin_of_t,
+                          int nbins, double *out, cudaStream_t st);
 cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st);
 // kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call)
 cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,

@@ -173,6 +173,26 @@ def k1_edge_cases():
     return res
 
 
+def record_case():
+    """The reference's own Integrator.propagate() with every recording option on:
+    save stride, (z, r, t) cube with r/t strides, absorption time bins, rho snapshot."""
+    Nr, Nt, dz, nz = 64, 256, 5e-6, 8
+    cfg = make_config(Nr, Nt, 100e-6, 10e-6, 300e-15, dz, nz, energy_uJ=2.0)
+    cfg.save_stride, cfg.rho_t_stride, cfg.rho_r_stride = 2, 4, 2
+    cfg.absorb_time_bins_fs = (-100.0, -50.0, 0.0, 50.0, 100.0)
+    cfg.rho_snapshot_t_fs = 50.0
+    integ = ref_integrator.Integrator(cfg, envelope=lens_envelope(100e-15, 2.0, 10e-6, 1e-2, 0))
+    res = integ.propagate()
+    keep = ("r", "rlist", "z", "fluence_rz", "rho_rz", "rho_s_rz", "Imax_z", "E_plasma_z", "E_MPI_z", "E_STE_z",
+            "E_total_z", "rho_rzt", "rho_s_rzt", "I_rzt", "t_sub_fs", "r_sub", "absorbed_rz", "Ipeak_rz",
+            "rho_rz_at", "absorbed_rz_bins", "absorb_bin_edges_fs", "rho_onaxis_t", "rho_s_onaxis_t",
+            "I_onaxis_t", "t_full_fs")
+    out = {k: res[k] for k in keep}
+    out["U0_uJ"] = integ.U0_uJ
+    out["meta"] = np.array([Nr, Nt, 100e-6, 10e-6, 300e-15, 100e-15, 2.0, 1e-2, dz, nz, 0], dtype=np.float64)
+    return out
+
+
 def main():
     # 2 uJ into a 10 um waist: Kerr phase ~0.2 rad and peak rho ~1e19 per step,
     # every term active, RK4 comfortably stable (used for propagation parity)
@@ -196,6 +216,7 @@ def main():
                   rows=list(range(0, 256, 8)), keep_steps=[1, 3], with_Y=False)
     np.savez_compressed(os.path.join(HERE, "config1_prefix.npz"), **c1)
     np.savez_compressed(os.path.join(HERE, "k1_edge.npz"), **k1_edge_cases())
+    np.savez_compressed(os.path.join(HERE, "record_tiny.npz"), **record_case())
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))
 
 
