@@ -64,21 +64,28 @@ __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs
 template <int NT>
 __device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float inv, int r, const RowFusedArgs &a,
                                           float *rho) {
-    float *sI = reinterpret_cast<float *>(O), *sW = sI + NT;
+    constexpr int S = scan_span(NT, NLSE_ROW_THREADS);
+    constexpr int C = (NT - 1 + NLSE_ROW_THREADS - 1) / NLSE_ROW_THREADS;
+    float *sI = reinterpret_cast<float *>(O), *sW = sI + S;
     for (int t = threadIdx.x; t < NT; t += blockDim.x) {
         const float2 v = c_scale(R[pidx(t)], inv);
-        sI[t] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
+        sI[scan_slot(t, C)] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
     }
     __syncthreads();
-    float *sx = reinterpret_cast<float *>(R), *sJ = sx + NT;
+    float *sx = reinterpret_cast<float *>(R), *sJ = sx + S;
     scan_row(sI, sW, sx, sJ, X, NT, a.sc, a.lut, 0.0f, a.stats);
     float *gr = rho + (size_t)r * NT;
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[t];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[scan_slot(t, C)];
 }
 
+// 2 padded complex row buffers (+ one float scan array, scan_span(NT) long, for the march).
+// The march aliases two float arrays into each complex buffer: 2 * span floats
+// must fit in fft_slots(NT) float2, which holds for every NT >= 16 with 256 threads.
 template <int NT>
 __host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
-    return 2 * (size_t)fft_slots(NT) * sizeof(float2) + (with_march ? (size_t)NT * sizeof(float) : 0);
+    constexpr int span = scan_span(NT, NLSE_ROW_THREADS);
+    static_assert(2 * span <= 2 * fft_slots(NT), "scan arrays must fit in the FFT buffers");
+    return 2 * (size_t)fft_slots(NT) * sizeof(float2) + (with_march ? (size_t)span * sizeof(float) : 0);
 }
 
 // Entry: physical u (interleaved) -> w = F[u] (state); optionally rho = march(|u|^2).
@@ -161,7 +168,7 @@ k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F3
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
          const float *__restrict__ rho) {
     row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho);
@@ -185,7 +192,7 @@ k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, i
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
 k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
@@ -202,7 +209,9 @@ k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, in
 
 template <typename K>
 static cudaError_t set_smem(K *fn, size_t bytes) {
-    return cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    cudaError_t e = cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+    if (e == cudaSuccess) e = cudaFuncSetAttribute(fn, cudaFuncAttributePreferredSharedMemoryCarveout, 100);
+    return e;
 }
 
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,

@@ -29,6 +29,7 @@ __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__restrict__ rho_s, int Nt,
             ScanParams p, const float *__restrict__ lut, int zero_first, int *__restrict__ stats) {
     extern __shared__ float sm[];
+    const int S = scan_span(Nt, blockDim.x), C = (Nt - 1 + blockDim.x - 1) / blockDim.x;
     float *sI = sm;
     const size_t row = blockIdx.x;
     const float2 *g = u + row * (size_t)Nt;
@@ -40,20 +41,20 @@ k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__rest
     }
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
         float2 v = g[t];
-        sI[t] = fmaf(v.x, v.x, v.y * v.y) * p.invE2;
+        sI[scan_slot(t, C)] = fmaf(v.x, v.x, v.y * v.y) * p.invE2;
     }
     __syncthreads();
-    float *sx = sm + 2 * Nt;
-    scan_row(sI, sm + Nt, sx, sm + 3 * Nt, sm + 4 * Nt, Nt, p, lut, x0, stats);
+    float *sx = sm + 2 * S;
+    scan_row(sI, sm + S, sx, sm + 3 * S, sm + 4 * S, Nt, p, lut, x0, stats);
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
-        if (t > 0 || zero_first) grho[t] = t == 0 ? 0.0f : sx[t];
+        if (t > 0 || zero_first) grho[t] = t == 0 ? 0.0f : sx[scan_slot(t, C)];
         if (rho_s && (t > 0 || zero_first)) rho_s[row * (size_t)Nt + t] = 0.0f;
     }
 }
 
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s, int zero_first,
                              cudaStream_t stream) {
-    size_t smem = 5 * (size_t)c->Nt * sizeof(float);
+    size_t smem = 5 * (size_t)scan_span(c->Nt, NLSE_ROW_THREADS) * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(k_rate_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
     k_rate_scan<<<c->Nr, NLSE_ROW_THREADS, smem, stream>>>(u, rho, rho_s, c->Nt, c->sc, c->d_lut_dt,

@@ -148,41 +148,61 @@ static __device__ void block_reduce(float &m1, float &m2, int &f, float *red) {
 // holds the intensities (synced); sW, sx, sJ, sB are scratch of Nt floats
 // each (may alias any other buffer the caller no longer needs).  On return
 // (synced) sx[t] holds the densities, sx[0] = x0.
+// Shared-memory slot of step n when thread t owns the contiguous chunk
+// [t C, (t + 1) C): slot j T + t for n = t C + j -- the threads of a warp then
+// touch consecutive words at every j (a plain layout would be C-way conflicted).
+__device__ __forceinline__ int scan_slot(int n, int C) { return (n % C) * (int)blockDim.x + n / C; }
+
+// Number of floats each scan array needs for Nt points with `threads` threads:
+// one past the largest slot, reached at remainder C - 1 (= Nt for powers of two).
+__host__ __device__ __forceinline__ constexpr int scan_span(int Nt, int threads) {
+    return ((Nt - 1 + threads - 1) / threads - 1) * threads +
+           (Nt - (Nt - 1 + threads - 1) / threads) / ((Nt - 1 + threads - 1) / threads) + 1;
+}
+
+// Solve one row's carrier march (all threads of the CTA).  On entry sI holds
+// the intensities at slots scan_slot(t, C) (synced); sW, sx, sJ, sB are
+// scratch of scan_span(Nt) floats each (may alias any other buffer the caller
+// no longer needs).  On return (synced) sx[scan_slot(t, C)] holds the density
+// at t, sx[slot 0] = x0.  C = chunk of steps per thread = ceil((Nt-1)/blockDim).
 static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ, float *sB, int Nt,
-                         const ScanParams &p, const float *__restrict__ lut, float x0, int *stats) {
+                                const ScanParams &p, const float *__restrict__ lut, float x0, int *stats) {
     __shared__ Aff wsum[32];
     __shared__ float red[100];
+    const int T = Nt - 1;
+    const int C = (T + blockDim.x - 1) / blockDim.x;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
-        sW[t] = lut_rate_dt(sI[t], lut, p);
-        sx[t] = t == 0 ? x0 : 0.0f;
+        const int q = scan_slot(t, C);
+        sW[q] = lut_rate_dt(sI[q], lut, p);
+        sx[q] = t == 0 ? x0 : 0.0f;
     }
     __syncthreads();
-    const int T = Nt - 1;
-    const int chunk = (T + blockDim.x - 1) / blockDim.x;
-    const int n0 = min((int)threadIdx.x * chunk, T), n1 = min(n0 + chunk, T);
+    const int n0 = min((int)threadIdx.x * C, T), n1 = min(n0 + C, T);
     int converged = 0, clamp_any = 0;
     for (int it = 0; it < SCAN_MAX_IT; ++it) {
         Aff acc{1.0f, 0.0f};
         bool cl = false;
         for (int n = n0; n < n1; ++n) {
-            float Ia = 0.5f * (sI[n] + sI[n + 1]);
-            float b = 0.5f * (sW[n] + sW[n + 1]);
-            float xn = sx[n];
+            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+            float Ia = 0.5f * (sI[q0] + sI[q1]);
+            float b = 0.5f * (sW[q0] + sW[q1]);
+            float xn = sx[q0];
             float J = 0.0f, F = 0.0f;
             if (isfinite(Ia)) F = step_map(xn, p.a_coef * Ia, b, p, &J, &cl);
             float Bv = fmaf(-J, xn, F);
-            sJ[n] = J;
-            sB[n] = Bv;
+            sJ[q0] = J;
+            sB[q0] = Bv;
             acc = aff_then(acc, Aff{J, Bv});
         }
         Aff pre = block_exclusive_scan(acc, wsum);
         float xs = fmaf(pre.A, x0, pre.B);
         float dmax = 0.0f, xmax = 0.0f;
         for (int n = n0; n < n1; ++n) {
-            xs = fmaf(sJ[n], xs, sB[n]);
-            dmax = fmaxf(dmax, fabsf(xs - sx[n + 1]));
+            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+            xs = fmaf(sJ[q0], xs, sB[q0]);
+            dmax = fmaxf(dmax, fabsf(xs - sx[q1]));
             xmax = fmaxf(xmax, fabsf(xs));
-            sx[n + 1] = xs;
+            sx[q1] = xs;
         }
         int f = cl ? 1 : 0;
         block_reduce(dmax, xmax, f, red);
@@ -202,11 +222,12 @@ static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ
             float x = x0;
             bool cl = false;
             for (int n = 0; n < T; ++n) {
-                float Ia = 0.5f * (sI[n] + sI[n + 1]);
-                float b = 0.5f * (sW[n] + sW[n + 1]);
+                const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+                float Ia = 0.5f * (sI[q0] + sI[q1]);
+                float b = 0.5f * (sW[q0] + sW[q1]);
                 float J;
                 x = isfinite(Ia) ? step_map(x, p.a_coef * Ia, b, p, &J, &cl) : 0.0f;
-                sx[n + 1] = x;
+                sx[q1] = x;
             }
             if (stats) atomicAdd(&stats[1], 1);
         }
