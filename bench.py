@@ -170,98 +170,147 @@ def run_ours(args, rank, world, local_rank):
     r = results[head]
     mode = modes[head]
 
-    # ---------------------------------------------------------- e2e: host buffers through the C ABI
-    uh = torch.from_numpy(u0).pin_memory()
-    uo = torch.empty_like(uh).pin_memory()
-    rho_h = torch.empty(u0.shape, dtype=torch.float32).pin_memory()
-    ud = torch.empty(u0.shape, dtype=torch.complex64, device=dev)
-    rd = torch.zeros(u0.shape, dtype=torch.float32, device=dev)
-    sd = torch.zeros_like(rd)
-    e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(r["K"])]
-    for i in range(r["K"] + 1):
-        flush.fill_(float(i))
-        if i > 0:
-            e_ev[i - 1][0].record()
-        ud.copy_(uh, non_blocking=True)
-        ctx.propagate(ud, rd, sd, w["dz"], Z, mode)
-        uo.copy_(ud, non_blocking=True)
-        rho_h.copy_(rd, non_blocking=True)
-        if i > 0:
-            e_ev[i - 1][1].record()
-    torch.cuda.synchronize()
-    e_ms = sum(a.elapsed_time(b) for a, b in e_ev)
-    assert np.isfinite(uo.numpy()).all()
-    e2e = {"value": world * r["K"] * Z / (e_ms * 1e-3), "unit": "z-steps/s",
-           "h2d_bytes_per_step": int(uh.numel() * 8), "d2h_bytes_per_step": int(uo.numel() * 8 + rho_h.numel() * 4)}
-
-    # ---------------------------------------------------------- batched form: B pulses of the same grid
-    batched = None
-    if args.batch > 0 and head == "split_bf16":
-        B = args.batch
-        env = [R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"] + i)(g["rr"], g["tt"], cfg, g)
-               for i in range(B)]
+    # ---------------------------------------------------------- headline: the batched split-BF16 form
+    # B pulses of the same 1024 x 2048 grid (seeds 0..B-1) advanced together:
+    # one grouped tensor-core launch per half step over all their tiles.
+    hbm, bf16, bf16_s, src = peaks()
+    Nr, Nt = w["Nr"], w["Nt"]
+    B = args.batch if head == "split_bf16" else 0
+    if B > 0:
+        envs = [np.ascontiguousarray(R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"] + i)(
+            g["rr"], g["tt"], cfg, g).astype(np.complex64)) for i in range(B)]
         bt = _lib.Batch([cfg] * B, [g] * B)
-        bu = [torch.from_numpy(np.ascontiguousarray(e.astype(np.complex64))).to(dev) for e in env]
+        bu = [torch.from_numpy(e).to(dev) for e in envs]
         br = [torch.zeros(u0.shape, dtype=torch.float32, device=dev) for _ in range(B)]
+        bt.propagate(bu, br, None, w["dz"], 1)
         for _ in range(args.warmup):
             bt.propagate(bu, br, None, w["dz"], Z)
         torch.cuda.synchronize()
-        KB = max(2, args.steps // 2)
-        bev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(KB)]
-        for i in range(KB):
+        K = args.steps
+        bev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        clk = ClockSampler(local_rank)
+        barrier()
+        torch.cuda.synchronize()
+        for i in range(K):
             flush.fill_(float(i))
             bev[i][0].record()
             bt.propagate(bu, br, None, w["dz"], Z)
             bev[i][1].record()
         torch.cuda.synchronize()
-        bms = sum(a.elapsed_time(b_) for a, b_ in bev)
+        barrier()
+        clocks = clk.stop()
+        t_ms = sum(a.elapsed_time(b_) for a, b_ in bev)
+        if world > 1:
+            import torch.distributed as dist
+            tt = torch.tensor([t_ms], device=dev)
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+            t_ms = float(tt.item())
+        value = world * B * K * Z / (t_ms * 1e-3)
+        pctx = bt.context_profile()
+        pctx.profile_start(K * Z * 16 + 64)
+        for i in range(K):
+            flush.fill_(float(i))
+            bt.propagate(bu, br, None, w["dz"], Z)
+        prof = pctx.profile_read()
         assert bt.device_status() == 0 and all(bool(torch.isfinite(x).all().item()) for x in bu)
-        bval = world * B * KB * Z / (bms * 1e-3)
-        batched = {"pulses": B, "grid": "1024x2048 each (seeds 0..B-1)", "value": bval,
-                   "unit": "pulse-z-steps/s", "ms_per_step": bms / KB, "steps": KB,
-                   "vs_single_pulse": bval / r["zsteps_per_s"],
-                   "vs_plain_fp32": (bval / results["plain"]["zsteps_per_s"]) if "zsteps_per_s" in results.get("plain", {}) else None}
+        # e2e through the C ABI with host buffers: every step copies each pulse's
+        # field in from pinned memory and its field + densities back out
+        uh = [torch.from_numpy(e).pin_memory() for e in envs]
+        uo = [torch.empty_like(x).pin_memory() for x in uh]
+        rh = [torch.empty(u0.shape, dtype=torch.float32).pin_memory() for _ in range(B)]
+        eev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        for i in range(K + 1):
+            flush.fill_(float(i))
+            if i > 0:
+                eev[i - 1][0].record()
+            for j in range(B):
+                bu[j].copy_(uh[j], non_blocking=True)
+            bt.propagate(bu, br, None, w["dz"], Z)
+            for j in range(B):
+                uo[j].copy_(bu[j], non_blocking=True)
+                rh[j].copy_(br[j], non_blocking=True)
+            if i > 0:
+                eev[i - 1][1].record()
+        torch.cuda.synchronize()
+        e_ms = sum(a.elapsed_time(b_) for a, b_ in eev)
+        assert all(np.isfinite(x.numpy()).all() for x in uo)
+        e2e = {"value": world * B * K * Z / (e_ms * 1e-3), "unit": "z-steps/s",
+               "h2d_bytes_per_step": int(sum(x.numel() * 8 for x in uh)),
+               "d2h_bytes_per_step": int(sum(x.numel() * 8 for x in uo) + sum(x.numel() * 4 for x in rh))}
         del bt, bu, br
+        gemm_flops = B * 8.0 * Nr * Nr * Nt          # one grouped launch, algorithmic
+        form = f"split_bf16 batched ({B} pulses of {Nr}x{Nt})"
+        ms_per_step = t_ms / K
+    else:
+        # single-pulse form only (split-BF16 unavailable): e2e through the single-context call
+        value, prof, clocks, K = r["zsteps_per_s"], r["prof"], r["clocks"], r["K"]
+        uh = torch.from_numpy(u0).pin_memory()
+        uo = torch.empty_like(uh).pin_memory()
+        rho_h = torch.empty(u0.shape, dtype=torch.float32).pin_memory()
+        ud = torch.empty(u0.shape, dtype=torch.complex64, device=dev)
+        rd = torch.zeros(u0.shape, dtype=torch.float32, device=dev)
+        sd = torch.zeros_like(rd)
+        e_ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        for i in range(K + 1):
+            flush.fill_(float(i))
+            if i > 0:
+                e_ev[i - 1][0].record()
+            ud.copy_(uh, non_blocking=True)
+            ctx.propagate(ud, rd, sd, w["dz"], Z, mode)
+            uo.copy_(ud, non_blocking=True)
+            rho_h.copy_(rd, non_blocking=True)
+            if i > 0:
+                e_ev[i - 1][1].record()
+        torch.cuda.synchronize()
+        e_ms = sum(a.elapsed_time(b) for a, b in e_ev)
+        e2e = {"value": world * K * Z / (e_ms * 1e-3), "unit": "z-steps/s",
+               "h2d_bytes_per_step": int(uh.numel() * 8),
+               "d2h_bytes_per_step": int(uo.numel() * 8 + rho_h.numel() * 4)}
+        gemm_flops = (8.0 if head == "split_bf16" else 4.0) * Nr * Nr * Nt
+        form = head
+        ms_per_step = r["t_ms"] / r["K"]
 
     # ---------------------------------------------------------- roofline of the dominant kernel
-    hbm, bf16, bf16_s, src = peaks()
-    prof = r["prof"]
     top = max(prof, key=lambda k: prof[k][1])
     n_launch, tot = prof[top]
     avg_s = tot / n_launch * 1e-3
-    Nr, Nt = w["Nr"], w["Nt"]
     traffic = None
     tpath = os.path.join(HERE, "profiles", "traffic_per_launch.json")
     if os.path.exists(tpath):
         with open(tpath) as f:
-            traffic = json.load(f).get(top)
+            tr = json.load(f)
+        traffic = tr.get(top + ("_batched" if B > 0 else ""), tr.get(top) if B == 0 else None)
     if top in ("k_gemm_tc", "k_gemm_f32"):
-        flops = (8.0 if top == "k_gemm_tc" else 4.0) * Nr * Nr * Nt   # per launch (algorithmic)
-        ach = flops / avg_s / 1e12
+        ach = gemm_flops / avg_s / 1e12
         roof = {"kernel": top, "bound": "tensor", "achieved": ach, "peak": bf16_s, "unit": "TFLOP/s",
                 "frac": ach / bf16_s, "traffic": traffic, "peak_source": f"bf16_tflops_sustained ({src})",
-                "per_launch": f"{flops:.3e} algorithmic FLOPs, avg {avg_s * 1e6:.1f} us over {n_launch} launches"}
+                "per_launch": f"{gemm_flops:.3e} algorithmic FLOPs, avg {avg_s * 1e6:.1f} us over {n_launch} launches",
+                "executed_bf16_tflops": 4 * ach if top == "k_gemm_tc" else None}
     else:
-        byts = {"k_rate_scan": 12.0, "k_row_scan": 20.0, "k_row_nl": 36.0, "k_nonlinear_step": 20.0,
-                "k_fft_phase_ifft": 16.0}.get(top, 16.0) * Nr * Nt
+        npts = (B if B > 0 else 1) * Nr * Nt
+        byts = {"k_row_nl": 36.0, "k_row_next": 36.0, "k_rate_scan": 12.0, "k_nonlinear_step": 20.0,
+                "k_fft_phase_ifft": 16.0}.get(top, 16.0) * npts
         ach = byts / avg_s / 1e9
         roof = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
                 "traffic": traffic, "peak_source": f"hbm_gbs ({src})",
                 "per_launch": f"{byts:.3e} algorithmic bytes, avg {avg_s * 1e6:.1f} us over {n_launch} launches"}
 
     line = {
-        "metric": METRIC, "value": r["zsteps_per_s"], "unit": "z-steps/s", "n_gpus": world, "steps": r["K"],
-        "warmup": args.warmup, "ms_per_step": r["t_ms"] / r["K"], "higher_is_better": True, "scaling": "weak",
+        "metric": METRIC, "value": value, "unit": "z-steps/s", "n_gpus": world, "steps": K,
+        "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "bf16x3-split + f32" if head == "split_bf16" else "f32",
-        "data": "synthetic (seeded lens-focused Gaussian pulse with 1% noise)",
-        "config": dict(CONFIG, form=head, z_steps_per_step=Z, parallelism=f"replicas{world}",
-                       l2="256 MB flush before each timed step (outside its events); inputs (24 MB) < L2",
+        "data": "synthetic (seeded lens-focused Gaussian pulses with 1% noise)",
+        "config": dict(CONFIG, form=form, pulses=max(B, 1), z_steps_per_step=Z, parallelism=f"replicas{world}",
+                       l2="256 MB flush before each timed step (outside its events); per pulse 24 MB",
                        kernel_times="second identical pass of K steps with per-launch events"),
         "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
-        "clocks": r["clocks"],
-        "forms": {k: (round(v["zsteps_per_s"], 1) if "zsteps_per_s" in v else v) for k, v in results.items()},
-        "batched": batched,
+        "clocks": clocks,
+        "forms": dict({k + "_single_pulse": (round(v["zsteps_per_s"], 1) if "zsteps_per_s" in v else v)
+                       for k, v in results.items()},
+                      **({"split_bf16_batched": round(value, 1)} if B > 0 else {})),
+        "speedup_vs_plain_fp32": (value / results["plain"]["zsteps_per_s"])
+        if "zsteps_per_s" in results.get("plain", {}) else None,
     }
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(args.cpu_zsteps)
@@ -423,7 +472,7 @@ def main():
     ap.add_argument("--zsteps", type=int, default=50, help="z-steps per bench step")
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--batch", type=int, default=8, help="pulses in the batched measurement (0 = skip)")
+    ap.add_argument("--batch", type=int, default=8, help="pulses of the batched (headline) form; 0 = single pulse")
     ap.add_argument("--workload", default="single", choices=["single", "config4"])
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))

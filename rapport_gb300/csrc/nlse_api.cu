@@ -847,9 +847,18 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
     std::vector<std::vector<int2>> work(16);
     for (int i = 0; i < n; ++i) {
         nlse_ctx *c = b->ctx[i];
-        memcpy(&maps[4 * i], &c->tmA, sizeof(CUtensorMap));
+        // pulses built from the same QDHT tables and k0 have the same operator
+        // (dz is common to the batch): they read the first such pulse's copy,
+        // so the grouped product streams one operator from L2 instead of many
+        int owner = i;
+        for (int j = 0; j < i && owner == i; ++j)
+            if (descs[j].Y == descs[i].Y && descs[j].rho_modes == descs[i].rho_modes && descs[j].Nr == descs[i].Nr &&
+                descs[j].komega == descs[i].komega)
+                owner = j;
+        nlse_ctx *oc = b->ctx[owner];
+        memcpy(&maps[4 * i], &oc->tmA, sizeof(CUtensorMap));
         memcpy(&maps[4 * i + 1], &c->tmB, sizeof(CUtensorMap));
-        memcpy(&maps[4 * i + 2], &c->tmA32, sizeof(CUtensorMap));
+        memcpy(&maps[4 * i + 2], &oc->tmA32, sizeof(CUtensorMap));
         memcpy(&maps[4 * i + 3], &c->tmB32, sizeof(CUtensorMap));
         const int M = 2 * c->Nr;
         for (int m0 = 0; m0 < M; m0 += 128)

@@ -76,3 +76,22 @@ def test_batch_rejects_untileable_grid():
     cfg = R.workload_config(64, 128, 1e-4, 1e-5, 3e-13, DZ, 1)
     with pytest.raises(_lib.NLSEError, match="split-BF16"):
         _lib.Batch([cfg], [R.build_grids(cfg)])
+
+
+def test_batch_shared_operator_pulses_match_single_contexts():
+    """Pulses on one grid share the first pulse's operator copy inside the batch."""
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, DZ, STEPS)
+    g = R.build_grids(cfg)
+    u0s = [R.envelope_lens(1e-5, 100e-15, 1.5 + i, 1e-2, 10 + i)(g["rr"], g["tt"], cfg, g) for i in range(3)]
+    b = _lib.Batch([cfg] * 3, [g] * 3)
+    us = [dev(u) for u in u0s]
+    rhos = [dev(np.zeros(u.shape)) for u in u0s]
+    b.propagate(us, rhos, None, DZ, STEPS)
+    ctx = _lib.Context(cfg, g)
+    for i, u0 in enumerate(u0s):
+        u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+        ctx.propagate(u, rho, rs, DZ, STEPS, _lib.MODE_SPLIT_BF16)
+        assert np.array_equal(host(us[i]), host(u)), i
+        assert np.array_equal(host(rhos[i]), host(rho)), i
