@@ -27,6 +27,9 @@
  *   nlse_update_plasma    NonlinearOperator.update_plasma + the
  *                         solve_rate_equation_kernel      (operators.py:165-183,
  *                                                          kernels.py:36-106)
+ *   nlse_rate_equation    the solve_rate_equation_kernel launch alone
+ *                         (marches from the given t = 0 values)
+ *                                                         (kernels.py:36-106)
  *   nlse_step             Integrator.step                (integrator.py:138-149)
  *   nlse_propagate        the z loop of Integrator.propagate: nsteps x
  *                         (update_plasma, step)           (integrator.py:156-158)
@@ -62,7 +65,7 @@ enum {
     NLSE_F_KERR_RAMAN     = 1 << 4,  /* not built: rejected         */
     NLSE_F_SELF_STEEP     = 1 << 5,  /* not built: rejected         */
     NLSE_F_SPACE_TIME     = 1 << 6,  /* not built: rejected         */
-    NLSE_F_STE            = 1 << 7   /* not built: rejected         */
+    NLSE_F_STE            = 1 << 7   /* enable_ste (N_t <= 4096)    */
 };
 
 /* Linear-operator arithmetic used by nlse_step. */
@@ -107,6 +110,11 @@ typedef struct {
     double lut_log_min, lut_inv_dlog, lut_Imin, lut_Imax;
     double beta_g;              /* avalanche coefficient sigma/Ui            */
     double inv_tau_r;           /* 1/tau_r (0 = recombination off)           */
+    /* self-trapped excitons (used with NLSE_F_STE; grids.py:125-137)       */
+    const double *lut_s;        /* W at the exciton gap on the same grid     */
+    double beta_s;              /* sigma/Us                                  */
+    double inv_tau_ste;         /* 1/tau_ste (0 = no decay)                  */
+    double ste_pref;            /* exciton index term of split()             */
 } nlse_grid_desc;
 
 /* Build a context on the current CUDA device. */
@@ -120,22 +128,31 @@ int nlse_half_linear(nlse_ctx *ctx, void *u, double dz, void *stream);
  * (one tcgen05 product with the merged operator Y diag(P_r) Y = I + E). */
 int nlse_half_linear_ex(nlse_ctx *ctx, void *u, double dz, int mode, void *stream);
 
-/* (rhs, alpha) <- split(u, rho): RK right-hand side and absorption rate.
- * rhs: complex64 Nr x Nt, alpha: float32 Nr x Nt (may be NULL). */
-int nlse_split(nlse_ctx *ctx, const void *u, const float *rho, void *rhs,
-               float *alpha, void *stream);
+/* (rhs, alpha) <- split(u, rho, rho_s): RK right-hand side and absorption
+ * rate.  rhs: complex64 Nr x Nt, alpha: float32 Nr x Nt (may be NULL);
+ * rho_s may be NULL (exciton index term off). */
+int nlse_split(nlse_ctx *ctx, const void *u, const float *rho, const float *rho_s,
+               void *rhs, float *alpha, void *stream);
 
-/* u <- e^{-alpha dz/2} . RK4 . e^{-alpha dz/2} (u), rho frozen, in place. */
-int nlse_nonlinear_step(nlse_ctx *ctx, void *u, const float *rho, double dz,
-                        void *stream);
+/* u <- e^{-alpha dz/2} . RK4 . e^{-alpha dz/2} (u), rho / rho_s frozen,
+ * in place (rho_s may be NULL). */
+int nlse_nonlinear_step(nlse_ctx *ctx, void *u, const float *rho, const float *rho_s,
+                        double dz, void *stream);
 
 /* rho[:,0] = 0, then march the carrier rate equation along t for every r.
- * rho_s may be NULL; when given it is zeroed (the STE channel is off). */
+ * With the exciton channel on, rho_s (required then) is marched with rho;
+ * with it off, rho_s may be NULL and is zeroed when given. */
 int nlse_update_plasma(nlse_ctx *ctx, const void *u, float *rho, float *rho_s,
                        void *stream);
 
+/* The rate-equation kernel alone: march every row from its t = 0 values
+ * (rho[:,0], and rho_s[:,0] with the exciton channel; non-finite or negative
+ * starts count as 0), without update_plasma's reset of that column. */
+int nlse_rate_equation(nlse_ctx *ctx, const void *u, float *rho, float *rho_s,
+                       void *stream);
+
 /* Integrator.step(dz): half-linear, nonlinear block, half-linear, mask_r;
- * u in place, rho read (frozen), rho_s unused (may be NULL). */
+ * u in place, rho / rho_s read (frozen; rho_s may be NULL without excitons). */
 int nlse_step(nlse_ctx *ctx, void *u, const float *rho, const float *rho_s,
               double dz, int mode, void *stream);
 

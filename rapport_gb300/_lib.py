@@ -19,7 +19,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 
 # every symbol include/nlse.h declares (checked by the CPU test suite)
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
-           "nlse_update_plasma", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
+           "nlse_update_plasma", "nlse_rate_equation", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
            "nlse_half_linear_noalloc", "nlse_record", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
            "nlse_batch_set_split_terms", "nlse_batch_device_status", "nlse_batch_get_last_error",
@@ -43,6 +43,7 @@ class GridDesc(ctypes.Structure):
         ("pchip_n", _I), ("pchip_x", _P), ("pchip_c", _P),
         ("lut_n", _I), ("lut", _P), ("lut_log_min", _D), ("lut_inv_dlog", _D),
         ("lut_Imin", _D), ("lut_Imax", _D), ("beta_g", _D), ("inv_tau_r", _D),
+        ("lut_s", _P), ("beta_s", _D), ("inv_tau_ste", _D), ("ste_pref", _D),
     ]
 
 
@@ -64,9 +65,10 @@ def load():
     lib.nlse_half_linear_noalloc.argtypes = [_P, _P, _P, _P, _I, _I, _P]
     lib.nlse_debug_operator_product.argtypes = [_P, _P, _P, _D, _P]
     lib.nlse_device_status.argtypes = [_P, ctypes.POINTER(_I)]
-    lib.nlse_split.argtypes = [_P, _P, _P, _P, _P, _P]
-    lib.nlse_nonlinear_step.argtypes = [_P, _P, _P, _D, _P]
+    lib.nlse_split.argtypes = [_P, _P, _P, _P, _P, _P, _P]
+    lib.nlse_nonlinear_step.argtypes = [_P, _P, _P, _P, _D, _P]
     lib.nlse_update_plasma.argtypes = [_P, _P, _P, _P, _P]
+    lib.nlse_rate_equation.argtypes = [_P, _P, _P, _P, _P]
     lib.nlse_step.argtypes = [_P, _P, _P, _P, _D, _I, _P]
     lib.nlse_propagate.argtypes = [_P, _P, _P, _P, _D, _I, _I, _P]
     lib.nlse_scan_fallback_rows.argtypes = [_P, ctypes.POINTER(_I)]
@@ -171,6 +173,11 @@ def make_desc(cfg, g):
     d.lut_Imin, d.lut_Imax = kel["Imin"], kel["Imax"]
     d.beta_g = g["avalanche_coef"]
     d.inv_tau_r = g["inv_taur_eff"]
+    if cfg.enable_ste:
+        d.lut_s = _arr(kel["W_LUT_s"], keep)
+        d.beta_s = g["avalanche_coef_s"]
+        d.inv_tau_ste = g["inv_tau_ste"]
+        d.ste_pref = g["ste_pref"]
     return d, keep
 
 
@@ -261,22 +268,31 @@ class Context:
         _check(self.lib, self.h, self.lib.nlse_device_status(self.h, ctypes.byref(w)))
         return w.value
 
-    def split(self, u, rho, rhs, alpha):
+    def split(self, u, rho, rhs, alpha, rho_s=None):
         a = self._rho(alpha, "alpha") if alpha is not None else None
-        _check(self.lib, self.h, self.lib.nlse_split(self.h, self._field(u, "u"), self._rho(rho, "rho"),
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
+        _check(self.lib, self.h, self.lib.nlse_split(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs,
                                                      self._field(rhs, "rhs"), a, self._stream()))
 
-    def nonlinear_step(self, u, rho, dz):
+    def nonlinear_step(self, u, rho, dz, rho_s=None):
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
         _check(self.lib, self.h, self.lib.nlse_nonlinear_step(self.h, self._field(u, "u"), self._rho(rho, "rho"),
-                                                              float(dz), self._stream()))
+                                                              rs, float(dz), self._stream()))
 
     def update_plasma(self, u, rho, rho_s=None):
         rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
         _check(self.lib, self.h, self.lib.nlse_update_plasma(self.h, self._field(u, "u"), self._rho(rho, "rho"),
                                                              rs, self._stream()))
 
-    def step(self, u, rho, dz, mode=MODE_PLAIN_F32):
-        _check(self.lib, self.h, self.lib.nlse_step(self.h, self._field(u, "u"), self._rho(rho, "rho"), None,
+    def rate_equation(self, u, rho, rho_s=None):
+        """The carrier march alone, from the t = 0 values already in rho / rho_s."""
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
+        _check(self.lib, self.h, self.lib.nlse_rate_equation(self.h, self._field(u, "u"), self._rho(rho, "rho"),
+                                                             rs, self._stream()))
+
+    def step(self, u, rho, dz, mode=MODE_PLAIN_F32, rho_s=None):
+        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
+        _check(self.lib, self.h, self.lib.nlse_step(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs,
                                                     float(dz), int(mode), self._stream()))
 
     def propagate(self, u, rho, rho_s, dz, nsteps, mode=MODE_PLAIN_F32):

@@ -24,26 +24,27 @@
 
 // Two points per thread per iteration (16-byte field loads, 8-byte rho loads).
 __global__ void __launch_bounds__(256)
-k_nonlinear_step(float4 *__restrict__ u, const float2 *__restrict__ rho, size_t npair, float dz,
-                 NLParams p, const float4 *__restrict__ tab) {
+k_nonlinear_step(float4 *__restrict__ u, const float2 *__restrict__ rho, const float2 *__restrict__ rho_s,
+                 size_t npair, float dz, NLParams p, const float4 *__restrict__ tab) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < npair;
          i += (size_t)gridDim.x * blockDim.x) {
         float4 v = u[i];
         float2 r = __ldg(&rho[i]);
-        float2 a = nl_point(make_float2(v.x, v.y), r.x, dz, p, tab);
-        float2 b = nl_point(make_float2(v.z, v.w), r.y, dz, p, tab);
+        float2 rs = rho_s ? __ldg(&rho_s[i]) : make_float2(0.0f, 0.0f);
+        float2 a = nl_point(make_float2(v.x, v.y), r.x, rs.x, dz, p, tab);
+        float2 b = nl_point(make_float2(v.z, v.w), r.y, rs.y, dz, p, tab);
         u[i] = make_float4(a.x, a.y, b.x, b.y);
     }
 }
 
 __global__ void __launch_bounds__(256)
-k_split(const float2 *__restrict__ u, const float *__restrict__ rho, float2 *__restrict__ rhs,
-        float *__restrict__ alpha, size_t n, NLParams p, const float4 *__restrict__ tab) {
+k_split(const float2 *__restrict__ u, const float *__restrict__ rho, const float *__restrict__ rho_s,
+        float2 *__restrict__ rhs, float *__restrict__ alpha, size_t n, NLParams p, const float4 *__restrict__ tab) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n;
          i += (size_t)gridDim.x * blockDim.x) {
         float2 v = u[i];
         float r = rho[i];
-        rhs[i] = nl_rhs(v, r, p, tab);
+        rhs[i] = nl_rhs(v, r, rho_s ? rho_s[i] : 0.0f, p, tab);
         if (alpha) {
             float raw;
             alpha[i] = alpha_of(fmaf(v.x, v.x, v.y * v.y), r, p, tab, &raw);
@@ -60,16 +61,17 @@ static int grid_for(size_t n) {
     return (int)(want < cap ? want : cap);
 }
 
-cudaError_t launch_nonlinear_step(nlse_ctx *c, float2 *u, const float *rho, float dz, cudaStream_t stream) {
+cudaError_t launch_nonlinear_step(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, float dz,
+                                  cudaStream_t stream) {
     size_t npair = (size_t)c->Nr * c->Nt / 2;
-    k_nonlinear_step<<<grid_for(npair), 256, 0, stream>>>((float4 *)u, (const float2 *)rho, npair, dz,
-                                                         c->nl, c->d_pchip);
+    k_nonlinear_step<<<grid_for(npair), 256, 0, stream>>>((float4 *)u, (const float2 *)rho, (const float2 *)rho_s,
+                                                         npair, dz, c->nl, c->d_pchip);
     return cudaGetLastError();
 }
 
-cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, float2 *rhs, float *alpha,
-                         cudaStream_t stream) {
+cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, float2 *rhs,
+                         float *alpha, cudaStream_t stream) {
     size_t n = (size_t)c->Nr * c->Nt;
-    k_split<<<grid_for(n), 256, 0, stream>>>(u, rho, rhs, alpha, n, c->nl, c->d_pchip);
+    k_split<<<grid_for(n), 256, 0, stream>>>(u, rho, rho_s, rhs, alpha, n, c->nl, c->d_pchip);
     return cudaGetLastError();
 }

@@ -124,10 +124,12 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
     __syncthreads();
     float2 *R = fft_row<NT, true>(b0, b1, a.tw);
     const float *gr = rho + (size_t)r * NT;
+    const float *gs = a.rho_s ? a.rho_s + (size_t)r * NT : nullptr;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
         const float2 rr = *reinterpret_cast<const float2 *>(gr + t);
-        R[pidx(t)] = nl_point(R[pidx(t)], rr.x, a.dz, a.nl, a.pchip);
-        R[pidx(t + 1)] = nl_point(R[pidx(t + 1)], rr.y, a.dz, a.nl, a.pchip);
+        const float2 rs = gs ? *reinterpret_cast<const float2 *>(gs + t) : make_float2(0.0f, 0.0f);
+        R[pidx(t)] = nl_point(R[pidx(t)], rr.x, rs.x, a.dz, a.nl, a.pchip);
+        R[pidx(t + 1)] = nl_point(R[pidx(t + 1)], rr.y, rs.y, a.dz, a.nl, a.pchip);
     }
     __syncthreads();
     float2 *Y = fft_row<NT, false>(R, R == b0 ? b1 : b0, a.tw);

@@ -27,8 +27,39 @@
 
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__restrict__ rho_s, int Nt,
-            ScanParams p, const float *__restrict__ lut, int zero_first, int *__restrict__ stats) {
+            ScanParams p, const float *__restrict__ lut, const float *__restrict__ lut_s, int zero_first,
+            int *__restrict__ stats) {
     extern __shared__ float sm[];
+    if (p.ste) {
+        // two populations: sI sW sWs se ss + J (4) + B (2) arrays
+        const int S = scan_span(Nt, blockDim.x), C = (Nt - 1 + blockDim.x - 1) / blockDim.x;
+        const size_t row = blockIdx.x;
+        const float2 *g = u + row * (size_t)Nt;
+        float *ge = rho + row * (size_t)Nt, *gs = rho_s + row * (size_t)Nt;
+        float x0e = 0.0f, x0s = 0.0f;
+        if (!zero_first) {
+            x0e = ge[0];
+            x0s = gs[0];
+            if (!isfinite(x0e) || x0e < 0.0f) x0e = 0.0f;
+            if (!isfinite(x0s) || x0s < 0.0f) x0s = 0.0f;
+        }
+        float *sI = sm;
+        for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
+            float2 v = g[t];
+            sI[scan_slot(t, C)] = fmaf(v.x, v.x, v.y * v.y) * p.invE2;
+        }
+        __syncthreads();
+        float *jm[4] = {sm + 5 * S, sm + 6 * S, sm + 7 * S, sm + 8 * S};
+        float *jb[2] = {sm + 9 * S, sm + 10 * S};
+        scan_row2(sI, sm + S, sm + 2 * S, sm + 3 * S, sm + 4 * S, jm, jb, Nt, p, lut, lut_s, x0e, x0s, stats);
+        for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
+            if (t == 0 && !zero_first) continue;
+            const int q = scan_slot(t, C);
+            ge[t] = t == 0 ? 0.0f : sm[3 * S + q];
+            gs[t] = t == 0 ? 0.0f : sm[4 * S + q];
+        }
+        return;
+    }
     const int S = scan_span(Nt, blockDim.x), C = (Nt - 1 + blockDim.x - 1) / blockDim.x;
     float *sI = sm;
     const size_t row = blockIdx.x;
@@ -54,10 +85,10 @@ k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__rest
 
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s, int zero_first,
                              cudaStream_t stream) {
-    size_t smem = 5 * (size_t)scan_span(c->Nt, NLSE_ROW_THREADS) * sizeof(float);
+    size_t smem = (c->sc.ste ? 11 : 5) * (size_t)scan_span(c->Nt, NLSE_ROW_THREADS) * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(k_rate_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_rate_scan<<<c->Nr, NLSE_ROW_THREADS, smem, stream>>>(u, rho, rho_s, c->Nt, c->sc, c->d_lut_dt,
+    k_rate_scan<<<c->Nr, NLSE_ROW_THREADS, smem, stream>>>(u, rho, rho_s, c->Nt, c->sc, c->d_lut_dt, c->d_lut_s_dt,
                                                            zero_first, c->d_flag);
     return cudaGetLastError();
 }

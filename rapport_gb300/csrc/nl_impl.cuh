@@ -48,12 +48,12 @@ __device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p
     return isfinite(ar) ? fmaxf(ar, 0.0f) : 0.0f;
 }
 
-// RK right-hand side of split() for one point; rho frozen.
-__device__ __forceinline__ float2 nl_rhs(float2 u, float rho, const NLParams &p,
+// RK right-hand side of split() for one point; rho, rho_s frozen.
+__device__ __forceinline__ float2 nl_rhs(float2 u, float rho, float rho_s, const NLParams &p,
                                          const float4 *__restrict__ tab) {
     float a2 = fmaf(u.x, u.x, u.y * u.y);
     if (!(a2 >= 1e-30f)) return make_float2(0.0f, 0.0f);  // also NaN
-    float w = fmaf(p.kp, a2, -p.pp_def * rho);             // i w u
+    float w = fmaf(p.kp, a2, fmaf(p.ste_pref, rho_s, -p.pp_def * rho));  // i w u
     float corr = 0.0f;
     if (rho < 0.0f) {
         float raw;
@@ -65,16 +65,16 @@ __device__ __forceinline__ float2 nl_rhs(float2 u, float rho, const NLParams &p,
     return r;
 }
 
-__device__ __forceinline__ float2 nl_point(float2 u, float rho, float dz, const NLParams &p,
+__device__ __forceinline__ float2 nl_point(float2 u, float rho, float rho_s, float dz, const NLParams &p,
                                            const float4 *__restrict__ tab) {
     const float hdz = 0.5f * dz;
     float raw;
     float a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
     u = c_scale(u, expf(-hdz * a));
-    float2 k1 = nl_rhs(u, rho, p, tab);
-    float2 k2 = nl_rhs(make_float2(fmaf(hdz, k1.x, u.x), fmaf(hdz, k1.y, u.y)), rho, p, tab);
-    float2 k3 = nl_rhs(make_float2(fmaf(hdz, k2.x, u.x), fmaf(hdz, k2.y, u.y)), rho, p, tab);
-    float2 k4 = nl_rhs(make_float2(fmaf(dz, k3.x, u.x), fmaf(dz, k3.y, u.y)), rho, p, tab);
+    float2 k1 = nl_rhs(u, rho, rho_s, p, tab);
+    float2 k2 = nl_rhs(make_float2(fmaf(hdz, k1.x, u.x), fmaf(hdz, k1.y, u.y)), rho, rho_s, p, tab);
+    float2 k3 = nl_rhs(make_float2(fmaf(hdz, k2.x, u.x), fmaf(hdz, k2.y, u.y)), rho, rho_s, p, tab);
+    float2 k4 = nl_rhs(make_float2(fmaf(dz, k3.x, u.x), fmaf(dz, k3.y, u.y)), rho, rho_s, p, tab);
     const float s6 = dz * (1.0f / 6.0f);
     u.x = fmaf(s6, k1.x + 2.0f * (k2.x + k3.x) + k4.x, u.x);
     u.y = fmaf(s6, k1.y + 2.0f * (k2.y + k3.y) + k4.y, u.y);

@@ -59,7 +59,7 @@ static void free_ctx(nlse_ctx *c) {
     if (!c) return;
     prof_free(c);
     void *ptrs[] = {c->d_tw,    c->d_Y,   c->d_Y64, c->d_rho_modes, c->d_delta_k, c->d_spec_mask,
-                    c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_Pt,   c->d_Pr,     c->d_work,
+                    c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_lut_s_dt, c->d_Pt,   c->d_Pr,     c->d_work,
                     c->d_flag,  c->d_Er,  c->d_Ei,  c->d_A,  c->d_F32, c->d_Fb,  c->d_D,   c->d_Ptf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -96,13 +96,27 @@ static int check_desc(const nlse_grid_desc *d, nlse_error_slot *err) {
                        NLSE_MAX_NT);
         return NLSE_ERR_INVALID_ARG;
     }
-    const int unsupported = NLSE_F_KERR_RAMAN | NLSE_F_SELF_STEEP | NLSE_F_SPACE_TIME | NLSE_F_STE;
+    const int unsupported = NLSE_F_KERR_RAMAN | NLSE_F_SELF_STEEP | NLSE_F_SPACE_TIME;
     if (d->flags & unsupported) {
         nlse_set_error(err, NLSE_ERR_UNSUPPORTED,
-                       "flags 0x%x request Raman / self-steepening / space-time focusing / STE, "
+                       "flags 0x%x request Raman / self-steepening / space-time focusing, "
                        "which this library does not implement",
                        d->flags & unsupported);
         return NLSE_ERR_UNSUPPORTED;
+    }
+    if (d->flags & NLSE_F_STE) {
+        if (d->Nt > 4096) {
+            nlse_set_error(err, NLSE_ERR_UNSUPPORTED,
+                           "the exciton channel's carrier march holds 11 rows of N_t floats in shared memory: "
+                           "Nt=%d > 4096",
+                           d->Nt);
+            return NLSE_ERR_UNSUPPORTED;
+        }
+        if (!d->lut_s || !(d->beta_s >= 0) || !(d->inv_tau_ste >= 0) || !isfinite(d->ste_pref)) {
+            nlse_set_error(err, NLSE_ERR_INVALID_ARG,
+                           "NLSE_F_STE needs lut_s, beta_s >= 0, inv_tau_ste >= 0 and a finite ste_pref");
+            return NLSE_ERR_INVALID_ARG;
+        }
     }
     if (!d->Y || !d->rho_modes || !d->delta_k || !d->spec_mask || !d->mask_r || !d->pchip_x ||
         !d->pchip_c || !d->lut) {
@@ -194,6 +208,11 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     sc.Imin = (float)d->lut_Imin;
     sc.Imax = (float)d->lut_Imax;
     sc.lut_n = d->lut_n;
+    const bool ste = (d->flags & NLSE_F_STE) != 0;
+    sc.ste = ste ? 1 : 0;
+    sc.as_coef = ste ? (float)(d->beta_s * d->dt) : 0.0f;
+    sc.cs_ste = ste ? (float)(d->dt * d->inv_tau_ste) : 0.0f;
+    nl.ste_pref = ste ? (float)d->ste_pref : 0.0f;
 
     nlse_error_slot *err = gerr;
     // twiddles exp(-2 pi i k / Nt), FP64 then rounded
@@ -249,6 +268,15 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
             l[k] = (float)v;
         }
         NLSE_TRY(dev_upload(err, &c->d_lut_dt, l.data(), d->lut_n));
+        if (d->flags & NLSE_F_STE) {
+            for (int k = 0; k < d->lut_n; ++k) {
+                double v = d->lut_s[k] * d->dt;
+                if (!isfinite(v) || v < 0) v = 0.0;
+                if (v > FLT_MAX / 8) v = FLT_MAX / 8;
+                l[k] = (float)v;
+            }
+            NLSE_TRY(dev_upload(err, &c->d_lut_s_dt, l.data(), d->lut_n));
+        }
     }
     NLSE_TRY(dev_upload<float2>(err, &c->d_Pt, nullptr, Nt));
     NLSE_TRY(dev_upload<float2>(err, &c->d_Pr, nullptr, Nr));
@@ -469,6 +497,7 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
     a.sc = c->sc;
     a.dz = (float)dz;
     a.stats = c->d_flag;
+    a.rho_s = nullptr;
     return a;
 }
 
@@ -551,9 +580,10 @@ static int half_linear_split(nlse_ctx *c, float2 *u, double dz, cudaStream_t st)
     return row_next(c, a, nullptr, u, 0, 0, 0, st);
 }
 
-static int step_split(nlse_ctx *c, float2 *u, const float *rho, double dz, cudaStream_t st) {
+static int step_split(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, double dz, cudaStream_t st) {
     NLSE_SEQ(split_ready(c, dz, st));
     RowFusedArgs a = row_args(c, dz);
+    a.rho_s = c->sc.ste ? rho_s : nullptr;
     NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
     NLSE_SEQ(tc_gemm(c, st));
     NLSE_SEQ(row_nl(c, a, rho, st));
@@ -561,9 +591,35 @@ static int step_split(nlse_ctx *c, float2 *u, const float *rho, double dz, cudaS
     return row_next(c, a, nullptr, u, 0, 0, 1, st);
 }
 
+static int rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s, cudaStream_t st) {
+    PROF(K_RATE_SCAN);
+    return launched(c, launch_rate_scan(c, u, rho, rho_s, 1, st), "rate scan");
+}
+
+// With the exciton channel the two-population march runs as its own kernel
+// on the physical field that row_next writes out (to the workspace between
+// steps); the one-population march stays fused into the row kernels.
+static int propagate_split_ste(nlse_ctx *c, float2 *u, float *rho, float *rho_s, double dz, int n,
+                               cudaStream_t st) {
+    RowFusedArgs a = row_args(c, dz);
+    a.rho_s = rho_s;
+    NLSE_SEQ(rate_scan(c, u, rho, rho_s, st));
+    NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
+    for (int i = 0; i < n; ++i) {
+        const bool last = i == n - 1;
+        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(row_nl(c, a, rho, st));
+        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(row_next(c, a, nullptr, last ? u : c->d_work, last ? 0 : 1, 0, 1, st));
+        if (!last) NLSE_SEQ(rate_scan(c, c->d_work, rho, rho_s, st));
+    }
+    return NLSE_OK;
+}
+
 static int propagate_split(nlse_ctx *c, float2 *u, float *rho, float *rho_s, double dz, int n, cudaStream_t st) {
     if (n == 0) return NLSE_OK;
     NLSE_SEQ(split_ready(c, dz, st));
+    if (c->sc.ste) return propagate_split_ste(c, u, rho, rho_s, dz, n, st);
     RowFusedArgs a = row_args(c, dz);
     if (rho_s)
         NLSE_SEQ(launched(c, cudaMemsetAsync(rho_s, 0, (size_t)c->Nr * c->Nt * sizeof(float), st), "rho_s memset"));
@@ -591,37 +647,60 @@ extern "C" int nlse_half_linear_ex(nlse_ctx *c, void *u, double dz, int mode, vo
     return half_linear_impl(c, (float2 *)u, dz, nullptr, (cudaStream_t)stream);
 }
 
-extern "C" int nlse_split(nlse_ctx *c, const void *u, const float *rho, void *rhs, float *alpha, void *stream) {
+// rho_s as the nonlinear kernels read it: NULL when the exciton channel is off.
+static const float *ste_density(const nlse_ctx *c, const float *rho_s) { return c->sc.ste ? rho_s : nullptr; }
+
+// The exciton channel needs rho_s wherever the carriers are read or marched.
+static bool ste_ok(nlse_ctx *c, const float *rho_s) {
+    if (!c->sc.ste) return true;
+    if (!rho_s) {
+        bad(c, NLSE_ERR_INVALID_ARG, "rho_s is required with the exciton channel (NLSE_F_STE)");
+        return false;
+    }
+    return field_ok(c, rho_s, "rho_s");
+}
+
+extern "C" int nlse_split(nlse_ctx *c, const void *u, const float *rho, const float *rho_s, void *rhs, float *alpha,
+                          void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !field_ok(c, rhs, "rhs")) return NLSE_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     PROF(K_SPLIT);
-    return launched(c, launch_split(c, (const float2 *)u, rho, (float2 *)rhs, alpha, st), "split");
+    return launched(c, launch_split(c, (const float2 *)u, rho, ste_density(c, rho_s), (float2 *)rhs, alpha, st),
+                    "split");
 }
 
-extern "C" int nlse_nonlinear_step(nlse_ctx *c, void *u, const float *rho, double dz, void *stream) {
+extern "C" int nlse_nonlinear_step(nlse_ctx *c, void *u, const float *rho, const float *rho_s, double dz,
+                                   void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
     if (!(dz > 0) || !isfinite(dz)) return bad(c, NLSE_ERR_INVALID_ARG, "dz must be positive and finite");
     cudaStream_t st = (cudaStream_t)stream;
     PROF(K_NONLINEAR);
-    return launched(c, launch_nonlinear_step(c, (float2 *)u, rho, (float)dz, st), "nonlinear step");
+    return launched(c, launch_nonlinear_step(c, (float2 *)u, rho, ste_density(c, rho_s), (float)dz, st),
+                    "nonlinear step");
 }
 
 extern "C" int nlse_update_plasma(nlse_ctx *c, const void *u, float *rho, float *rho_s, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
-    if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
-    cudaStream_t st = (cudaStream_t)stream;
-    PROF(K_RATE_SCAN);
-    return launched(c, launch_rate_scan(c, (const float2 *)u, rho, rho_s, 1, st), "rate scan");
+    if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !ste_ok(c, rho_s)) return NLSE_ERR_INVALID_ARG;
+    return rate_scan(c, (const float2 *)u, rho, rho_s, (cudaStream_t)stream);
 }
 
-static int step_plain(nlse_ctx *c, float2 *u, const float *rho, double dz, cudaStream_t st) {
+extern "C" int nlse_rate_equation(nlse_ctx *c, const void *u, float *rho, float *rho_s, void *stream) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !ste_ok(c, rho_s)) return NLSE_ERR_INVALID_ARG;
+    cudaStream_t st = (cudaStream_t)stream;
+    PROF(K_RATE_SCAN);
+    return launched(c, launch_rate_scan(c, (const float2 *)u, rho, rho_s, 0, st), "rate scan");
+}
+
+static int step_plain(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, double dz, cudaStream_t st) {
     int s = half_linear_impl(c, u, dz, nullptr, st);
     if (s) return s;
     {
         PROF(K_NONLINEAR);
-        s = launched(c, launch_nonlinear_step(c, u, rho, (float)dz, st), "nonlinear step");
+        s = launched(c, launch_nonlinear_step(c, u, rho, ste_density(c, rho_s), (float)dz, st), "nonlinear step");
     }
     if (s) return s;
     return half_linear_impl(c, u, dz, c->d_mask_r, st);
@@ -629,31 +708,25 @@ static int step_plain(nlse_ctx *c, float2 *u, const float *rho, double dz, cudaS
 
 extern "C" int nlse_step(nlse_ctx *c, void *u, const float *rho, const float *rho_s, double dz, int mode,
                          void *stream) {
-    (void)rho_s;
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
-    if (mode == NLSE_MODE_SPLIT_BF16) return step_split(c, (float2 *)u, rho, dz, (cudaStream_t)stream);
+    if (c->sc.ste && rho_s && !field_ok(c, rho_s, "rho_s")) return NLSE_ERR_INVALID_ARG;
+    if (mode == NLSE_MODE_SPLIT_BF16) return step_split(c, (float2 *)u, rho, rho_s, dz, (cudaStream_t)stream);
     if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
-    return step_plain(c, (float2 *)u, rho, dz, (cudaStream_t)stream);
+    return step_plain(c, (float2 *)u, rho, rho_s, dz, (cudaStream_t)stream);
 }
 
 extern "C" int nlse_propagate(nlse_ctx *c, void *u, float *rho, float *rho_s, double dz, int nsteps, int mode,
                               void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
-    if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
+    if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !ste_ok(c, rho_s)) return NLSE_ERR_INVALID_ARG;
     if (nsteps < 0) return bad(c, NLSE_ERR_INVALID_ARG, "nsteps < 0");
     cudaStream_t st = (cudaStream_t)stream;
     if (mode == NLSE_MODE_SPLIT_BF16) return propagate_split(c, (float2 *)u, rho, rho_s, dz, nsteps, st);
     if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
     for (int i = 0; i < nsteps; ++i) {
-        int s;
-        {
-            PROF(K_RATE_SCAN);
-            s = launched(c, launch_rate_scan(c, (const float2 *)u, rho, rho_s, 1, st), "rate scan");
-        }
-        if (s) return s;
-        s = step_plain(c, (float2 *)u, rho, dz, st);
-        if (s) return s;
+        NLSE_SEQ(rate_scan(c, (const float2 *)u, rho, rho_s, st));
+        NLSE_SEQ(step_plain(c, (float2 *)u, rho, rho_s, dz, st));
     }
     return NLSE_OK;
 }
@@ -840,6 +913,8 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
             BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: batches run the split-BF16 form, which needs Nr %% 64 == 0 "
                                              "and Nt %% 256 == 0",
                        i);
+        if (b->ctx[i]->sc.ste)
+            BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: the exciton channel runs on single contexts only", i);
     }
     std::vector<GemmTile> tiles;
     std::vector<CUtensorMap> maps(4 * (size_t)n);

@@ -43,6 +43,7 @@ struct NLParams {
     float Imin, Imax;   // spline clip range
     float tiny_I;       // 1e-30 * invE2 (the +1e-30 of the reference, in I units)
     int n_int;          // spline intervals
+    float ste_pref;     // exciton index term: rhs += i ste_pref rho_s u
 };
 
 // Carrier-rate scan constants.
@@ -53,6 +54,9 @@ struct ScanParams {
     float na;           // rho_max
     float inv_na;
     float x_tiny;       // na * 2^-26: below it the depletion factor is exactly 1 in FP32
+    int ste;            // self-trapped-exciton channel on
+    float as_coef;      // beta_s * dt (re-ionisation by avalanche of excitons)
+    float cs_ste;       // dt / tau_ste
     float lut_log_min, lut_inv_dlog, Imin, Imax;
     int lut_n;
 };
@@ -69,6 +73,7 @@ struct RowFusedArgs {
     ScanParams sc;
     float dz;
     int *stats;
+    const float *rho_s;   // exciton density for the nonlinear step (NULL: channel off)
 };
 
 // One pulse of a batch, as the batched kernels see it (device memory).
@@ -105,6 +110,7 @@ struct nlse_ctx {
     float *d_mask_r;       // Nr
     float4 *d_pchip;       // n_int scaled Hermite coefficients
     float *d_lut_dt;       // lut_n entries of W * dt
+    float *d_lut_s_dt;     // lut_n entries of W(exciton gap) * dt
     // per-dz tables (rebuilt on the stream when dz changes)
     double cached_dz;
     float2 *d_Pt;          // Nt  exp(i dk dz/2) mask Rk iRk / Nt
@@ -156,9 +162,9 @@ cudaError_t launch_phase_tables(nlse_ctx *c, double dz, cudaStream_t stream);
 cudaError_t launch_gemm_f32(const float *A, const float *B, float *C, int M, int N, int K,
                             const float *row_scale, cudaStream_t stream);
 cudaError_t launch_fft_phase_ifft(nlse_ctx *c, float2 *u, cudaStream_t stream);
-cudaError_t launch_nonlinear_step(nlse_ctx *c, float2 *u, const float *rho, float dz,
+cudaError_t launch_nonlinear_step(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, float dz,
                                   cudaStream_t stream);
-cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, float2 *rhs,
+cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, float2 *rhs,
                          float *alpha, cudaStream_t stream);
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s,
                              int zero_first, cudaStream_t stream);

@@ -234,3 +234,262 @@ static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ
     }
     __syncthreads();
 }
+
+// ------------------------------------------------------------------ two populations (self-trapped excitons)
+// With the exciton channel on, the reference march (kernels.py:72-95) advances
+// (e, s) = (rho_e, rho_s) by
+//   e' = e^{ze} e + qe phi1(ze),  ze = a d - c,            qe = b d + r s / na
+//   s' = e^{zs} s + qs phi1(zs),  zs = -r / na - cs,       qs = c e
+// with d = depletion(e), r = bs + as e (re-ionisation), a = beta_g dt I_avg,
+// as = beta_s dt I_avg, b / bs = dt W_avg / dt Ws_avg, c = dt / tau_r,
+// cs = dt / tau_ste; each population's non-finite/negative result -> 0, and
+// e' + s' > na rescales both.  Newton's method linearises the map into a 2x2
+// affine recurrence, solved by a block scan of (matrix, vector) pairs.
+struct Aff2 {
+    float m00, m01, m10, m11, v0, v1;  // x -> M x + v
+};
+
+__device__ __forceinline__ Aff2 aff2_then(const Aff2 &f, const Aff2 &g) {  // f first, then g
+    Aff2 r;
+    r.m00 = fmaf(g.m00, f.m00, g.m01 * f.m10);
+    r.m01 = fmaf(g.m00, f.m01, g.m01 * f.m11);
+    r.m10 = fmaf(g.m10, f.m00, g.m11 * f.m10);
+    r.m11 = fmaf(g.m10, f.m01, g.m11 * f.m11);
+    r.v0 = fmaf(g.m00, f.v0, fmaf(g.m01, f.v1, g.v0));
+    r.v1 = fmaf(g.m10, f.v0, fmaf(g.m11, f.v1, g.v1));
+    return r;
+}
+
+__device__ __forceinline__ Aff2 aff2_identity() { return Aff2{1.0f, 0.0f, 0.0f, 1.0f, 0.0f, 0.0f}; }
+
+// phi1(z) and phi1'(z), accurate for small |z|
+__device__ __forceinline__ void phi1_d(float z, float e, float em1, float *ph, float *dph) {
+    const float az = fabsf(z);
+    *ph = az > 1e-4f ? em1 / z : fmaf(z, fmaf(z, fmaf(z, 1.0f / 24.0f, 1.0f / 6.0f), 0.5f), 1.0f);
+    *dph = az < 0.1f ? fmaf(z, fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.0f / 840.0f, 1.0f / 144.0f), 1.0f / 30.0f), 0.125f),
+                                    1.0f / 3.0f), 0.5f)
+                     : (z * e - em1) / (z * z);
+}
+
+// One step of the two-population march and its Jacobian; sets *clamped when
+// the e + s <= na rescale fires or e^{ze} leaves the FP32 range (ze > 80):
+// the caller then re-marches sequentially with step_exact2.  s / na is formed
+// first: r s alone overflows FP32 once both densities pass ~1e19.
+__device__ __forceinline__ void step_map2(float e, float s, float a, float as, float b, float bs, const ScanParams &p,
+                                          float *eo, float *so, Aff2 *J, bool *clamped) {
+    const float d = e < p.x_tiny ? 1.0f : fminf(fmaxf((p.na - e) * p.inv_na, 0.0f), 1.0f);
+    const float dd = (e >= p.x_tiny && e < p.na) ? -p.inv_na : 0.0f;
+    const float r = fmaf(as, e, bs);
+    const float ze = fmaf(a, d, -p.c_rec), zs = fmaf(-r, p.inv_na, -p.cs_ste);
+    if (ze > 80.0f) *clamped = true;
+    const float ee = expf(ze), eem1 = expm1f(ze), es = expf(zs), esm1 = expm1f(zs);
+    float phe, dphe, phs, dphs;
+    phi1_d(ze, ee, eem1, &phe, &dphe);
+    phi1_d(zs, es, esm1, &phs, &dphs);
+    const float sn = s * p.inv_na;
+    const float qe = fmaf(b, d, r * sn), qs = p.c_rec * e;
+    float y0 = fmaf(ee, e, qe * phe);
+    float y1 = fmaf(es, s, qs * phs);
+    const float ze_e = a * dd, zs_e = -as * p.inv_na;
+    const float qe_e = fmaf(b, dd, as * sn), qe_s = r * p.inv_na;
+    Aff2 j;
+    j.m00 = fmaf(ee, fmaf(e, ze_e, 1.0f), fmaf(qe_e, phe, qe * dphe * ze_e));
+    j.m01 = qe_s * phe;
+    j.m10 = fmaf(es * s, zs_e, fmaf(p.c_rec, phs, qs * dphs * zs_e));
+    j.m11 = es;
+    if (!isfinite(j.m00) || !isfinite(j.m01)) j.m00 = j.m01 = 0.0f;
+    if (!isfinite(j.m10) || !isfinite(j.m11)) j.m10 = j.m11 = 0.0f;
+    if (!isfinite(y0) || y0 < 0.0f) {
+        y0 = 0.0f;
+        j.m00 = j.m01 = 0.0f;
+    }
+    if (!isfinite(y1) || y1 < 0.0f) {
+        y1 = 0.0f;
+        j.m10 = j.m11 = 0.0f;
+    }
+    if (y0 + y1 > p.na) *clamped = true;
+    *eo = y0;
+    *so = y1;
+    *J = j;
+}
+
+// The reference's two-population step in FP32 (sequential).  Where e^{ze}
+// overflows FP32 but not FP64 (80 < ze <= 709.78) the electron update
+// e' = e^{ze} (e + qe/ze) - qe/ze is taken in log space; when it exceeds na the
+// reference's rescale by na / (e' + s') is applied in that form too, which
+// leaves s' = na s' / (e' + s') tiny but resolved.  Beyond 709.78 FP64
+// overflows as well and the non-finite -> 0 rule resets e'.
+__device__ __forceinline__ void step_exact2(float &e, float &s, float Ia, float b, float bs, const ScanParams &p) {
+    if (!isfinite(Ia)) {
+        e = s = 0.0f;
+        return;
+    }
+    const float a = p.a_coef * Ia, as = p.as_coef * Ia;
+    const float d = e < p.x_tiny ? 1.0f : fminf(fmaxf((p.na - e) * p.inv_na, 0.0f), 1.0f);
+    const float r = fmaf(as, e, bs);
+    const float ze = fmaf(a, d, -p.c_rec), zs = fmaf(-r, p.inv_na, -p.cs_ste);
+    const float qe = fmaf(b, d, r * (s * p.inv_na)), qs = p.c_rec * e;
+    float ph, dph;
+    const float es = expf(zs);
+    phi1_d(zs, es, expm1f(zs), &ph, &dph);
+    float y1 = fmaf(es, s, qs * ph);
+    if (!isfinite(y1) || y1 < 0.0f) y1 = 0.0f;
+    float y0;
+    if (ze > 709.78f) {
+        y0 = 0.0f;
+    } else if (ze > 80.0f) {
+        const float c0 = qe / ze, sm = e + c0;
+        if (!(sm > 0.0f) || !isfinite(sm)) {
+            y0 = 0.0f;
+        } else {
+            const float lg = ze + logf(sm);
+            if (lg > logf(p.na)) {
+                const float w = y1 > 0.0f ? expf(logf(y1) - lg) : 0.0f;  // s' / e' before the rescale
+                const float k = p.na / (1.0f + w);
+                e = k;
+                s = k * w;
+                return;
+            }
+            y0 = expf(lg) - c0;
+        }
+    } else {
+        const float ee = expf(ze);
+        phi1_d(ze, ee, expm1f(ze), &ph, &dph);
+        y0 = fmaf(ee, e, qe * ph);
+        if (!isfinite(y0) || y0 < 0.0f) y0 = 0.0f;
+    }
+    if (y0 + y1 > p.na) {
+        const float k = p.na / (y0 + y1);
+        y0 *= k;
+        y1 *= k;
+    }
+    e = y0;
+    s = y1;
+}
+
+static __device__ Aff2 block_exclusive_scan2(Aff2 v, Aff2 *wsum) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, nw = blockDim.x >> 5;
+    Aff2 inc = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        Aff2 o;
+        o.m00 = __shfl_up_sync(0xffffffffu, inc.m00, off);
+        o.m01 = __shfl_up_sync(0xffffffffu, inc.m01, off);
+        o.m10 = __shfl_up_sync(0xffffffffu, inc.m10, off);
+        o.m11 = __shfl_up_sync(0xffffffffu, inc.m11, off);
+        o.v0 = __shfl_up_sync(0xffffffffu, inc.v0, off);
+        o.v1 = __shfl_up_sync(0xffffffffu, inc.v1, off);
+        if (lane >= off) inc = aff2_then(o, inc);
+    }
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        Aff2 w = lane < nw ? wsum[lane] : aff2_identity();
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            Aff2 o;
+            o.m00 = __shfl_up_sync(0xffffffffu, w.m00, off);
+            o.m01 = __shfl_up_sync(0xffffffffu, w.m01, off);
+            o.m10 = __shfl_up_sync(0xffffffffu, w.m10, off);
+            o.m11 = __shfl_up_sync(0xffffffffu, w.m11, off);
+            o.v0 = __shfl_up_sync(0xffffffffu, w.v0, off);
+            o.v1 = __shfl_up_sync(0xffffffffu, w.v1, off);
+            if (lane >= off) w = aff2_then(o, w);
+        }
+        wsum[lane] = w;
+    }
+    __syncthreads();
+    const Aff2 wpre = wid > 0 ? wsum[wid - 1] : aff2_identity();
+    Aff2 lex;
+    lex.m00 = __shfl_up_sync(0xffffffffu, inc.m00, 1);
+    lex.m01 = __shfl_up_sync(0xffffffffu, inc.m01, 1);
+    lex.m10 = __shfl_up_sync(0xffffffffu, inc.m10, 1);
+    lex.m11 = __shfl_up_sync(0xffffffffu, inc.m11, 1);
+    lex.v0 = __shfl_up_sync(0xffffffffu, inc.v0, 1);
+    lex.v1 = __shfl_up_sync(0xffffffffu, inc.v1, 1);
+    if (lane == 0) lex = aff2_identity();
+    const Aff2 r = aff2_then(wpre, lex);
+    __syncthreads();
+    return r;
+}
+
+// Two-population march of one row (all threads).  sI: intensities at slots
+// (synced); scratch arrays of scan_span(Nt) floats: sW, sWs, se, ss, and J
+// (4 arrays jm[0..3]) + B (2 arrays jb[0..1]).  On return (synced) se / ss hold
+// rho_e / rho_s at the slots.  x0e / x0s: the t = 0 values.
+static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *se, float *ss, float *const *jm,
+                                 float *const *jb, int Nt, const ScanParams &p, const float *__restrict__ lut,
+                                 const float *__restrict__ lut_s, float x0e, float x0s, int *stats) {
+    __shared__ Aff2 wsum[32];
+    __shared__ float red[100];
+    const int T = Nt - 1;
+    const int C = (T + blockDim.x - 1) / blockDim.x;
+    for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
+        const int q = scan_slot(t, C);
+        sW[q] = lut_rate_dt(sI[q], lut, p);
+        sWs[q] = lut_rate_dt(sI[q], lut_s, p);
+        se[q] = t == 0 ? x0e : 0.0f;
+        ss[q] = t == 0 ? x0s : 0.0f;
+    }
+    __syncthreads();
+    const int n0 = min((int)threadIdx.x * C, T), n1 = min(n0 + C, T);
+    int converged = 0, clamp_any = 0;
+    for (int it = 0; it < SCAN_MAX_IT; ++it) {
+        Aff2 acc = aff2_identity();
+        bool cl = false;
+        for (int n = n0; n < n1; ++n) {
+            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+            const float Ia = 0.5f * (sI[q0] + sI[q1]);
+            const float b = 0.5f * (sW[q0] + sW[q1]), bs = 0.5f * (sWs[q0] + sWs[q1]);
+            const float e = se[q0], s = ss[q0];
+            Aff2 J = {0.0f, 0.0f, 0.0f, 0.0f, 0.0f, 0.0f};
+            float eo = 0.0f, so = 0.0f;
+            if (isfinite(Ia)) step_map2(e, s, p.a_coef * Ia, p.as_coef * Ia, b, bs, p, &eo, &so, &J, &cl);
+            J.v0 = eo - fmaf(J.m00, e, J.m01 * s);
+            J.v1 = so - fmaf(J.m10, e, J.m11 * s);
+            jm[0][q0] = J.m00;
+            jm[1][q0] = J.m01;
+            jm[2][q0] = J.m10;
+            jm[3][q0] = J.m11;
+            jb[0][q0] = J.v0;
+            jb[1][q0] = J.v1;
+            acc = aff2_then(acc, J);
+        }
+        const Aff2 pre = block_exclusive_scan2(acc, wsum);
+        float xe = fmaf(pre.m00, x0e, fmaf(pre.m01, x0s, pre.v0));
+        float xs = fmaf(pre.m10, x0e, fmaf(pre.m11, x0s, pre.v1));
+        float dmax = 0.0f, xmax = 0.0f;
+        for (int n = n0; n < n1; ++n) {
+            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+            const float ne = fmaf(jm[0][q0], xe, fmaf(jm[1][q0], xs, jb[0][q0]));
+            const float ns = fmaf(jm[2][q0], xe, fmaf(jm[3][q0], xs, jb[1][q0]));
+            xe = ne;
+            xs = ns;
+            dmax = fmaxf(dmax, fmaxf(fabsf(xe - se[q1]), fabsf(xs - ss[q1])));
+            xmax = fmaxf(xmax, fmaxf(fabsf(xe), fabsf(xs)));
+            se[q1] = xe;
+            ss[q1] = xs;
+        }
+        int f = cl ? 1 : 0;
+        block_reduce(dmax, xmax, f, red);
+        clamp_any |= f;
+        if (clamp_any) break;
+        if (it > 0 && dmax <= SCAN_TOL * xmax) {
+            converged = 1;
+            break;
+        }
+    }
+    if (!converged) {
+        if (threadIdx.x == 0) {
+            float e = x0e, s = x0s;
+            for (int n = 0; n < T; ++n) {
+                const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+                step_exact2(e, s, 0.5f * (sI[q0] + sI[q1]), 0.5f * (sW[q0] + sW[q1]), 0.5f * (sWs[q0] + sWs[q1]), p);
+                se[q1] = e;
+                ss[q1] = s;
+            }
+            if (stats) atomicAdd(&stats[1], 1);
+        }
+    }
+    __syncthreads();
+}

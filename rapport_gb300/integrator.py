@@ -124,7 +124,7 @@ class Integrator:
     # ------------------------------------------------------------------ stepping
     def step(self, dz):
         """Integrator.step: half-linear, nonlinear block, half-linear, mask_r (rho frozen)."""
-        self.ctx.step(self.u, self.rho, dz, self.mode)
+        self.ctx.step(self.u, self.rho, dz, self.mode, self.rho_s)
 
     def advance(self, nsteps):
         """nsteps iterations of update_plasma + step, queued without host syncs."""

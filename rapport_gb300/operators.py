@@ -48,9 +48,10 @@ class NonlinearOperator:
         """-> (rhs, alpha): RK right-hand side and absorption rate (operators.py:89-146)."""
         u = u.contiguous()
         rho = rho.contiguous()
+        rho_s = rho_s.contiguous() if (rho_s is not None and self.enable_ste) else None
         rhs = torch.empty_like(u)
         alpha = torch.empty(u.shape, dtype=torch.float32, device=u.device)
-        self.ctx.split(u, rho, rhs, alpha)
+        self.ctx.split(u, rho, rhs, alpha, rho_s)
         return rhs, alpha
 
     def update_plasma(self, u, rho, rho_s, dt=None, blocks=None, threads=None):
@@ -59,7 +60,7 @@ class NonlinearOperator:
         signature compatibility (dt is fixed by the grid)."""
         self.ctx.update_plasma(u, rho, rho_s)
 
-    def nonlinear_step(self, u, rho, dz):
+    def nonlinear_step(self, u, rho, dz, rho_s=None):
         """The alpha/2 + RK4 + alpha/2 block of Integrator.step, in place."""
-        self.ctx.nonlinear_step(u, rho, dz)
+        self.ctx.nonlinear_step(u, rho, dz, rho_s if self.enable_ste else None)
         return u

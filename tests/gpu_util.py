@@ -32,7 +32,7 @@ class Case:
         self.lin = R.LinearOperator(self.cfg, self.g)
         self.nl = R.NonlinearOperator(self.cfg, self.g, self.lin.ctx)
         self.ctx = self.lin.ctx
-        self.og = O.OracleGrid(O.workload_config(Nr, Nt, R_max, w0, T_half))
+        self.og = O.OracleGrid(O.workload_config(Nr, Nt, R_max, w0, T_half, **over))
         self.dz = dz
         self.u0 = O.lens_gaussian(self.og, w0, fwhm, E, f, seed)
 
