@@ -20,8 +20,12 @@ INCLUDE = os.path.join(os.path.dirname(PKG), "include")
 
 NVCC = os.environ.get("NVCC", "nvcc")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
+# -fmad=false: no implicit multiply-add contraction.  Multiply-adds are written
+# as fmaf in the sources, so every instance of a shared device function (the
+# single-pulse and the batched row kernels, the elementwise and the fused
+# nonlinear step) rounds identically and their results agree bit for bit.
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", INCLUDE,
-         "--expt-relaxed-constexpr"]
+         "--expt-relaxed-constexpr", "-fmad=false"]
 
 
 def _newest_header():

@@ -41,11 +41,11 @@ k_record(const float2 *__restrict__ u, const float *__restrict__ rho, const floa
         const float plasma = p.pp_abs * rh;
         const double w = 2.0 * (double)a2;
         acc[0] += (double)a2;
-        acc[4] += w * photo;
-        acc[5] += w * plasma;
+        acc[4] = fma(w, (double)photo, acc[4]);
+        acc[5] = fma(w, (double)plasma, acc[5]);
         if (nbins) {
             const int b = bin_of_t[t];
-            if (b >= 0 && b < nbins) acc[REC_FIXED + b] += w * (double)(photo + plasma);
+            if (b >= 0 && b < nbins) acc[REC_FIXED + b] = fma(w, (double)(photo + plasma), acc[REC_FIXED + b]);
         }
     }
     __shared__ double sred[8][REC_FIXED + 8];

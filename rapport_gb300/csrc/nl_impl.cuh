@@ -43,7 +43,7 @@ __device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p
             photo = I;  // NaN: split() turns the sum into alpha = 0 (nan_to_num)
         }             // +Inf: W(Imax) / Inf = 0 in split()
     }
-    float ar = photo + p.pp_abs * rho;
+    float ar = fmaf(p.pp_abs, rho, photo);
     *raw = ar;
     return isfinite(ar) ? fmaxf(ar, 0.0f) : 0.0f;
 }
@@ -76,8 +76,8 @@ __device__ __forceinline__ float2 nl_point(float2 u, float rho, float rho_s, flo
     float2 k3 = nl_rhs(make_float2(fmaf(hdz, k2.x, u.x), fmaf(hdz, k2.y, u.y)), rho, rho_s, p, tab);
     float2 k4 = nl_rhs(make_float2(fmaf(dz, k3.x, u.x), fmaf(dz, k3.y, u.y)), rho, rho_s, p, tab);
     const float s6 = dz * (1.0f / 6.0f);
-    u.x = fmaf(s6, k1.x + 2.0f * (k2.x + k3.x) + k4.x, u.x);
-    u.y = fmaf(s6, k1.y + 2.0f * (k2.y + k3.y) + k4.y, u.y);
+    u.x = fmaf(s6, fmaf(2.0f, k2.x + k3.x, k1.x) + k4.x, u.x);
+    u.y = fmaf(s6, fmaf(2.0f, k2.y + k3.y, k1.y) + k4.y, u.y);
     a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
     return c_scale(u, expf(-hdz * a));
 }

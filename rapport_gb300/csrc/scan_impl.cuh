@@ -62,9 +62,9 @@ __device__ __forceinline__ float step_map(float x, float a, float b, const ScanP
         dph = fmaf(z, fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.0f / 840.0f, 1.0f / 144.0f), 1.0f / 30.0f),
                                    0.125f), 1.0f / 3.0f), 0.5f);
     else
-        dph = (z * e - em1) / (z * z);
+        dph = fmaf(z, e, -em1) / (z * z);
     float zp = a * dd;
-    float Jv = fmaf(x * e, zp, e) + b * fmaf(dd, ph, d * dph * zp);
+    float Jv = fmaf(b, fmaf(dd, ph, d * dph * zp), fmaf(x * e, zp, e));
     if (!isfinite(Jv)) Jv = 0.0f;
     if (!isfinite(y) || y < 0.0f) {
         y = 0.0f;
@@ -268,7 +268,7 @@ __device__ __forceinline__ void phi1_d(float z, float e, float em1, float *ph, f
     *ph = az > 1e-4f ? em1 / z : fmaf(z, fmaf(z, fmaf(z, 1.0f / 24.0f, 1.0f / 6.0f), 0.5f), 1.0f);
     *dph = az < 0.1f ? fmaf(z, fmaf(z, fmaf(z, fmaf(z, fmaf(z, 1.0f / 840.0f, 1.0f / 144.0f), 1.0f / 30.0f), 0.125f),
                                     1.0f / 3.0f), 0.5f)
-                     : (z * e - em1) / (z * z);
+                     : fmaf(z, e, -em1) / (z * z);
 }
 
 // One step of the two-population march and its Jacobian; sets *clamped when
