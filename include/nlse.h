@@ -62,9 +62,10 @@ enum {
     NLSE_F_PHOTO_LOSS     = 1 << 1,  /* enable_photoionization_loss */
     NLSE_F_PLASMA_DEFOC   = 1 << 2,  /* enable_plasma_defocusing    */
     NLSE_F_PLASMA_ABSORB  = 1 << 3,  /* enable_plasma_absorption    */
-    NLSE_F_KERR_RAMAN     = 1 << 4,  /* not built: rejected         */
-    NLSE_F_SELF_STEEP     = 1 << 5,  /* not built: rejected         */
-    NLSE_F_SPACE_TIME     = 1 << 6,  /* not built: rejected         */
+    NLSE_F_KERR_RAMAN     = 1 << 4,  /* enable_kerr_raman  (N_t <= 4096) */
+    NLSE_F_SELF_STEEP     = 1 << 5,  /* enable_self_steepening (N_t <= 4096) */
+    NLSE_F_SPACE_TIME     = 1 << 6,  /* enable_space_time_focusing (N_t <= 4096,
+                                        plain mode only)          */
     NLSE_F_STE            = 1 << 7   /* enable_ste (N_t <= 4096)    */
 };
 
@@ -115,6 +116,13 @@ typedef struct {
     double beta_s;              /* sigma/Us                                  */
     double inv_tau_ste;         /* 1/tau_ste (0 = no decay)                  */
     double ste_pref;            /* exciton index term of split()             */
+    /* full-physics split (grids.py:79-116; used with the flags above)     */
+    double f_R;                 /* Raman fraction (kerr_I weights 1-f_R, f_R) */
+    const double *R_f;          /* NLSE_F_KERR_RAMAN: Raman response spectrum,
+                                   Nt complex, interleaved re,im, FFT order  */
+    const double *T_op;         /* NLSE_F_SELF_STEEP: T-hat(Omega), Nt       */
+    const double *inv_U_nl;     /* NLSE_F_SPACE_TIME: U^-1 of split(), Nt    */
+    const double *inv_U_op;     /* NLSE_F_SPACE_TIME: U^-1 of half_linear, Nt */
 } nlse_grid_desc;
 
 /* Build a context on the current CUDA device. */

@@ -44,6 +44,7 @@ class GridDesc(ctypes.Structure):
         ("lut_n", _I), ("lut", _P), ("lut_log_min", _D), ("lut_inv_dlog", _D),
         ("lut_Imin", _D), ("lut_Imax", _D), ("beta_g", _D), ("inv_tau_r", _D),
         ("lut_s", _P), ("beta_s", _D), ("inv_tau_ste", _D), ("ste_pref", _D),
+        ("f_R", _D), ("R_f", _P), ("T_op", _P), ("inv_U_nl", _P), ("inv_U_op", _P),
     ]
 
 
@@ -178,6 +179,14 @@ def make_desc(cfg, g):
         d.beta_s = g["avalanche_coef_s"]
         d.inv_tau_ste = g["inv_tau_ste"]
         d.ste_pref = g["ste_pref"]
+    d.f_R = cfg.f_R
+    if cfg.enable_kerr_raman:
+        d.R_f = _arr(np.ascontiguousarray(np.asarray(g["R_f"], dtype=np.complex128)).view(np.float64), keep)
+    if cfg.enable_self_steepening:
+        d.T_op = _arr(g["T_op"], keep)
+    if cfg.enable_space_time_focusing:
+        d.inv_U_nl = _arr(g["inv_U_nl"], keep)
+        d.inv_U_op = _arr(g["inv_U_op"], keep)
     return d, keep
 
 

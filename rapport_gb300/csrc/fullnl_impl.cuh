@@ -1,0 +1,224 @@
+// Full-physics nonlinear block: split() with Raman, self-steepening and
+// space-time focusing (operators.py:89-146, grids.py:79-116), one row of the
+// field per CTA, every transform in shared memory.
+//
+// split(S) of the reference, for a row S(t):
+//   kerr_I = (1 - f_R) |S|^2 [instantaneous] + f_R Re F^-1[F[|S|^2] R_f] [Raman]
+//   X1 = i kerr_pref kerr_I S,   X2 = photo S,
+//   X3 = (-pp_abs rho + i (-pp_def rho + ste_pref rho_s)) S
+//   k  = F^-1[(T^2 F[X1] - T F[X2] + F[X3]) U^-1] + alpha S
+// with T = 1 without self-steepening and U^-1 = 1 without space-time focusing.
+// Transforms a term does not need are skipped: with U^-1 = 1, X3 is added
+// pointwise; with T = U^-1 = 1 the whole right-hand side is pointwise (the
+// algebraically reduced form of nl_rhs, with the Raman-convolved intensity).
+// The reference then zeroes k where |S|^2 < 1e-30 and every non-finite k
+// (nan_to_num).  Because every term of the row passes through FFTs there, one
+// non-finite X anywhere in the row makes the whole row of k non-finite, i.e.
+// zero; the block reproduces that with a row-wide flag (__syncthreads_or), so
+// the rule holds whichever transforms run.
+//
+// Thread t of the CTA owns the points t, t + T, t + 2T, ... (T = 256).  Shared
+// memory holds three padded complex rows (the FFT ping-pong buffers) and three
+// plain complex rows: the post-alpha field U, the RK accumulator and the stage
+// field S, each read and written only by the thread owning the point.
+#pragma once
+#include "nl_impl.cuh"
+
+// Shared memory of the full block: three padded complex row buffers (FFTs)
+// and the rows U, KS, S.  202,752 bytes at N_t = 4096.
+template <int NT>
+__host__ __device__ constexpr size_t full_smem_bytes() {
+    return 3 * (size_t)fft_slots(NT) * sizeof(float2) + 3 * (size_t)NT * sizeof(float2);
+}
+
+struct FullRows {
+    float2 *B0, *B1, *B2;  // padded FFT buffers
+    float2 *U, *KS, *S;    // post-alpha field, RK accumulator, stage field (index t)
+};
+
+template <int NT>
+__device__ __forceinline__ FullRows full_rows(float2 *smem) {
+    FullRows r;
+    r.B0 = smem;
+    r.B1 = smem + fft_slots(NT);
+    r.B2 = smem + 2 * fft_slots(NT);
+    r.U = smem + 3 * fft_slots(NT);
+    r.KS = r.U + NT;
+    r.S = r.KS + NT;
+    return r;
+}
+
+// photo (before alpha) as split() computes it: NaN for a NaN intensity or a
+// NaN density (the reference's clip propagates NaN), 0 for +Inf intensity.
+__device__ __forceinline__ float photo_term(float a2, float rho, const NLParams &p,
+                                            const float4 *__restrict__ tab) {
+    if (!p.photo_on) return 0.0f;
+    const float I = a2 * p.invE2;
+    if (isfinite(I)) {
+        const float dep = isnan(rho) ? rho : fminf(fmaxf((p.rho_max - rho) * p.inv_rho_max, 0.0f), 1.0f);
+        return photo_rate(I, p, tab) * dep;
+    }
+    return isnan(I) ? I : 0.0f;
+}
+
+// alpha = max(nan_to_num(photo + pp_abs rho), 0)
+__device__ __forceinline__ float alpha_from(float photo, float rho, const NLParams &p) {
+    const float ar = fmaf(p.pp_abs, rho, photo);
+    return isfinite(ar) ? fmaxf(ar, 0.0f) : 0.0f;
+}
+
+__device__ __forceinline__ bool c_finite(float2 v) { return isfinite(v.x) && isfinite(v.y); }
+
+// k = split(S) for the thread's points of the stage field S (shared, index
+// t); sink(t, k_t) consumes each value and may overwrite S[t], which is not
+// read again for that point.  All threads of the CTA call it; the three FFT
+// buffers are free again on return (synced).
+template <int NT, typename Sink>
+__device__ __forceinline__ void rhs_full(const FullRows &m, const float *__restrict__ rho,
+                                         const float *__restrict__ rhos, const NLParams &p,
+                                         const float4 *__restrict__ tab, const FullTabs &ft,
+                                         const float2 *__restrict__ tw, Sink sink) {
+    constexpr int TT = NLSE_ROW_THREADS;
+    constexpr float inv_n = 1.0f / (float)NT;
+    const bool fft_path = ft.T != nullptr || ft.invU != nullptr;
+    float2 *B0 = m.B0, *B1 = m.B1, *B2 = m.B2;
+    const float2 *S = m.S;
+    // Raman: kerr_I's convolution term Re F^-1[F[|S|^2] R_f], left in Q
+    const float2 *Q = nullptr;
+    if (ft.Rf) {
+        for (int t = threadIdx.x; t < NT; t += TT) {
+            const float2 v = S[t];
+            B0[pidx(t)] = make_float2(fmaf(v.x, v.x, v.y * v.y), 0.0f);
+        }
+        __syncthreads();
+        float2 *R = fft_row<NT, false>(B0, B1, tw);
+        for (int f = threadIdx.x; f < NT; f += TT) R[pidx(f)] = c_mul(R[pidx(f)], __ldg(&ft.Rf[f]));
+        __syncthreads();
+        Q = fft_row<NT, true>(R, R == B0 ? B1 : B0, tw);
+    }
+    // the pointwise terms; X1 (and X2) into the transform buffers on the FFT
+    // path (a point's Q value is read before the same thread overwrites it)
+    int bad = 0;
+    for (int t = threadIdx.x; t < NT; t += TT) {
+        const float2 s = S[t];
+        const float a2 = fmaf(s.x, s.x, s.y * s.y);
+        const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
+        const float ph = photo_term(a2, r, p, tab);
+        const float kr = Q ? Q[pidx(t)].x * inv_n : 0.0f;
+        const float K = fmaf(p.kp, a2, p.kp_raman * kr);  // kerr_pref * kerr_I
+        const float2 x1 = make_float2(-K * s.y, K * s.x);   // i K S
+        const float2 x2 = c_scale(s, ph);
+        const float2 x3 = c_mul(s, make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r)));
+        bad |= !(c_finite(x1) && c_finite(x2) && c_finite(x3));
+        if (ft.T) {
+            B0[pidx(t)] = x1;
+            B2[pidx(t)] = x2;
+        } else if (ft.invU) {
+            B0[pidx(t)] = c_add(c_sub(x1, x2), x3);
+        }
+    }
+    bad = __syncthreads_or(bad);  // also orders the buffer writes before the transforms
+    const float2 *Y = nullptr;    // the spectral part of k (inverse-transformed, unnormalised)
+    if (fft_path && !bad) {
+        float2 *C;
+        if (ft.T) {
+            float2 *P1 = fft_row<NT, false>(B0, B1, tw);
+            float2 *fr = P1 == B0 ? B1 : B0;
+            float2 *P2 = fft_row<NT, false>(B2, fr, tw);
+            float2 *fr2 = P2 == B2 ? fr : B2;  // the buffer neither P1 nor P2 occupies
+            for (int f = threadIdx.x; f < NT; f += TT) {
+                const float T = __ldg(&ft.T[f]);
+                const float2 a = P1[pidx(f)], b = P2[pidx(f)];
+                // T^2 F[X1] - T F[X2] = T (T F[X1] - F[X2])
+                P1[pidx(f)] = c_scale(make_float2(fmaf(T, a.x, -b.x), fmaf(T, a.y, -b.y)), T);
+            }
+            C = P1;
+            if (ft.invU) {
+                // F[X3] through the two free buffers, then the U^-1 factor
+                for (int t = threadIdx.x; t < NT; t += TT) {
+                    const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
+                    P2[pidx(t)] = c_mul(S[t], make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r)));
+                }
+                __syncthreads();
+                float2 *P3 = fft_row<NT, false>(P2, fr2, tw);
+                for (int f = threadIdx.x; f < NT; f += TT)
+                    C[pidx(f)] = c_scale(c_add(C[pidx(f)], P3[pidx(f)]), __ldg(&ft.invU[f]));
+                __syncthreads();
+                Y = fft_row<NT, true>(C, P3 == P2 ? fr2 : P2, tw);
+            } else {
+                __syncthreads();
+                Y = fft_row<NT, true>(C, P2, tw);
+            }
+        } else {
+            C = fft_row<NT, false>(B0, B1, tw);
+            for (int f = threadIdx.x; f < NT; f += TT) C[pidx(f)] = c_scale(C[pidx(f)], __ldg(&ft.invU[f]));
+            __syncthreads();
+            Y = fft_row<NT, true>(C, C == B0 ? B1 : B0, tw);
+        }
+    }
+    // k per point
+    for (int t = threadIdx.x; t < NT; t += TT) {
+        const float2 s = S[t];
+        const float a2 = fmaf(s.x, s.x, s.y * s.y);
+        const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
+        const float ph = photo_term(a2, r, p, tab);
+        const float al = alpha_from(ph, r, p);
+        float2 k;
+        if (fft_path) {
+            k = bad ? make_float2(0.0f, 0.0f) : c_scale(Y[pidx(t)], inv_n);
+            if (!ft.invU)  // X3 pointwise
+                k = c_add(k, c_mul(s, make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r))));
+            k = make_float2(fmaf(al, s.x, k.x), fmaf(al, s.y, k.y));
+        } else {
+            // X1 - X2 + X3 + alpha S = i w S + (alpha - photo - pp_abs rho) S
+            const float kr = Q ? Q[pidx(t)].x * inv_n : 0.0f;
+            const float w = fmaf(p.kp, a2, p.kp_raman * kr) + fmaf(p.ste_pref, rs, -p.pp_def * r);
+            const float corr = al - fmaf(p.pp_abs, r, ph);
+            k = make_float2(fmaf(corr, s.x, -w * s.y), fmaf(corr, s.y, w * s.x));
+        }
+        if (bad || !(a2 >= 1e-30f) || !c_finite(k)) k = make_float2(0.0f, 0.0f);
+        sink(t, k);
+    }
+    __syncthreads();  // the FFT buffers are free for the next call
+}
+
+// alpha/2, RK4 on split(), alpha/2 (Integrator.step, integrator.py:140-147)
+// for the row held in m.U (index t; all threads); rho / rho_s frozen.  On
+// return (synced) m.U holds the new field.
+template <int NT>
+__device__ __forceinline__ void nl_block_full(const FullRows &m, const float *__restrict__ rho,
+                                              const float *__restrict__ rhos, float dz, const NLParams &p,
+                                              const float4 *__restrict__ tab, const FullTabs &ft,
+                                              const float2 *__restrict__ tw) {
+    constexpr int TT = NLSE_ROW_THREADS;
+    const float hdz = 0.5f * dz;
+    float2 *U = m.U, *KS = m.KS, *S = m.S;
+    for (int t = threadIdx.x; t < NT; t += TT) {
+        const float2 u = U[t];
+        const float r = __ldg(&rho[t]);
+        const float al = alpha_from(photo_term(fmaf(u.x, u.x, u.y * u.y), r, p, tab), r, p);
+        U[t] = S[t] = c_scale(u, expf(-hdz * al));
+    }
+    // k1..k4; KS = k1 + 2 k2 + 2 k3 + k4 (each thread touches only its points)
+    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) {
+        KS[t] = k;
+        S[t] = make_float2(fmaf(hdz, k.x, U[t].x), fmaf(hdz, k.y, U[t].y));
+    });
+    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) {
+        KS[t] = make_float2(fmaf(2.0f, k.x, KS[t].x), fmaf(2.0f, k.y, KS[t].y));
+        S[t] = make_float2(fmaf(hdz, k.x, U[t].x), fmaf(hdz, k.y, U[t].y));
+    });
+    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) {
+        KS[t] = make_float2(fmaf(2.0f, k.x, KS[t].x), fmaf(2.0f, k.y, KS[t].y));
+        S[t] = make_float2(fmaf(dz, k.x, U[t].x), fmaf(dz, k.y, U[t].y));
+    });
+    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) { KS[t] = c_add(KS[t], k); });
+    const float s6 = dz * (1.0f / 6.0f);
+    for (int t = threadIdx.x; t < NT; t += TT) {
+        float2 u = make_float2(fmaf(s6, KS[t].x, U[t].x), fmaf(s6, KS[t].y, U[t].y));
+        const float r = __ldg(&rho[t]);
+        const float al = alpha_from(photo_term(fmaf(u.x, u.x, u.y * u.y), r, p, tab), r, p);
+        U[t] = c_scale(u, expf(-hdz * al));
+    }
+    __syncthreads();
+}

@@ -44,11 +44,36 @@ cudaError_t launch_phase_tables(nlse_ctx *c, double dz, cudaStream_t stream) {
     return cudaGetLastError();
 }
 
-// u[m, :] <- ifft( Pr[m] Pt * fft(u[m, :]) ), one CTA per row, in place.
+// With space-time focusing the diffraction phase depends on Omega through
+// U^-1 (operators.py:50), so it no longer separates: per dz the whole table
+//   P2[m, k] = exp(i (delta_k[k] - rho_m^2 invU[k] / (2 k0)) dz/2) spec_mask[k] Rk iRk / Nt
+// is built in FP64 and rounded once (8 Nr Nt bytes, allocated only then).
+__global__ void k_phase_table_2d(const double *__restrict__ delta_k, const double *__restrict__ spec_mask,
+                                 const double *__restrict__ rho_modes, const double *__restrict__ inv_U, int Nt,
+                                 int Nr, double dz, double komega, double scale, float2 *__restrict__ P2) {
+    const size_t n = (size_t)Nr * Nt;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const int m = (int)(i / Nt), k = (int)(i % Nt);
+        const double r = rho_modes[m];
+        double s, c;
+        sincos((delta_k[k] - r * r / (2.0 * komega) * inv_U[k]) * dz * 0.5, &s, &c);
+        const double a = spec_mask[k] * scale / (double)Nt;
+        P2[i] = make_float2((float)(c * a), (float)(s * a));
+    }
+}
+
+cudaError_t launch_phase_table_2d(nlse_ctx *c, double dz, cudaStream_t stream) {
+    k_phase_table_2d<<<4 * 152, 256, 0, stream>>>(c->d_delta_k, c->d_spec_mask, c->d_rho_modes, c->d_invUop, c->Nt,
+                                                   c->Nr, dz, c->komega, c->Rk_iRk, c->d_P2);
+    return cudaGetLastError();
+}
+
+// u[m, :] <- ifft( Pr[m] Pt * fft(u[m, :]) ), one CTA per row, in place
+// (P2 given: ifft( P2[m, :] * fft(u[m, :]) )).
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_fft_phase_ifft(float2 *__restrict__ u, const float2 *__restrict__ tw, const float2 *__restrict__ Pt,
-                 const float2 *__restrict__ Pr) {
+                 const float2 *__restrict__ Pr, const float2 *__restrict__ P2) {
     extern __shared__ float2 smem[];
     float2 *b0 = smem, *b1 = smem + fft_slots(NT);
     const size_t row = blockIdx.x;
@@ -56,32 +81,37 @@ k_fft_phase_ifft(float2 *__restrict__ u, const float2 *__restrict__ tw, const fl
     for (int i = threadIdx.x; i < NT; i += blockDim.x) b0[pidx(i)] = g[i];
     __syncthreads();
     float2 *s = fft_row<NT, false>(b0, b1, tw);
-    const float2 pr = Pr[row];
-    for (int i = threadIdx.x; i < NT; i += blockDim.x) s[pidx(i)] = c_mul(s[pidx(i)], c_mul(pr, __ldg(&Pt[i])));
+    if (P2) {
+        const float2 *q = P2 + row * (size_t)NT;
+        for (int i = threadIdx.x; i < NT; i += blockDim.x) s[pidx(i)] = c_mul(s[pidx(i)], __ldg(&q[i]));
+    } else {
+        const float2 pr = Pr[row];
+        for (int i = threadIdx.x; i < NT; i += blockDim.x) s[pidx(i)] = c_mul(s[pidx(i)], c_mul(pr, __ldg(&Pt[i])));
+    }
     __syncthreads();
     float2 *r = fft_row<NT, true>(s, s == b0 ? b1 : b0, tw);
     for (int i = threadIdx.x; i < NT; i += blockDim.x) g[i] = r[pidx(i)];
 }
 
 static cudaError_t fft_phase_ifft(float2 *u, int Nr, int logNt, const float2 *tw, const float2 *Pt,
-                                  const float2 *Pr, cudaStream_t stream) {
+                                  const float2 *Pr, const float2 *P2, cudaStream_t stream) {
     NLSE_DISPATCH_NT(logNt, {
         const size_t smem = 2 * (size_t)fft_slots(NT) * sizeof(float2);
         cudaError_t e = cudaFuncSetAttribute(k_fft_phase_ifft<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
-        k_fft_phase_ifft<NT><<<Nr, NLSE_ROW_THREADS, smem, stream>>>(u, tw, Pt, Pr);
+        k_fft_phase_ifft<NT><<<Nr, NLSE_ROW_THREADS, smem, stream>>>(u, tw, Pt, Pr, P2);
     });
     return cudaGetLastError();
 }
 
 cudaError_t launch_fft_phase_ifft(nlse_ctx *c, float2 *u, cudaStream_t stream) {
-    return fft_phase_ifft(u, c->Nr, c->logNt, c->d_tw, c->d_Pt, c->d_Pr, stream);
+    return fft_phase_ifft(u, c->Nr, c->logNt, c->d_tw, c->d_Pt, c->d_Pr, c->d_P2, stream);
 }
 
 // The same row kernel on caller-provided tables (used by the allocation-free entry point).
 cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, const float2 *tw, const float2 *Pt,
                                          const float2 *Pr, cudaStream_t stream) {
     (void)Nt;
-    return fft_phase_ifft(u, Nr, logNt, tw, Pt, Pr, stream);
+    return fft_phase_ifft(u, Nr, logNt, tw, Pt, Pr, nullptr, stream);
 }

@@ -17,7 +17,7 @@
 // scan in shared memory.
 #include <cuda_bf16.h>
 
-#include "nl_impl.cuh"
+#include "fullnl_impl.cuh"
 #include "scan_impl.cuh"
 
 
@@ -162,6 +162,28 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
     march_row<NT>(R, R == b0 ? b1 : b0, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), inv, r, a, rho);
 }
 
+// row_nl with the full-physics nonlinear block (Raman / self-steepening in
+// split(); three row buffers).
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+              const float *__restrict__ rho) {
+    extern __shared__ float2 sm2[];
+    const FullRows m = full_rows<NT>(sm2);
+    const int r = blockIdx.x;
+    load_mw_row<NT>(m.B0, r, a, F32, D, 1.0f / (float)NT);
+    __syncthreads();
+    const float2 *R = fft_row<NT, true>(m.B0, m.B1, a.tw);
+    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.U[t] = R[pidx(t)];
+    __syncthreads();
+    nl_block_full<NT>(m, rho + (size_t)r * NT, a.rho_s ? a.rho_s + (size_t)r * NT : nullptr, a.dz, a.nl, a.pchip,
+                      a.ft, a.tw);
+    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.B0[pidx(t)] = m.U[t];
+    __syncthreads();
+    float2 *Y = fft_row<NT, false>(m.B0, m.B1, a.tw);
+    store_state_row<NT>(Y, r, a, F32, Fb);
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb,
@@ -223,6 +245,17 @@ cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32,
         cudaError_t e = set_smem(k_row_entry<NT>, smem);
         if (e != cudaSuccess) return e;
         k_row_entry<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, u, F32, Fb, rho, do_scan);
+    });
+    return cudaGetLastError();
+}
+
+cudaError_t launch_row_nl_full(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
+                               const float *rho, cudaStream_t st) {
+    NLSE_DISPATCH_NT_FULL(a.logNt, {
+        const size_t smem = full_smem_bytes<NT>();
+        cudaError_t e = set_smem(k_row_nl_full<NT>, smem);
+        if (e != cudaSuccess) return e;
+        k_row_nl_full<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho);
     });
     return cudaGetLastError();
 }

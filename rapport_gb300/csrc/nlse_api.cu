@@ -59,7 +59,7 @@ static void free_ctx(nlse_ctx *c) {
     if (!c) return;
     prof_free(c);
     void *ptrs[] = {c->d_tw,    c->d_Y,   c->d_Y64, c->d_rho_modes, c->d_delta_k, c->d_spec_mask,
-                    c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_lut_s_dt, c->d_Pt,   c->d_Pr,     c->d_work,
+                    c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_lut_s_dt, c->d_Rf, c->d_Tss, c->d_invUnl, c->d_invUop, c->d_P2, c->d_Pt,   c->d_Pr,     c->d_work,
                     c->d_flag,  c->d_Er,  c->d_Ei,  c->d_A,  c->d_F32, c->d_Fb,  c->d_D,   c->d_Ptf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
@@ -96,13 +96,26 @@ static int check_desc(const nlse_grid_desc *d, nlse_error_slot *err) {
                        NLSE_MAX_NT);
         return NLSE_ERR_INVALID_ARG;
     }
-    const int unsupported = NLSE_F_KERR_RAMAN | NLSE_F_SELF_STEEP | NLSE_F_SPACE_TIME;
-    if (d->flags & unsupported) {
-        nlse_set_error(err, NLSE_ERR_UNSUPPORTED,
-                       "flags 0x%x request Raman / self-steepening / space-time focusing, "
-                       "which this library does not implement",
-                       d->flags & unsupported);
-        return NLSE_ERR_UNSUPPORTED;
+    const int full = NLSE_F_KERR_RAMAN | NLSE_F_SELF_STEEP | NLSE_F_SPACE_TIME;
+    if (d->flags & ~(full | NLSE_F_STE | 0xF)) {
+        nlse_set_error(err, NLSE_ERR_INVALID_ARG, "unknown flag bits 0x%x", d->flags & ~(full | NLSE_F_STE | 0xF));
+        return NLSE_ERR_INVALID_ARG;
+    }
+    if (d->flags & full) {
+        if (d->Nt > 4096) {
+            nlse_set_error(err, NLSE_ERR_UNSUPPORTED,
+                           "Raman / self-steepening / space-time focusing run the row transforms of split() in "
+                           "shared memory: Nt=%d > 4096",
+                           d->Nt);
+            return NLSE_ERR_UNSUPPORTED;
+        }
+        if (((d->flags & NLSE_F_KERR_RAMAN) && !d->R_f) || ((d->flags & NLSE_F_SELF_STEEP) && !d->T_op) ||
+            ((d->flags & NLSE_F_SPACE_TIME) && (!d->inv_U_nl || !d->inv_U_op)) || !(d->f_R >= 0 && d->f_R <= 1)) {
+            nlse_set_error(err, NLSE_ERR_INVALID_ARG,
+                           "a full-physics flag is set without its table (R_f / T_op / inv_U_nl, inv_U_op), "
+                           "or f_R is outside [0, 1]");
+            return NLSE_ERR_INVALID_ARG;
+        }
     }
     if (d->flags & NLSE_F_STE) {
         if (d->Nt > 4096) {
@@ -213,6 +226,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     sc.as_coef = ste ? (float)(d->beta_s * d->dt) : 0.0f;
     sc.cs_ste = ste ? (float)(d->dt * d->inv_tau_ste) : 0.0f;
     nl.ste_pref = ste ? (float)d->ste_pref : 0.0f;
+    nl.kp_raman = (d->flags & NLSE_F_KERR_RAMAN) ? (float)(d->kerr_pref * d->f_R) : 0.0f;
 
     nlse_error_slot *err = gerr;
     // twiddles exp(-2 pi i k / Nt), FP64 then rounded
@@ -277,6 +291,24 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
             }
             NLSE_TRY(dev_upload(err, &c->d_lut_s_dt, l.data(), d->lut_n));
         }
+    }
+    c->full_nl = (d->flags & (NLSE_F_KERR_RAMAN | NLSE_F_SELF_STEEP | NLSE_F_SPACE_TIME)) != 0;
+    if (d->flags & NLSE_F_KERR_RAMAN) {
+        std::vector<float2> rf(Nt);
+        for (int k = 0; k < Nt; ++k) rf[k] = make_float2((float)d->R_f[2 * k], (float)d->R_f[2 * k + 1]);
+        NLSE_TRY(dev_upload(err, &c->d_Rf, rf.data(), Nt));
+    }
+    if (d->flags & NLSE_F_SELF_STEEP) {
+        std::vector<float> t(Nt);
+        for (int k = 0; k < Nt; ++k) t[k] = (float)d->T_op[k];
+        NLSE_TRY(dev_upload(err, &c->d_Tss, t.data(), Nt));
+    }
+    if (d->flags & NLSE_F_SPACE_TIME) {
+        std::vector<float> t(Nt);
+        for (int k = 0; k < Nt; ++k) t[k] = (float)d->inv_U_nl[k];
+        NLSE_TRY(dev_upload(err, &c->d_invUnl, t.data(), Nt));
+        NLSE_TRY(dev_upload(err, &c->d_invUop, d->inv_U_op, Nt));
+        NLSE_TRY(dev_upload<float2>(err, &c->d_P2, nullptr, (size_t)Nr * Nt));
     }
     NLSE_TRY(dev_upload<float2>(err, &c->d_Pt, nullptr, Nt));
     NLSE_TRY(dev_upload<float2>(err, &c->d_Pr, nullptr, Nr));
@@ -438,6 +470,7 @@ static int ensure_tables(nlse_ctx *c, double dz, cudaStream_t st) {
     if (dz == c->cached_dz) return NLSE_OK;
     PROF(K_PHASE_TABLES);
     int s = launched(c, launch_phase_tables(c, dz, st), "phase tables");
+    if (s == NLSE_OK && c->d_P2) s = launched(c, launch_phase_table_2d(c, dz, st), "2-d phase table");
     if (s == NLSE_OK) c->cached_dz = dz;
     return s;
 }
@@ -469,6 +502,10 @@ static int split_ready(nlse_ctx *c, double dz, cudaStream_t st) {
     if (!c->split_ok)
         return bad(c, NLSE_ERR_UNSUPPORTED,
                    "split-BF16 mode needs Nr % 64 == 0 and Nt % 256 == 0 (this grid: use the plain mode)");
+    if (c->d_P2)
+        return bad(c, NLSE_ERR_UNSUPPORTED,
+                   "space-time focusing makes the diffraction phase depend on Omega, so the half step has no "
+                   "single radial operator for the split-BF16 product: use the plain mode");
     int s = ensure_tables(c, dz, st);
     if (s) return s;
     if (dz == c->cached_dz_op) return NLSE_OK;
@@ -498,6 +535,7 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
     a.dz = (float)dz;
     a.stats = c->d_flag;
     a.rho_s = nullptr;
+    a.ft = FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf};
     return a;
 }
 
@@ -556,6 +594,7 @@ static int row_entry(nlse_ctx *c, const RowFusedArgs &a, const float2 *u, float 
 
 static int row_nl(nlse_ctx *c, const RowFusedArgs &a, const float *rho, cudaStream_t st) {
     PROF(K_ROW_NL);
+    if (c->full_nl) return launched(c, launch_row_nl_full(a, c->d_F32, c->d_Fb, c->d_D, rho, st), "row nonlinear");
     return launched(c, launch_row_nl(a, c->d_F32, c->d_Fb, c->d_D, rho, st), "row nonlinear");
 }
 
@@ -660,12 +699,24 @@ static bool ste_ok(nlse_ctx *c, const float *rho_s) {
     return field_ok(c, rho_s, "rho_s");
 }
 
+// alpha/2 + RK4 + alpha/2 of the plain form: elementwise for the measured
+// toggles, the row-resident full-physics block otherwise.
+static cudaError_t nonlinear_block(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, float dz,
+                                   cudaStream_t st) {
+    if (c->full_nl) return launch_nl_full(c, u, rho, ste_density(c, rho_s), dz, st);
+    return launch_nonlinear_step(c, u, rho, ste_density(c, rho_s), dz, st);
+}
+
 extern "C" int nlse_split(nlse_ctx *c, const void *u, const float *rho, const float *rho_s, void *rhs, float *alpha,
                           void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !field_ok(c, rhs, "rhs")) return NLSE_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     PROF(K_SPLIT);
+    if (c->full_nl)
+        return launched(c, launch_split_full(c, (const float2 *)u, rho, ste_density(c, rho_s), (float2 *)rhs, alpha,
+                                             st),
+                        "split");
     return launched(c, launch_split(c, (const float2 *)u, rho, ste_density(c, rho_s), (float2 *)rhs, alpha, st),
                     "split");
 }
@@ -677,8 +728,7 @@ extern "C" int nlse_nonlinear_step(nlse_ctx *c, void *u, const float *rho, const
     if (!(dz > 0) || !isfinite(dz)) return bad(c, NLSE_ERR_INVALID_ARG, "dz must be positive and finite");
     cudaStream_t st = (cudaStream_t)stream;
     PROF(K_NONLINEAR);
-    return launched(c, launch_nonlinear_step(c, (float2 *)u, rho, ste_density(c, rho_s), (float)dz, st),
-                    "nonlinear step");
+    return launched(c, nonlinear_block(c, (float2 *)u, rho, rho_s, (float)dz, st), "nonlinear step");
 }
 
 extern "C" int nlse_update_plasma(nlse_ctx *c, const void *u, float *rho, float *rho_s, void *stream) {
@@ -700,7 +750,7 @@ static int step_plain(nlse_ctx *c, float2 *u, const float *rho, const float *rho
     if (s) return s;
     {
         PROF(K_NONLINEAR);
-        s = launched(c, launch_nonlinear_step(c, u, rho, ste_density(c, rho_s), (float)dz, st), "nonlinear step");
+        s = launched(c, nonlinear_block(c, u, rho, rho_s, (float)dz, st), "nonlinear step");
     }
     if (s) return s;
     return half_linear_impl(c, u, dz, c->d_mask_r, st);
@@ -913,8 +963,9 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
             BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: batches run the split-BF16 form, which needs Nr %% 64 == 0 "
                                              "and Nt %% 256 == 0",
                        i);
-        if (b->ctx[i]->sc.ste)
-            BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: the exciton channel runs on single contexts only", i);
+        if (b->ctx[i]->sc.ste || b->ctx[i]->full_nl)
+            BATCH_FAIL(NLSE_ERR_UNSUPPORTED,
+                       "pulse %d: the exciton channel and the full-physics split run on single contexts only", i);
     }
     std::vector<GemmTile> tiles;
     std::vector<CUtensorMap> maps(4 * (size_t)n);

@@ -44,6 +44,14 @@ struct NLParams {
     float tiny_I;       // 1e-30 * invE2 (the +1e-30 of the reference, in I units)
     int n_int;          // spline intervals
     float ste_pref;     // exciton index term: rhs += i ste_pref rho_s u
+    float kp_raman;     // kerr_pref * f_R (0 if Raman off)
+};
+
+// Tables of the full-physics split() (device, FFT order; NULL = that term off).
+struct FullTabs {
+    const float *T;       // T-hat(Omega) (self-steepening)
+    const float *invU;    // U^-1(Omega) of split() (space-time focusing)
+    const float2 *Rf;     // Raman response spectrum R_f
 };
 
 // Carrier-rate scan constants.
@@ -74,6 +82,7 @@ struct RowFusedArgs {
     float dz;
     int *stats;
     const float *rho_s;   // exciton density for the nonlinear step (NULL: channel off)
+    FullTabs ft;          // full-physics split tables (all NULL: the measured toggles)
 };
 
 // One pulse of a batch, as the batched kernels see it (device memory).
@@ -111,6 +120,13 @@ struct nlse_ctx {
     float4 *d_pchip;       // n_int scaled Hermite coefficients
     float *d_lut_dt;       // lut_n entries of W * dt
     float *d_lut_s_dt;     // lut_n entries of W(exciton gap) * dt
+    // full-physics split (allocated only for the terms the flags request)
+    int full_nl;           // Raman, self-steepening or space-time focusing on
+    float *d_Tss;          // Nt T-hat
+    float *d_invUnl;       // Nt U^-1 of split()
+    float2 *d_Rf;          // Nt Raman spectrum
+    double *d_invUop;      // Nt U^-1 of half_linear (space-time focusing)
+    float2 *d_P2;          // Nr x Nt phase of half_linear with space-time focusing (per dz)
     // per-dz tables (rebuilt on the stream when dz changes)
     double cached_dz;
     float2 *d_Pt;          // Nt  exp(i dk dz/2) mask Rk iRk / Nt
@@ -166,6 +182,13 @@ cudaError_t launch_nonlinear_step(nlse_ctx *c, float2 *u, const float *rho, cons
                                   cudaStream_t stream);
 cudaError_t launch_split(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, float2 *rhs,
                          float *alpha, cudaStream_t stream);
+cudaError_t launch_nl_full(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, float dz,
+                           cudaStream_t stream);
+cudaError_t launch_split_full(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, float2 *rhs,
+                              float *alpha, cudaStream_t stream);
+cudaError_t launch_row_nl_full(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
+                               const float *rho, cudaStream_t st);
+cudaError_t launch_phase_table_2d(nlse_ctx *c, double dz, cudaStream_t stream);
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s,
                              int zero_first, cudaStream_t stream);
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
@@ -332,4 +355,20 @@ __device__ __forceinline__ float2 *fft_row(float2 *buf0, float2 *buf1, const flo
         case 12: { constexpr int NT = 4096; __VA_ARGS__; break; } \
         case 13: { constexpr int NT = 8192; __VA_ARGS__; break; } \
         default: return cudaErrorInvalidValue;               \
+    }
+
+// The same for the full-physics kernels (N_t <= 4096: three row buffers and
+// the per-thread register arrays of the RK stages).
+#define NLSE_DISPATCH_NT_FULL(logn, ...)                          \
+    switch (logn) {                                               \
+        case 4: { constexpr int NT = 16; __VA_ARGS__; break; }    \
+        case 5: { constexpr int NT = 32; __VA_ARGS__; break; }    \
+        case 6: { constexpr int NT = 64; __VA_ARGS__; break; }    \
+        case 7: { constexpr int NT = 128; __VA_ARGS__; break; }   \
+        case 8: { constexpr int NT = 256; __VA_ARGS__; break; }   \
+        case 9: { constexpr int NT = 512; __VA_ARGS__; break; }   \
+        case 10: { constexpr int NT = 1024; __VA_ARGS__; break; } \
+        case 11: { constexpr int NT = 2048; __VA_ARGS__; break; } \
+        case 12: { constexpr int NT = 4096; __VA_ARGS__; break; } \
+        default: return cudaErrorInvalidValue;                    \
     }

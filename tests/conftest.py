@@ -34,6 +34,17 @@ def cfg1():
 
 
 @pytest.fixture(scope="session")
+def full():
+    return load_golden("tiny_full.npz")
+
+
+# every split() term on (tiny_full.npz): Raman with f_R 0.18, self-steepening,
+# space-time focusing, excitons with a 1 ps decay
+FULL_PHYSICS = dict(f_R=0.18, enable_kerr_raman=True, enable_self_steepening=True,
+                    enable_space_time_focusing=True, enable_ste=True, tau_ste=1e-12)
+
+
+@pytest.fixture(scope="session")
 def k1edge():
     return load_golden("k1_edge.npz")
 

@@ -55,9 +55,9 @@ class MPIPowerLaw:
 ref_grids.KeldyshSiO2 = MPIPowerLaw
 
 
-def make_config(Nr, Nt, R_max, w0, T_half, dz, nz, energy_uJ=1.0):
+def make_config(Nr, Nt, R_max, w0, T_half, dz, nz, energy_uJ=1.0, **over):
     out = tempfile.mkdtemp(prefix="golden_")
-    return ref_config.Config(
+    kw = dict(
         nz=nz, Nt=Nt, N=Nr + 1, begin=0.0, end=nz * dz,
         R_factor=R_max / w0, w0=w0, wavelength=800e-9,
         delta_t=T_half * np.sqrt(2 * np.log(2)) / 5.0, energy_uJ=energy_uJ,
@@ -65,6 +65,8 @@ def make_config(Nr, Nt, R_max, w0, T_half, dz, nz, energy_uJ=1.0):
         f_R=0.0, enable_kerr_raman=False, enable_self_steepening=False,
         enable_space_time_focusing=False, enable_ste=False,
         verbose=False, out_dir=out, rho_t_stride=0)
+    kw.update(over)
+    return ref_config.Config(**kw)
 
 
 def lens_envelope(fwhm, energy_uJ, w0, f, seed):
@@ -98,8 +100,8 @@ def grid_arrays(integ):
 
 
 def run_case(Nr, Nt, R_max, w0, T_half, fwhm, energy_uJ, f, dz, nsteps, seed, rows,
-             keep_steps, with_Y=True):
-    cfg = make_config(Nr, Nt, R_max, w0, T_half, dz, nsteps, energy_uJ)
+             keep_steps, with_Y=True, **over):
+    cfg = make_config(Nr, Nt, R_max, w0, T_half, dz, nsteps, energy_uJ, **over)
     integ = ref_integrator.Integrator(cfg, envelope=lens_envelope(fwhm, energy_uJ, w0, f, seed))
     out = grid_arrays(integ)
     u0 = integ.u.copy()
@@ -113,16 +115,21 @@ def run_case(Nr, Nt, R_max, w0, T_half, fwhm, energy_uJ, f, dz, nsteps, seed, ro
     # split on a field with plasma present: the half-linear output + rho of u0
     rhs, alpha = integ.nl.split(out_hl := integ.lin.half_linear(u0, dz), rho0, rs0)
     out["split_rhs"], out["split_alpha"] = rhs[rows], alpha[rows]
+    if over.get("enable_ste"):
+        out["rho_s_u0"] = rs0[rows]
     del out_hl
-    traj_u, traj_rho = [], []
+    traj_u, traj_rho, traj_rs = [], [], []
     for i in range(nsteps):
         integ.nl.update_plasma(integ.u, integ.rho, integ.rho_s, integ.dt,
                                integ.blocks, integ.threads)
         integ.step(integ.dz)
         traj_u.append(integ.u[rows].copy())
         traj_rho.append(integ.rho[rows].copy())
+        traj_rs.append(integ.rho_s[rows].copy())
     out["u_steps"] = np.stack([traj_u[i - 1] for i in keep_steps])
     out["rho_steps"] = np.stack([traj_rho[i - 1] for i in keep_steps])
+    if over.get("enable_ste"):
+        out["rho_s_steps"] = np.stack([traj_rs[i - 1] for i in keep_steps])
     out["steps_kept"] = np.asarray(keep_steps)
     if not with_Y:
         del out["Y"]
@@ -215,6 +222,14 @@ def main():
                   energy_uJ=1.0, f=0.1, dz=5e-6, nsteps=3, seed=0,
                   rows=list(range(0, 256, 8)), keep_steps=[1, 3], with_Y=False)
     np.savez_compressed(os.path.join(HERE, "config1_prefix.npz"), **c1)
+    # every split() term of the reference on: Raman (f_R 0.18), self-steepening,
+    # space-time focusing, the exciton channel (1 ps decay) -- the full-physics path
+    full = run_case(Nr=64, Nt=128, R_max=100e-6, w0=10e-6, T_half=300e-15, fwhm=100e-15,
+                    energy_uJ=2.0, f=1e-2, dz=5e-6, nsteps=4, seed=0, rows=list(range(64)),
+                    keep_steps=[1, 4], f_R=0.18, enable_kerr_raman=True, enable_self_steepening=True,
+                    enable_space_time_focusing=True, enable_ste=True, tau_ste=1e-12)
+    full["flags"] = np.array([0.18, 1, 1, 1, 1, 1e-12])
+    np.savez_compressed(os.path.join(HERE, "tiny_full.npz"), **full)
     np.savez_compressed(os.path.join(HERE, "k1_edge.npz"), **k1_edge_cases())
     np.savez_compressed(os.path.join(HERE, "record_tiny.npz"), **record_case())
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))

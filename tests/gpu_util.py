@@ -42,10 +42,10 @@ class Case:
         return cls(m["Nr"], m["Nt"], m["R_max"], m["w0"], m["T_half"], m["fwhm"], m["E"], m["f"], m["dz"],
                    m["nsteps"], m["seed"])
 
-    def oracle_nl_block(self, u, rho):
+    def oracle_nl_block(self, u, rho, rs=None):
         """alpha/2, RK4, alpha/2 of Integrator.step (integrator.py:140-147) in FP64."""
         og, dz = self.og, self.dz
-        rs = np.zeros_like(rho)
+        rs = np.zeros_like(rho) if rs is None else rs
         _, a = og.split(u, rho, rs)
         u = u * np.exp(-0.5 * dz * a)
         k1, _ = og.split(u, rho, rs)

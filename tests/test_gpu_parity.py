@@ -181,11 +181,3 @@ def test_bad_arguments_raise(tiny_case):
         c.ctx.half_linear(dev(c.u0), -1.0)
     with pytest.raises(NLSEError):
         c.ctx.step(dev(c.u0), dev(np.zeros(c.u0.shape)), c.dz, mode=7)
-
-
-def test_unsupported_physics_rejected():
-    import rapport_gb300 as R
-    from rapport_gb300._lib import NLSEError
-    cfg = R.workload_config(16, 64, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_kerr_raman=True, f_R=0.18)
-    with pytest.raises(NLSEError, match="Raman"):
-        R.LinearOperator(cfg, R.build_grids(cfg))

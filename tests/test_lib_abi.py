@@ -43,8 +43,12 @@ def test_create_error_path_without_device_or_with_bad_desc():
     buf = ctypes.create_string_buffer(256)
     assert lib.nlse_get_last_error(None, buf, 256) == _lib.NLSE_ERR_INVALID_ARG
     assert b"power of two" in buf.value
-    d.Nt, d.flags = 64, _lib.F_KERR_RAMAN
+    d.Nt, d.flags = 64, _lib.F_KERR_RAMAN      # Raman without its R_f table
+    assert lib.nlse_create(ctypes.byref(d), ctypes.byref(h)) == _lib.NLSE_ERR_INVALID_ARG
+    d.Nt, d.flags = 8192, _lib.F_SELF_STEEP    # the full-physics block holds N_t <= 4096
     assert lib.nlse_create(ctypes.byref(d), ctypes.byref(h)) == _lib.NLSE_ERR_UNSUPPORTED
+    d.Nt, d.flags = 64, 1 << 12                 # unknown flag bit
+    assert lib.nlse_create(ctypes.byref(d), ctypes.byref(h)) == _lib.NLSE_ERR_INVALID_ARG
     assert lib.nlse_half_linear(None, None, 1.0, None) == _lib.NLSE_ERR_INVALID_ARG
 
 

@@ -102,3 +102,32 @@ def test_oracle_rate_scan_matches_compiled_reference_kernel():
         O.rate_scan(E, ne_o, ns_o, *args, ste, lut, lut * 0.5, 0.0, 4095 / 17.0, 1.0, 9.99e16)
         np.testing.assert_array_equal(ne_o, ne_r)
         np.testing.assert_array_equal(ns_o, ns_r)
+
+
+def test_full_physics_matches_reference(full):
+    """Raman, self-steepening, space-time focusing and excitons all on: the
+    oracle's half_linear (Omega-dependent diffraction), split and carrier march
+    reproduce the reference's, and so do 4 whole z-steps."""
+    from conftest import FULL_PHYSICS
+    m = meta_case(full)
+    g = O.OracleGrid(O.workload_config(m["Nr"], m["Nt"], m["R_max"], m["w0"], m["T_half"], **FULL_PHYSICS))
+    u0 = O.lens_gaussian(g, m["w0"], m["fwhm"], m["E"], m["f"], m["seed"])
+    assert rel_l2(u0, full["u0"]) < 1e-14
+    assert rel_l2(g.half_linear(u0, m["dz"]), full["hl_u0"]) < 1e-12
+    rho, rs = np.zeros(u0.shape), np.zeros(u0.shape)
+    g.update_plasma(u0, rho, rs)
+    assert rel_l2(rho, full["rho_u0"]) < 1e-12
+    assert rs.max() > 0 and rel_l2(rs, full["rho_s_u0"]) < 1e-12
+    rhs, al = g.split(g.half_linear(u0, m["dz"]), rho, rs)
+    assert rel_l2(rhs, full["split_rhs"]) < 1e-12
+    assert rel_l2(al, full["split_alpha"]) < 1e-12
+    u, rho, rs = u0, np.zeros(u0.shape), np.zeros(u0.shape)
+    kept = list(full["steps_kept"])
+    for i in range(1, max(kept) + 1):
+        g.update_plasma(u, rho, rs)
+        u = g.step(u, rho, rs, m["dz"])
+        if i in kept:
+            j = kept.index(i)
+            assert rel_l2(u, full["u_steps"][j]) < 1e-12, i
+            assert rel_l2(rho, full["rho_steps"][j]) < 1e-12, i
+            assert rel_l2(rs, full["rho_s_steps"][j]) < 1e-12, i
