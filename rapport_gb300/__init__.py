@@ -10,7 +10,9 @@ from .grids import ENVELOPES, build_grids, envelope_gaussian_focused, envelope_l
 from .operators import LinearOperator, NonlinearOperator
 from .integrator import Integrator
 from .filament_sim import FIELD_TOGGLES, run
+from .sweeps import build_scenarios, energy_scenarios, load_scenario_npz, run_scenarios, summarize
 
 __all__ = ["Config", "n_sellmeier", "workload_config", "build_grids", "envelope_gaussian_focused",
            "envelope_lens", "ENVELOPES", "keldysh_rate", "LinearOperator", "NonlinearOperator",
-           "Integrator", "run", "FIELD_TOGGLES"]
+           "Integrator", "run", "FIELD_TOGGLES", "build_scenarios", "energy_scenarios", "load_scenario_npz",
+           "run_scenarios", "summarize"]

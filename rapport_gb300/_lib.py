@@ -389,16 +389,6 @@ class Batch:
             self.lib.nlse_batch_get_last_error(self.h, buf, 512)
             raise NLSEError(status, buf.value.decode(errors="replace"))
 
-    def record(self, u, rho, rho_s, bin_of_t, nbins, out):
-        """Per-radius plane diagnostics into out (float64 CUDA tensor, Nr x (6 + nbins))."""
-        import torch
-        if out.dtype != torch.float64 or tuple(out.shape) != (self.Nr, 6 + nbins) or not out.is_contiguous():
-            raise ValueError("out must be a contiguous float64 CUDA tensor of shape (Nr, 6 + nbins)")
-        rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
-        b = ctypes.c_void_p(bin_of_t.data_ptr()) if bin_of_t is not None else None
-        _check(self.lib, self.h, self.lib.nlse_record(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs, b,
-                                                      int(nbins), ctypes.c_void_p(out.data_ptr()), self._stream()))
-
     def set_split_terms(self, n):
         _check(self.lib, None, self.lib.nlse_batch_set_split_terms(self.h, int(n)))
 
@@ -407,11 +397,20 @@ class Batch:
         self.lib.nlse_batch_device_status(self.h, ctypes.byref(w))
         return w.value
 
+    def context(self, i):
+        """Pulse i's context (owned by the batch: valid while the batch lives).
+        Its single-pulse operations (record, update_plasma, ...) act on that
+        pulse's grid and tables."""
+        if not 0 <= i < self.n:
+            raise IndexError(i)
+        c = _P()
+        _check(self.lib, None, self.lib.nlse_batch_get_context(self.h, int(i), ctypes.byref(c)))
+        ctx = Context.__new__(Context)
+        ctx.lib, ctx.h, ctx.Nr, ctx.Nt = self.lib, c, self.shapes[i][0], self.shapes[i][1]
+        ctx._borrowed = True
+        ctx._owner = self
+        return ctx
+
     def context_profile(self):
         """The first pulse's context (the batch records its launches there)."""
-        c = _P()
-        _check(self.lib, None, self.lib.nlse_batch_get_context(self.h, 0, ctypes.byref(c)))
-        ctx = Context.__new__(Context)
-        ctx.lib, ctx.h, ctx.Nr, ctx.Nt = self.lib, c, self.shapes[0][0], self.shapes[0][1]
-        ctx._borrowed = True
-        return ctx
+        return self.context(0)

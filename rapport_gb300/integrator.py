@@ -40,14 +40,16 @@ def code_fingerprint():
 
 
 class Integrator:
-    def __init__(self, cfg: Config, envelope="gaussian_focused", device=None):
+    def __init__(self, cfg: Config, envelope="gaussian_focused", device=None, ctx=None, g=None):
+        """ctx / g: an existing context for this grid (e.g. a batch pulse's)
+        and its build_grids() dict; built here when not given."""
         self.cfg = cfg
         if device is not None:
             torch.cuda.set_device(device)
-        g = build_grids(cfg)
+        g = build_grids(cfg) if g is None else g
         self.g = g
         self.dz, self.dt = cfg.dz, g["dt"]
-        self.ctx = Context(cfg, g)
+        self.ctx = Context(cfg, g) if ctx is None else ctx
         self.lin = LinearOperator(cfg, g, self.ctx)
         self.nl = NonlinearOperator(cfg, g, self.ctx)
         self.mode = _MODES[cfg.linear_mode]
@@ -130,24 +132,36 @@ class Integrator:
         """nsteps iterations of update_plasma + step, queued without host syncs."""
         self.ctx.propagate(self.u, self.rho, self.rho_s, self.dz, nsteps, self.mode)
 
-    def propagate(self):
+    def chunks(self):
+        """The z loop of Integrator.propagate (integrator.py:151-177) as
+        (n, z_record, i) chunks: advance n iterations, then record the plane
+        at z_record (None: no record); i = the last iteration's index.  The
+        reference records after iterations 0, stride, 2 stride, ..."""
         cfg = self.cfg
         total, stride = cfg.nz + 1, max(1, int(cfg.save_stride))
         done = 0
         while done < total:
-            # the reference records after iterations 0, stride, 2 stride, ...
             n = 1 if done == 0 else min(stride, total - done)
-            self.advance(n)
             done += n
             i = done - 1
-            if i % stride == 0:
-                self._record(cfg.begin + i * self.dz)
-            if cfg.verbose and i > 0 and i % cfg.ckpt_every == 0 and self.k_save:
-                k = self.k_save - 1
-                flu = self.fluence_rz[k].double().cpu().numpy()
-                pct = float(np.sum(flu * self._ring)) * 100.0 / self.U0_uJ * 100.0
-                print(f"[z] {(cfg.begin + i * self.dz) * 1e6:+.0f} um  U {pct:.1f} %  "
-                      f"I_peak {self.Imax_z[k]:.2e}", flush=True)
+            yield n, (cfg.begin + i * self.dz if i % stride == 0 else None), i
+
+    def after_chunk(self, z_record, i):
+        """Record (and report) after a chunk of chunks()."""
+        cfg = self.cfg
+        if z_record is not None:
+            self._record(z_record)
+        if cfg.verbose and i > 0 and i % cfg.ckpt_every == 0 and self.k_save:
+            k = self.k_save - 1
+            flu = self.fluence_rz[k].double().cpu().numpy()
+            pct = float(np.sum(flu * self._ring)) * 100.0 / self.U0_uJ * 100.0
+            print(f"[z] {(cfg.begin + i * self.dz) * 1e6:+.0f} um  U {pct:.1f} %  "
+                  f"I_peak {self.Imax_z[k]:.2e}", flush=True)
+
+    def propagate(self):
+        for n, z_rec, i in self.chunks():
+            self.advance(n)
+            self.after_chunk(z_rec, i)
         return self._results()
 
     # ------------------------------------------------------------------ recording
