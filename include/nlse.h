@@ -33,6 +33,8 @@
  *   nlse_step             Integrator.step                (integrator.py:138-149)
  *   nlse_propagate        the z loop of Integrator.propagate: nsteps x
  *                         (update_plasma, step)           (integrator.py:156-158)
+ *   nlse_step_batched     that loop for several pulses on one grid (the
+ *                         notebooks' sweeps over run(); filament_sim.py:59-106)
  *   nlse_destroy          (context teardown; the reference frees by GC)
  */
 #ifndef NLSE_H
@@ -170,6 +172,22 @@ int nlse_step(nlse_ctx *ctx, void *u, const float *rho, const float *rho_s,
  * the field entering that step), exactly as after the reference loop. */
 int nlse_propagate(nlse_ctx *ctx, void *u, float *rho, float *rho_s, double dz,
                    int nsteps, int mode, void *stream);
+
+/* Pulses that share this context's grid and physics (e.g. an energy sweep):
+ * for each pulse, nsteps iterations of (update_plasma, step) in its mode, all
+ * queued on the stream in order (the context's tables and operator are shared;
+ * the pulses run one after another).  For pulses on different grids, or one
+ * grouped launch per kernel across pulses, use the nlse_batch_* entry points. */
+typedef struct nlse_pulse_desc {
+    void *u;          /* complex64 Nr x Nt */
+    float *rho;       /* float32 Nr x Nt */
+    float *rho_s;     /* float32 Nr x Nt, or NULL (required with NLSE_F_STE) */
+    double dz;
+    int nsteps;
+    int mode;         /* NLSE_MODE_* */
+} nlse_pulse_desc;
+
+int nlse_step_batched(nlse_ctx *ctx, const nlse_pulse_desc *pulses, int n, void *stream);
 
 /* Diagnostic: out = E' w for a planar FP32 field w (2Nr x Nt: Re rows then
  * Im rows) through the tcgen05 product alone, E' = [[Re E, -Im E], [Im E, Re E]]

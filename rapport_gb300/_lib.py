@@ -19,7 +19,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
 
 # every symbol include/nlse.h declares (checked by the CPU test suite)
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
-           "nlse_update_plasma", "nlse_rate_equation", "nlse_step", "nlse_propagate", "nlse_set_split_terms",
+           "nlse_update_plasma", "nlse_rate_equation", "nlse_step", "nlse_step_batched", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
            "nlse_half_linear_noalloc", "nlse_record", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
            "nlse_batch_set_split_terms", "nlse_batch_device_status", "nlse_batch_get_last_error",
@@ -48,6 +48,11 @@ class GridDesc(ctypes.Structure):
     ]
 
 
+class PulseDesc(ctypes.Structure):
+    """Mirror of nlse_pulse_desc."""
+    _fields_ = [("u", _P), ("rho", _P), ("rho_s", _P), ("dz", _D), ("nsteps", _I), ("mode", _I)]
+
+
 _lib = None
 
 
@@ -72,6 +77,7 @@ def load():
     lib.nlse_rate_equation.argtypes = [_P, _P, _P, _P, _P]
     lib.nlse_step.argtypes = [_P, _P, _P, _P, _D, _I, _P]
     lib.nlse_propagate.argtypes = [_P, _P, _P, _P, _D, _I, _I, _P]
+    lib.nlse_step_batched.argtypes = [_P, ctypes.POINTER(PulseDesc), _I, _P]
     lib.nlse_scan_fallback_rows.argtypes = [_P, ctypes.POINTER(_I)]
     lib.nlse_get_last_error.argtypes = [_P, ctypes.c_char_p, ctypes.c_size_t]
     lib.nlse_destroy.argtypes = [_P]
@@ -308,6 +314,17 @@ class Context:
         rs = self._rho(rho_s, "rho_s") if rho_s is not None else None
         _check(self.lib, self.h, self.lib.nlse_propagate(self.h, self._field(u, "u"), self._rho(rho, "rho"), rs,
                                                          float(dz), int(nsteps), int(mode), self._stream()))
+
+    def step_batched(self, pulses, dz, nsteps, mode=MODE_PLAIN_F32):
+        """pulses: [(u, rho, rho_s or None)] on this context's grid; each advances
+        nsteps iterations of update_plasma + step."""
+        arr = (PulseDesc * len(pulses))()
+        for i, (u, rho, rs) in enumerate(pulses):
+            arr[i].u = self._field(u, "u")
+            arr[i].rho = self._rho(rho, "rho")
+            arr[i].rho_s = self._rho(rs, "rho_s") if rs is not None else None
+            arr[i].dz, arr[i].nsteps, arr[i].mode = float(dz), int(nsteps), int(mode)
+        _check(self.lib, self.h, self.lib.nlse_step_batched(self.h, arr, len(pulses), self._stream()))
 
     def profile_start(self, capacity):
         _check(self.lib, self.h, self.lib.nlse_profile_start(self.h, int(capacity)))

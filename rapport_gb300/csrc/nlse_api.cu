@@ -781,6 +781,21 @@ extern "C" int nlse_propagate(nlse_ctx *c, void *u, float *rho, float *rho_s, do
     return NLSE_OK;
 }
 
+extern "C" int nlse_step_batched(nlse_ctx *c, const nlse_pulse_desc *p, int n, void *stream) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    if (n < 0 || (n > 0 && !p)) return bad(c, NLSE_ERR_INVALID_ARG, "pulses NULL or n < 0");
+    for (int i = 0; i < n; ++i) {
+        int s = nlse_propagate(c, p[i].u, p[i].rho, p[i].rho_s, p[i].dz, p[i].nsteps, p[i].mode, stream);
+        if (s) {
+            char msg[400];
+            snprintf(msg, sizeof(msg), "%s", c->err.msg);
+            nlse_set_error(&c->err, s, "pulse %d: %s", i, msg);
+            return s;
+        }
+    }
+    return NLSE_OK;
+}
+
 extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *out, double dz, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, w, "w") || !field_ok(c, out, "out")) return NLSE_ERR_INVALID_ARG;

@@ -95,3 +95,24 @@ def test_batch_shared_operator_pulses_match_single_contexts():
         ctx.propagate(u, rho, rs, DZ, STEPS, _lib.MODE_SPLIT_BF16)
         assert np.array_equal(host(us[i]), host(u)), i
         assert np.array_equal(host(rhos[i]), host(rho)), i
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_step_batched_equals_propagate_per_pulse(mode):
+    """nlse_step_batched: pulses on one context's grid, each exactly as its own nlse_propagate."""
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, DZ, STEPS)
+    g = R.build_grids(cfg)
+    u0s = [R.envelope_lens(1e-5, 100e-15, 1.0 + i, 1e-2, i)(g["rr"], g["tt"], cfg, g) for i in range(3)]
+    ctx = _lib.Context(cfg, g)
+    bu = [dev(u) for u in u0s]
+    br = [dev(np.zeros(u.shape)) for u in u0s]
+    ctx.step_batched([(u, r, None) for u, r in zip(bu, br)], DZ, STEPS, mode)
+    for i, u0 in enumerate(u0s):
+        u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+        ctx.propagate(u, rho, rs, DZ, STEPS, mode)
+        assert np.array_equal(host(bu[i]), host(u)), i
+        assert np.array_equal(host(br[i]), host(rho)), i
+    with pytest.raises(_lib.NLSEError, match="pulse 1"):
+        ctx.step_batched([(bu[0], br[0], None), (bu[1], br[1], None)], -1.0, 1, mode)
