@@ -114,5 +114,5 @@ def test_step_batched_equals_propagate_per_pulse(mode):
         ctx.propagate(u, rho, rs, DZ, STEPS, mode)
         assert np.array_equal(host(bu[i]), host(u)), i
         assert np.array_equal(host(br[i]), host(rho)), i
-    with pytest.raises(_lib.NLSEError, match="pulse 1"):
+    with pytest.raises(_lib.NLSEError, match="pulse 0: dz"):
         ctx.step_batched([(bu[0], br[0], None), (bu[1], br[1], None)], -1.0, 1, mode)
