@@ -214,9 +214,11 @@ int nlse_batch_get_last_error(const nlse_batch *b, char *buf, size_t len);
 void nlse_batch_destroy(nlse_batch *b);
 
 /* Tensor-core pipeline of the split mode: 0 = 64-deep k slices x 2 stages,
- * 1 = 32-deep x 4 stages, -1 = autotune (default: the first split-mode call
- * times both on the live operands and keeps the faster; that call
- * synchronises its stream, so make it before any stream capture). */
+ * 1 = 32-deep x 4 stages, 2 = 32-deep x 3 stages, 3 = 32-deep x 2 stages
+ * (2 and 3 leave shared memory for other kernels' blocks on the same SM),
+ * -1 = autotune (default: the first split-mode call times 0 and 1 on the
+ * live operands and keeps the faster; that call synchronises its stream, so
+ * make it before any stream capture).  A batch uses its first pulse's. */
 int nlse_set_gemm_variant(nlse_ctx *ctx, int variant);
 int nlse_get_gemm_variant(const nlse_ctx *ctx);
 

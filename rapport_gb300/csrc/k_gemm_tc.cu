@@ -294,12 +294,17 @@ static size_t tc_smem_bytes(int a_terms, int bk, int stages) {
     return (size_t)stages * (a_terms * TC_BM * bk * 2 + 2 * bk * TC_BN * 2) + 1024;
 }
 
-// variant: 0 = (BK 64, 2 stages), 1 = (BK 32, 4 stages)
-#define TC_DISPATCH(a_terms, variant, ...)                                                     \
-    if (a_terms == 3 && variant == 0) { constexpr int AT = 3, BK = 64, ST = 2; __VA_ARGS__; } \
-    else if (a_terms == 3) { constexpr int AT = 3, BK = 32, ST = 4; __VA_ARGS__; }            \
-    else if (variant == 0) { constexpr int AT = 2, BK = 64, ST = 2; __VA_ARGS__; }            \
-    else { constexpr int AT = 2, BK = 32, ST = 4; __VA_ARGS__; }
+// variant: 0 = (BK 64, 2 stages), 1 = (BK 32, 4 stages), 2 = (BK 32, 3 stages),
+// 3 = (BK 32, 2 stages).  2 and 3 leave shared memory for a row-kernel CTA
+// on the same SM (169 KB / 116 KB of the 228 KB).
+#define TC_DISPATCH_AT(AT_, variant, ...)                                                   \
+    if (variant == 0) { constexpr int AT = AT_, BK = 64, ST = 2; __VA_ARGS__; }            \
+    else if (variant == 1) { constexpr int AT = AT_, BK = 32, ST = 4; __VA_ARGS__; }       \
+    else if (variant == 2) { constexpr int AT = AT_, BK = 32, ST = 3; __VA_ARGS__; }       \
+    else { constexpr int AT = AT_, BK = 32, ST = 2; __VA_ARGS__; }
+#define TC_DISPATCH(a_terms, variant, ...)                                                  \
+    if (a_terms == 3) { TC_DISPATCH_AT(3, variant, __VA_ARGS__) }                           \
+    else { TC_DISPATCH_AT(2, variant, __VA_ARGS__) }
 
 cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
                                    int a_terms, int variant, int *err, cudaStream_t stream) {

@@ -819,7 +819,7 @@ extern "C" int nlse_record(nlse_ctx *c, const void *u, const float *rho, const f
 
 extern "C" int nlse_set_gemm_variant(nlse_ctx *c, int variant) {
     if (!c) return NLSE_ERR_INVALID_ARG;
-    if (variant < -1 || variant > 1) return bad(c, NLSE_ERR_INVALID_ARG, "variant must be -1 (autotune), 0 or 1");
+    if (variant < -1 || variant > 3) return bad(c, NLSE_ERR_INVALID_ARG, "variant must be -1 (autotune) or 0..3");
     c->gemm_variant = variant < 0 ? 0 : variant;
     c->tuned = variant >= 0;
     return NLSE_OK;
