@@ -65,17 +65,17 @@ template <int NT>
 __device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float inv, int r, const RowFusedArgs &a,
                                           float *rho) {
     constexpr int S = scan_span(NT, NLSE_ROW_THREADS);
-    constexpr int C = (NT - 1 + NLSE_ROW_THREADS - 1) / NLSE_ROW_THREADS;
+    const ScanLayout L = scan_layout(NT);
     float *sI = reinterpret_cast<float *>(O), *sW = sI + S;
     for (int t = threadIdx.x; t < NT; t += blockDim.x) {
         const float2 v = c_scale(R[pidx(t)], inv);
-        sI[scan_slot(t, C)] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
+        sI[scan_slot(t, L)] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
     }
     __syncthreads();
     float *sx = reinterpret_cast<float *>(R), *sJ = sx + S;
     scan_row(sI, sW, sx, sJ, X, NT, a.sc, a.lut, 0.0f, a.stats);
     float *gr = rho + (size_t)r * NT;
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[scan_slot(t, C)];
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[scan_slot(t, L)];
 }
 
 // 2 padded complex row buffers (+ one float scan array, scan_span(NT) long, for the march).
@@ -199,7 +199,7 @@ k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
 k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
            float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask) {
     row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask);
@@ -224,7 +224,7 @@ k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work) {
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
 k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];

@@ -32,7 +32,8 @@ k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__rest
     extern __shared__ float sm[];
     if (p.ste) {
         // two populations: sI sW sWs se ss + J (4) + B (2) arrays
-        const int S = scan_span(Nt, blockDim.x), C = (Nt - 1 + blockDim.x - 1) / blockDim.x;
+        const int S = scan_span(Nt, blockDim.x);
+        const ScanLayout L = scan_layout(Nt);
         const size_t row = blockIdx.x;
         const float2 *g = u + row * (size_t)Nt;
         float *ge = rho + row * (size_t)Nt, *gs = rho_s + row * (size_t)Nt;
@@ -46,7 +47,7 @@ k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__rest
         float *sI = sm;
         for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
             float2 v = g[t];
-            sI[scan_slot(t, C)] = fmaf(v.x, v.x, v.y * v.y) * p.invE2;
+            sI[scan_slot(t, L)] = fmaf(v.x, v.x, v.y * v.y) * p.invE2;
         }
         __syncthreads();
         float *jm[4] = {sm + 5 * S, sm + 6 * S, sm + 7 * S, sm + 8 * S};
@@ -54,13 +55,14 @@ k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__rest
         scan_row2(sI, sm + S, sm + 2 * S, sm + 3 * S, sm + 4 * S, jm, jb, Nt, p, lut, lut_s, x0e, x0s, stats);
         for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
             if (t == 0 && !zero_first) continue;
-            const int q = scan_slot(t, C);
+            const int q = scan_slot(t, L);
             ge[t] = t == 0 ? 0.0f : sm[3 * S + q];
             gs[t] = t == 0 ? 0.0f : sm[4 * S + q];
         }
         return;
     }
-    const int S = scan_span(Nt, blockDim.x), C = (Nt - 1 + blockDim.x - 1) / blockDim.x;
+    const int S = scan_span(Nt, blockDim.x);
+    const ScanLayout L = scan_layout(Nt);
     float *sI = sm;
     const size_t row = blockIdx.x;
     const float2 *g = u + row * (size_t)Nt;
@@ -72,13 +74,13 @@ k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__rest
     }
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
         float2 v = g[t];
-        sI[scan_slot(t, C)] = fmaf(v.x, v.x, v.y * v.y) * p.invE2;
+        sI[scan_slot(t, L)] = fmaf(v.x, v.x, v.y * v.y) * p.invE2;
     }
     __syncthreads();
     float *sx = sm + 2 * S;
     scan_row(sI, sm + S, sx, sm + 3 * S, sm + 4 * S, Nt, p, lut, x0, stats);
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
-        if (t > 0 || zero_first) grho[t] = t == 0 ? 0.0f : sx[scan_slot(t, C)];
+        if (t > 0 || zero_first) grho[t] = t == 0 ? 0.0f : sx[scan_slot(t, L)];
         if (rho_s && (t > 0 || zero_first)) rho_s[row * (size_t)Nt + t] = 0.0f;
     }
 }

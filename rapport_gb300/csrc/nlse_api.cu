@@ -229,14 +229,21 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     nl.kp_raman = (d->flags & NLSE_F_KERR_RAMAN) ? (float)(d->kerr_pref * d->f_R) : 0.0f;
 
     nlse_error_slot *err = gerr;
-    // twiddles exp(-2 pi i k / Nt), FP64 then rounded
+    // twiddles exp(-2 pi i m / Nt) in the per-pass row layout, FP64 then rounded
     {
-        std::vector<float2> tw(Nt);
-        for (int k = 0; k < Nt; ++k) {
-            double a = -2.0 * M_PI * (double)k / (double)Nt;
-            tw[k] = make_float2((float)cos(a), (float)sin(a));
+        const int n = fft_tw_size(Nt);
+        std::vector<float2> tw(n > 0 ? n : 1);
+        for (int e = 0; e < n; ++e) {
+            int m;
+            fft_tw_entry(Nt, e, &m);
+            if (m < 0) {
+                tw[e] = make_float2(0.0f, 0.0f);
+                continue;
+            }
+            double a = -2.0 * M_PI * (double)m / (double)Nt;
+            tw[e] = make_float2((float)cos(a), (float)sin(a));
         }
-        NLSE_TRY(dev_upload(err, &c->d_tw, tw.data(), Nt));
+        NLSE_TRY(dev_upload(err, &c->d_tw, tw.data(), tw.size()));
     }
     {
         std::vector<float> Yf((size_t)Nr * Nr);

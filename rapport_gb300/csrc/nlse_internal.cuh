@@ -286,14 +286,36 @@ __device__ __forceinline__ void dft_small(float2 *v) {
 __host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 4); }
 __host__ __device__ __forceinline__ constexpr int fft_slots(int n) { return n + (n >> 4); }
 
+// Radix of the Stockham pass at NS (the product of the radices applied so far)
+// for an N-point row: 8 while it divides what remains, then 4 or 2.
+__host__ __device__ constexpr int fft_radix(int N, int NS) {
+    return (N / NS) % 8 == 0 ? 8 : ((N / NS) % 4 == 0 ? 4 : 2);
+}
+
+// Twiddle table layout: the pass at NS > 1 owns NS rows of fft_tw_row(R)
+// float2, row k = exp(-2 pi i r k (N / (NS R)) / N) for r = 1 .. R-1, padded
+// to an even count so a butterfly reads its twiddles with R/2 16-byte loads
+// from one contiguous row (the values are those of a plain exp(-2 pi i m / N)
+// table; only the order differs).
+__host__ __device__ constexpr int fft_tw_row(int R) { return R == 2 ? 2 : R; }
+
+__host__ __device__ constexpr int fft_tw_offset(int N, int NS) {
+    int off = 0;
+    for (int s = 1; s < NS; s *= fft_radix(N, s))
+        if (s > 1) off += s * fft_tw_row(fft_radix(N, s));
+    return off;
+}
+
+// float2 entries of the whole table of an N-point row.
+__host__ __device__ constexpr int fft_tw_size(int N) { return fft_tw_offset(N, N); }
+
 // One Stockham autosort pass of radix R over a row of N points (compile-time
 // sizes): reads src, writes dst (padded indexing).  NS = product of the
-// radices already applied; tw = forward twiddles exp(-2 pi i k / N).
+// radices already applied; tw = the twiddle table above.
 template <int R, bool INV, int N, int NS, int T>
 __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                               const float2 *__restrict__ tw) {
     constexpr int nb = N / R;
-    constexpr int tstride = N / (NS * R);
 #pragma unroll
     for (int jj = 0; jj < (nb + T - 1) / T; ++jj) {
         const int j = (int)threadIdx.x + jj * T;
@@ -303,11 +325,20 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = src[pidx(j + r * nb)];
             if (NS > 1) {
+                const float4 *w4 =
+                    reinterpret_cast<const float4 *>(tw + fft_tw_offset(N, NS) + k * fft_tw_row(R));
+                float2 w[fft_tw_row(R)];
+#pragma unroll
+                for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
+                    const float4 p = __ldg(&w4[q]);
+                    w[2 * q] = make_float2(p.x, p.y);
+                    w[2 * q + 1] = make_float2(p.z, p.w);
+                }
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
-                    float2 w = __ldg(&tw[r * k * tstride]);
-                    if (INV) w.y = -w.y;
-                    v[r] = c_mul(v[r], w);
+                    float2 x = w[r - 1];
+                    if (INV) x.y = -x.y;
+                    v[r] = c_mul(v[r], x);
                 }
             }
             dft_small<R, INV>(v);
@@ -318,14 +349,13 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
     }
 }
 
-// Remaining passes from NS on; radix 8 while it divides, then 4 or 2.
+// Remaining passes from NS on.
 template <int N, int NS, bool INV, int T>
 __device__ __forceinline__ float2 *fft_passes(float2 *src, float2 *dst, const float2 *__restrict__ tw) {
     if constexpr (NS >= N) {
         return src;
     } else {
-        constexpr int REM = N / NS;
-        constexpr int R = (REM % 8 == 0) ? 8 : ((REM % 4 == 0) ? 4 : 2);
+        constexpr int R = fft_radix(N, NS);
         stockham_pass<R, INV, N, NS, T>(src, dst, tw);
         __syncthreads();
         return fft_passes<N, NS * R, INV, T>(dst, src, tw);
@@ -338,6 +368,23 @@ __device__ __forceinline__ float2 *fft_passes(float2 *src, float2 *dst, const fl
 template <int N, bool INV, int T = NLSE_ROW_THREADS>
 __device__ __forceinline__ float2 *fft_row(float2 *buf0, float2 *buf1, const float2 *__restrict__ tw) {
     return fft_passes<N, 1, INV, T>(buf0, buf1, tw);
+}
+
+// Entry e of the twiddle table of an N-point row (host or device, FP64 then
+// rounded): the pass, row k and r it stands for give m = r k N / (NS R).
+__host__ __device__ inline void fft_tw_entry(int N, int e, int *m_out) {
+    int off = 0, m = -1;
+    for (int NS = 1; NS < N; NS *= fft_radix(N, NS)) {
+        if (NS == 1) continue;
+        const int R = fft_radix(N, NS), row = fft_tw_row(R), n = NS * row;
+        if (e < off + n) {
+            const int k = (e - off) / row, r = (e - off) % row + 1;
+            m = r < R ? r * k * (N / (NS * R)) : -1;  // -1: padding
+            break;
+        }
+        off += n;
+    }
+    *m_out = m;
 }
 
 // Dispatch a runtime power-of-two size to a kernel template instantiated for

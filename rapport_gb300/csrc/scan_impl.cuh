@@ -144,46 +144,65 @@ static __device__ void block_reduce(float &m1, float &m2, int &f, float *red) {
 }
 
 
-// Solve one row's carrier march (all threads of the CTA).  On entry sI[0..Nt)
-// holds the intensities (synced); sW, sx, sJ, sB are scratch of Nt floats
-// each (may alias any other buffer the caller no longer needs).  On return
-// (synced) sx[t] holds the densities, sx[0] = x0.
 // Shared-memory slot of step n when thread t owns the contiguous chunk
-// [t C, (t + 1) C): slot j T + t for n = t C + j -- the threads of a warp then
-// touch consecutive words at every j (a plain layout would be C-way conflicted).
-__device__ __forceinline__ int scan_slot(int n, int C) { return (n % C) * (int)blockDim.x + n / C; }
+// [t C, (t + 1) C): slot j (T + pad) + t for n = t C + j.  In the sweeps the
+// threads of a warp touch consecutive words at every j; in the loops where
+// consecutive threads take consecutive n (filling the intensities, reading
+// the densities out), n % C spreads the lanes over C rows whose stride
+// T + pad is (32 / C) banks apart mod 32, so those are conflict-free too
+// (without the pad they would be C-way conflicted).
+__host__ __device__ __forceinline__ constexpr int scan_pad(int C) { return C >= 32 ? 1 : 32 / C; }
+
+// C = ceil((Nt - 1) / T) is a power of two for power-of-two Nt and T = 256,
+// so the slot map is two masks / shifts; S = T + pad is the row stride.
+struct ScanLayout {
+    int C, logC, S;
+};
+
+__device__ __forceinline__ ScanLayout scan_layout(int Nt) {
+    const int C = (Nt - 1 + (int)blockDim.x - 1) / (int)blockDim.x;
+    return ScanLayout{C, 31 - __clz(C), (int)blockDim.x + scan_pad(C)};
+}
+
+__device__ __forceinline__ int scan_slot(int n, const ScanLayout &L) {
+    return (n & (L.C - 1)) * L.S + (n >> L.logC);
+}
 
 // Number of floats each scan array needs for Nt points with `threads` threads:
-// one past the largest slot, reached at remainder C - 1 (= Nt for powers of two).
+// one past the largest slot, reached at n = Nt - 1 (remainder C - 1 for powers of two).
 __host__ __device__ __forceinline__ constexpr int scan_span(int Nt, int threads) {
-    return ((Nt - 1 + threads - 1) / threads - 1) * threads +
-           (Nt - (Nt - 1 + threads - 1) / threads) / ((Nt - 1 + threads - 1) / threads) + 1;
+    return ((Nt - 1 + threads - 1) / threads - 1) * (threads + scan_pad((Nt - 1 + threads - 1) / threads)) +
+           (Nt - 1) / ((Nt - 1 + threads - 1) / threads) + 1;
 }
 
 // Solve one row's carrier march (all threads of the CTA).  On entry sI holds
-// the intensities at slots scan_slot(t, C) (synced); sW, sx, sJ, sB are
-// scratch of scan_span(Nt) floats each (may alias any other buffer the caller
-// no longer needs).  On return (synced) sx[scan_slot(t, C)] holds the density
+// the intensities at slots scan_slot(t, scan_layout(Nt)) (synced); sW, sx, sJ,
+// sB are scratch of scan_span(Nt) floats each (may alias any other buffer the
+// caller no longer needs).  On return (synced) sx[slot of t] holds the density
 // at t, sx[slot 0] = x0.  C = chunk of steps per thread = ceil((Nt-1)/blockDim).
 static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ, float *sB, int Nt,
                                 const ScanParams &p, const float *__restrict__ lut, float x0, int *stats) {
     __shared__ Aff wsum[32];
     __shared__ float red[100];
     const int T = Nt - 1;
-    const int C = (T + blockDim.x - 1) / blockDim.x;
+    const ScanLayout L = scan_layout(Nt);
+    const int C = L.C;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
-        const int q = scan_slot(t, C);
+        const int q = scan_slot(t, L);
         sW[q] = lut_rate_dt(sI[q], lut, p);
         sx[q] = t == 0 ? x0 : 0.0f;
     }
     __syncthreads();
+    // the thread's chunk: steps n0 .. n1-1 at slots j S + tid; the step after
+    // the chunk's last is the next thread's first (slot tid + 1)
     const int n0 = min((int)threadIdx.x * C, T), n1 = min(n0 + C, T);
+    const int q_last = (int)threadIdx.x + 1;
     int converged = 0, clamp_any = 0;
     for (int it = 0; it < SCAN_MAX_IT; ++it) {
         Aff acc{1.0f, 0.0f};
         bool cl = false;
-        for (int n = n0; n < n1; ++n) {
-            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+        for (int n = n0, q0 = threadIdx.x; n < n1; ++n, q0 += L.S) {
+            const int q1 = n + 1 - n0 < C ? q0 + L.S : q_last;
             float Ia = 0.5f * (sI[q0] + sI[q1]);
             float b = 0.5f * (sW[q0] + sW[q1]);
             float xn = sx[q0];
@@ -197,8 +216,8 @@ static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ
         Aff pre = block_exclusive_scan(acc, wsum);
         float xs = fmaf(pre.A, x0, pre.B);
         float dmax = 0.0f, xmax = 0.0f;
-        for (int n = n0; n < n1; ++n) {
-            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+        for (int n = n0, q0 = threadIdx.x; n < n1; ++n, q0 += L.S) {
+            const int q1 = n + 1 - n0 < C ? q0 + L.S : q_last;
             xs = fmaf(sJ[q0], xs, sB[q0]);
             dmax = fmaxf(dmax, fabsf(xs - sx[q1]));
             xmax = fmaxf(xmax, fabsf(xs));
@@ -222,7 +241,7 @@ static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ
             float x = x0;
             bool cl = false;
             for (int n = 0; n < T; ++n) {
-                const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+                const int q0 = scan_slot(n, L), q1 = scan_slot(n + 1, L);
                 float Ia = 0.5f * (sI[q0] + sI[q1]);
                 float b = 0.5f * (sW[q0] + sW[q1]);
                 float J;
@@ -423,9 +442,10 @@ static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *
     __shared__ Aff2 wsum[32];
     __shared__ float red[100];
     const int T = Nt - 1;
-    const int C = (T + blockDim.x - 1) / blockDim.x;
+    const ScanLayout L = scan_layout(Nt);
+    const int C = L.C;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
-        const int q = scan_slot(t, C);
+        const int q = scan_slot(t, L);
         sW[q] = lut_rate_dt(sI[q], lut, p);
         sWs[q] = lut_rate_dt(sI[q], lut_s, p);
         se[q] = t == 0 ? x0e : 0.0f;
@@ -433,12 +453,13 @@ static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *
     }
     __syncthreads();
     const int n0 = min((int)threadIdx.x * C, T), n1 = min(n0 + C, T);
+    const int q_last = (int)threadIdx.x + 1;
     int converged = 0, clamp_any = 0;
     for (int it = 0; it < SCAN_MAX_IT; ++it) {
         Aff2 acc = aff2_identity();
         bool cl = false;
-        for (int n = n0; n < n1; ++n) {
-            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+        for (int n = n0, q0 = threadIdx.x; n < n1; ++n, q0 += L.S) {
+            const int q1 = n + 1 - n0 < C ? q0 + L.S : q_last;
             const float Ia = 0.5f * (sI[q0] + sI[q1]);
             const float b = 0.5f * (sW[q0] + sW[q1]), bs = 0.5f * (sWs[q0] + sWs[q1]);
             const float e = se[q0], s = ss[q0];
@@ -459,8 +480,8 @@ static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *
         float xe = fmaf(pre.m00, x0e, fmaf(pre.m01, x0s, pre.v0));
         float xs = fmaf(pre.m10, x0e, fmaf(pre.m11, x0s, pre.v1));
         float dmax = 0.0f, xmax = 0.0f;
-        for (int n = n0; n < n1; ++n) {
-            const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+        for (int n = n0, q0 = threadIdx.x; n < n1; ++n, q0 += L.S) {
+            const int q1 = n + 1 - n0 < C ? q0 + L.S : q_last;
             const float ne = fmaf(jm[0][q0], xe, fmaf(jm[1][q0], xs, jb[0][q0]));
             const float ns = fmaf(jm[2][q0], xe, fmaf(jm[3][q0], xs, jb[1][q0]));
             xe = ne;
@@ -483,7 +504,7 @@ static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *
         if (threadIdx.x == 0) {
             float e = x0e, s = x0s;
             for (int n = 0; n < T; ++n) {
-                const int q0 = scan_slot(n, C), q1 = scan_slot(n + 1, C);
+                const int q0 = scan_slot(n, L), q1 = scan_slot(n + 1, L);
                 step_exact2(e, s, 0.5f * (sI[q0] + sI[q1]), 0.5f * (sW[q0] + sW[q1]), 0.5f * (sWs[q0] + sWs[q1]), p);
                 se[q1] = e;
                 ss[q1] = s;
