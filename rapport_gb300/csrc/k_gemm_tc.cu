@@ -21,11 +21,12 @@
 // hi/lo 3-MMA scheme).  E's own rounding is systematic and would accumulate
 // over thousands of steps; carrying it in three terms removes that drift.
 //
-// Kernel: one 128 x 256 output tile per CTA; warp 0 = TMA producer, warp 1 =
-// TMEM allocator + MMA issuer (one elected thread), warps 2-5 = epilogue
-// (tcgen05.ld of their 32-lane TMEM quadrant, FP32 rows to global).  Operands
-// are staged by TMA (128-byte swizzle) into a 2-stage mbarrier pipeline:
-// A tiles K-major (box 64 x 128), B tiles MN-major (4 boxes of 64 x 64).
+// Kernel: persistent, 128 x 256 output tiles, one CTA per SM; warp 0 = TMA
+// producer, warp 1 = TMEM allocator + MMA issuer (one elected thread), warps
+// 2-5 = epilogue (tcgen05.ld of their 32-lane TMEM quadrant, FP32 rows to
+// global) on a double-buffered TMEM accumulator.  Operands are staged by TMA
+// (128- or 64-byte swizzle) into an mbarrier ring of 2-4 stages: A tiles
+// K-major (box BK x 128), B tiles MN-major (4 boxes of 64 x BK).
 // Every wait is bounded by %globaltimer; on timeout the kernel raises an
 // error word, drains what it issued, frees TMEM and returns.
 #include <cuda.h>
@@ -138,14 +139,67 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((uint32_t)(TC_BN >> 3) << 17) |
                             ((uint32_t)(TC_BM >> 4) << 24);
 
-// One 128 x 256 output tile at (m0, n0) of D[M x N] = A[M x K] B[K x N]; every
-// thread of the CTA calls it.  tmA / tmB: generic addresses of the tensor maps
-// (kernel-parameter or global memory).  TC_BK = k depth of one pipeline stage
-// (64: A rows of 128 B, 128-byte swizzle; 32: rows of 64 B, 64-byte swizzle),
-// TC_STAGES stages in the ring.
+// Where the tiles of a launch come from: one product D[M x N] = A B tiled
+// row-major (tiles == NULL), or a table of (pulse, m0, n0) over the pulses of
+// a batch, each with its own tensor maps (global memory) and sizes.
+struct TileSource {
+    const CUtensorMap *tmA, *tmB;  // single product
+    float *D;
+    int M, N, K;
+    const GemmTile *tiles;         // grouped: tile table, maps, pulses
+    const CUtensorMap *maps;
+    const BatchPulse *P;
+    int map_off;                   // 0: the k-64 maps of a pulse, 2: the k-32 maps
+};
+
+struct TileJob {
+    const CUtensorMap *tmA, *tmB;
+    float *D;
+    int M, N, K, m0, n0;
+};
+
+__device__ __forceinline__ TileJob tile_job(const TileSource &src, int t) {
+    TileJob j;
+    if (src.tiles) {
+        const GemmTile g = src.tiles[t];
+        const BatchPulse &q = src.P[g.pulse];
+        j.tmA = src.maps + 4 * g.pulse + src.map_off;
+        j.tmB = j.tmA + 1;
+        j.D = q.D;
+        j.M = q.M;
+        j.N = q.N;
+        j.K = q.K;
+        j.m0 = g.m0;
+        j.n0 = g.n0;
+    } else {
+        const int nt = src.N / TC_BN;
+        j.tmA = src.tmA;
+        j.tmB = src.tmB;
+        j.D = src.D;
+        j.M = src.M;
+        j.N = src.N;
+        j.K = src.K;
+        j.m0 = (t / nt) * TC_BM;
+        j.n0 = (t % nt) * TC_BN;
+    }
+    return j;
+}
+
+// Persistent warp-specialised product: CTA b computes tiles b, b + G, b + 2G,
+// ... (G = gridDim.x, at most one CTA per SM).  The TMA producer runs the
+// stage ring across tile boundaries, and the accumulator is double-buffered
+// in TMEM (2 x 256 columns): while the epilogue warps drain tile i from one
+// buffer, the MMA issuer already accumulates tile i + 1 into the other, so the
+// tensor pipe does not wait for the epilogue, the pipeline fill or the CTA
+// set-up of the next tile.  Each tile's MMA sequence is exactly that of a
+// single-tile CTA (same k order, first MMA without accumulate).
+//   warp 0: TMA producer; warp 1: TMEM allocator + MMA issuer; warps 2-5:
+//   epilogue (each its 32-lane TMEM quadrant).
+// Every wait is bounded by %globaltimer; on timeout the CTA raises an error
+// bit, stops issuing, waits (bounded) for the copies and MMAs it issued,
+// frees TMEM and returns.
 template <int A_TERMS, int TC_BK, int TC_STAGES>
-__device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensorMap *tmB, float *__restrict__ D,
-                                          int M, int N, int K, int m0, int n0, int *__restrict__ err) {
+__device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntiles, int *__restrict__ err) {
     constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;  // one term
     constexpr uint32_t B_BYTES = TC_BK * TC_BN * 2;  // one term
     constexpr uint32_t B_BOX = 64 * TC_BK * 2;       // one 64-column box
@@ -154,19 +208,23 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensor
     constexpr uint32_t A_SBO = TC_BK * 2 * 8;        // 8 rows of one swizzle atom
     extern __shared__ uint8_t smem_raw[];
     uint8_t *smem = (uint8_t *)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-    __shared__ __align__(8) uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES], acc_bar;
+    __shared__ __align__(8) uint64_t full_bar[TC_STAGES], empty_bar[TC_STAGES];
+    __shared__ __align__(8) uint64_t acc_full[2], acc_empty[2], done_bar;
     __shared__ uint32_t tmem_base;
     __shared__ int abort_flag, issued;
 
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int KB = K / TC_BK;
 
     if (threadIdx.x == 0) {
         for (int s = 0; s < TC_STAGES; ++s) {
             mbar_init(&full_bar[s], 1);
             mbar_init(&empty_bar[s], 1);
         }
-        mbar_init(&acc_bar, 1);
+        for (int a = 0; a < 2; ++a) {
+            mbar_init(&acc_full[a], 1);
+            mbar_init(&acc_empty[a], 4);  // one arrival per epilogue warp
+        }
+        mbar_init(&done_bar, 1);
         abort_flag = 0;
         issued = 0;
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -174,7 +232,7 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensor
     if (warp == 1) {
         asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                          smem_u32(&tmem_base)),
-                     "r"(TC_BN));
+                     "r"(2 * TC_BN));
         asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
     }
     tc_fence_before();
@@ -184,86 +242,121 @@ __device__ __forceinline__ void gemm_tile(const CUtensorMap *tmA, const CUtensor
 
     if (warp == 0 && lane == 0) {
         // ------------------------------------------------ TMA producer
-        for (int kb = 0; kb < KB; ++kb) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-            if (!mbar_wait(&empty_bar[s], ph ^ 1u) || *(volatile int *)&abort_flag) {
-                atomicOr(err, 1);
-                abort_flag = 1;
-                break;
+        int g = 0;  // stage sequence number across tiles
+        for (int t = blockIdx.x; t < ntiles && !*(volatile int *)&abort_flag; t += gridDim.x) {
+            const TileJob j = tile_job(src, t);
+            const int KB = j.K / TC_BK;
+            for (int kb = 0; kb < KB; ++kb, ++g) {
+                const int s = g % TC_STAGES;
+                const uint32_t ph = (uint32_t)(g / TC_STAGES) & 1u;
+                if (!mbar_wait(&empty_bar[s], ph ^ 1u) || *(volatile int *)&abort_flag) {
+                    atomicOr(err, 1);
+                    abort_flag = 1;
+                    break;
+                }
+                uint8_t *st = smem + (size_t)s * STAGE;
+                mbar_expect_tx(&full_bar[s], STAGE);
+#pragma unroll
+                for (int a = 0; a < A_TERMS; ++a)
+                    tma_load_2d(st + a * A_BYTES, j.tmA, &full_bar[s], kb * TC_BK, a * j.M + j.m0);
+#pragma unroll
+                for (int b = 0; b < 2; ++b)
+#pragma unroll
+                    for (int c = 0; c < TC_BN / 64; ++c)
+                        tma_load_2d(st + A_TERMS * A_BYTES + b * B_BYTES + c * B_BOX, j.tmB, &full_bar[s],
+                                    j.n0 + 64 * c, b * j.K + kb * TC_BK);
+                issued = g + 1;
             }
-            uint8_t *st = smem + (size_t)s * STAGE;
-            mbar_expect_tx(&full_bar[s], STAGE);
-#pragma unroll
-            for (int t = 0; t < A_TERMS; ++t) tma_load_2d(st + t * A_BYTES, tmA, &full_bar[s], kb * TC_BK, t * M + m0);
-#pragma unroll
-            for (int t = 0; t < 2; ++t)
-#pragma unroll
-                for (int j = 0; j < TC_BN / 64; ++j)
-                    tma_load_2d(st + A_TERMS * A_BYTES + t * B_BYTES + j * B_BOX, tmB, &full_bar[s], n0 + 64 * j,
-                                t * K + kb * TC_BK);
-            issued = kb + 1;
         }
     } else if (warp == 1 && lane == 0) {
         // ------------------------------------------------ MMA issuer
         // term pairs (a, b): Eh.wh, Eh.wl, Em.wh [, El.wh]
         const int pa[4] = {0, 0, 1, 2}, pb[4] = {0, 1, 0, 0};
         constexpr int NPAIR = A_TERMS == 3 ? 4 : 3;
-        for (int kb = 0; kb < KB; ++kb) {
-            const int s = kb % TC_STAGES;
-            const uint32_t ph = (uint32_t)(kb / TC_STAGES) & 1u;
-            if (!mbar_wait(&full_bar[s], ph) || *(volatile int *)&abort_flag) {
+        int g = 0, i = 0;
+        for (int t = blockIdx.x; t < ntiles && !*(volatile int *)&abort_flag; t += gridDim.x, ++i) {
+            const int acc = i & 1;
+            const uint32_t d_tmem = tmem + (uint32_t)(acc * TC_BN);
+            // the epilogue has drained this buffer (tile i - 2)
+            if (!mbar_wait(&acc_empty[acc], (((uint32_t)i >> 1) & 1u) ^ 1u)) {
                 atomicOr(err, 2);
                 abort_flag = 1;
                 break;
             }
             tc_fence_after();
-            const uint32_t a0 = smem_u32(smem + (size_t)s * STAGE);
-            const uint32_t b0 = a0 + A_TERMS * A_BYTES;
-#pragma unroll
-            for (int kk = 0; kk < TC_BK / 16; ++kk) {
-#pragma unroll
-                for (int p = 0; p < NPAIR; ++p) {
-                    const uint64_t ad = smem_desc(a0 + pa[p] * A_BYTES + kk * 32, 16, A_SBO, A_SWZ);
-                    const uint64_t bd = smem_desc(b0 + pb[p] * B_BYTES + kk * 2048, B_BOX, 1024, 2u);
-                    umma_bf16(tmem, ad, bd, kIdesc, (kb | kk | p) != 0);
+            const int KB = src.tiles ? src.P[src.tiles[t].pulse].K / TC_BK : src.K / TC_BK;
+            bool ok = true;
+            for (int kb = 0; kb < KB; ++kb, ++g) {
+                const int s = g % TC_STAGES;
+                const uint32_t ph = (uint32_t)(g / TC_STAGES) & 1u;
+                if (!mbar_wait(&full_bar[s], ph) || *(volatile int *)&abort_flag) {
+                    atomicOr(err, 2);
+                    abort_flag = 1;
+                    ok = false;
+                    break;
                 }
+                tc_fence_after();
+                const uint32_t a0 = smem_u32(smem + (size_t)s * STAGE);
+                const uint32_t b0 = a0 + A_TERMS * A_BYTES;
+#pragma unroll
+                for (int kk = 0; kk < TC_BK / 16; ++kk) {
+#pragma unroll
+                    for (int p = 0; p < NPAIR; ++p) {
+                        const uint64_t ad = smem_desc(a0 + pa[p] * A_BYTES + kk * 32, 16, A_SBO, A_SWZ);
+                        const uint64_t bd = smem_desc(b0 + pb[p] * B_BYTES + kk * 2048, B_BOX, 1024, 2u);
+                        umma_bf16(d_tmem, ad, bd, kIdesc, (kb | kk | p) != 0);
+                    }
+                }
+                umma_commit(&empty_bar[s]);
             }
-            umma_commit(&empty_bar[s]);
+            if (!ok) break;
+            umma_commit(&acc_full[acc]);
         }
-        umma_commit(&acc_bar);  // always: the epilogue / teardown waits on it
+        umma_commit(&done_bar);  // always: teardown waits for every MMA issued here
     } else if (warp >= 2) {
         // ------------------------------------------------ epilogue
         const int q = warp & 3;
-        const bool ok = mbar_wait(&acc_bar, 0);
-        if (!ok) atomicOr(err, 4);
-        if (ok && !*(volatile int *)&abort_flag) {
+        int i = 0;
+        for (int t = blockIdx.x; t < ntiles; t += gridDim.x, ++i) {
+            const int acc = i & 1;
+            if (!mbar_wait(&acc_full[acc], ((uint32_t)i >> 1) & 1u)) {
+                atomicOr(err, 4);
+                abort_flag = 1;
+                break;
+            }
+            if (*(volatile int *)&abort_flag) break;
             tc_fence_after();
-            float *row = D + (size_t)(m0 + q * 32 + lane) * N + n0;
+            const TileJob j = tile_job(src, t);
+            float *row = j.D + (size_t)(j.m0 + q * 32 + lane) * j.N + j.n0;
+            const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TC_BN);
 #pragma unroll 1
             for (int c = 0; c < TC_BN / 32; ++c) {
                 uint32_t r[32];
-                tmem_ld32(tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(c * 32), r);
+                tmem_ld32(tq + (uint32_t)(c * 32), r);
                 float4 *dst = reinterpret_cast<float4 *>(row + c * 32);
 #pragma unroll
                 for (int v = 0; v < 8; ++v)
                     dst[v] = make_float4(__uint_as_float(r[4 * v]), __uint_as_float(r[4 * v + 1]),
                                          __uint_as_float(r[4 * v + 2]), __uint_as_float(r[4 * v + 3]));
             }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(&acc_empty[acc]))
+                                        : "memory");
         }
     }
     tc_fence_before();
     __syncthreads();
     if (abort_flag && threadIdx.x == 0) {
         // drain: the last loads this CTA issued must land before it exits
-        for (int kb = issued - TC_STAGES; kb < issued; ++kb)
-            if (kb >= 0) mbar_wait(&full_bar[kb % TC_STAGES], (uint32_t)(kb / TC_STAGES) & 1u);
+        for (int g = issued - TC_STAGES; g < issued; ++g)
+            if (g >= 0) mbar_wait(&full_bar[g % TC_STAGES], (uint32_t)(g / TC_STAGES) & 1u);
     }
     if (warp == 1) {
-        if (abort_flag && lane == 0) mbar_wait(&acc_bar, 0);  // MMAs done before TMEM is released
+        if (lane == 0) mbar_wait(&done_bar, 0);  // every MMA done before TMEM is released
         __syncwarp();
         tc_fence_after();
-        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_BN));
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(2 * TC_BN));
     }
 }
 
@@ -271,27 +364,39 @@ template <int A_TERMS, int BK, int ST>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
           float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
-    const int n_tiles = N / TC_BN;
-    gemm_tile<A_TERMS, BK, ST>(&tmA, &tmB, D, M, N, K, (blockIdx.x / n_tiles) * TC_BM,
-                               (blockIdx.x % n_tiles) * TC_BN, err);
+    TileSource src{&tmA, &tmB, D, M, N, K, nullptr, nullptr, nullptr, 0};
+    gemm_persistent<A_TERMS, BK, ST>(src, (M / TC_BM) * (N / TC_BN), err);
 }
 
-// Grouped product over many pulses: CTA b computes tiles[b] of pulse tiles[b].pulse,
-// whose A / B tensor maps are maps[2 p] / maps[2 p + 1] (global memory, written
-// by the host before the launch).
+// Grouped product over many pulses: the tiles of tiles[0 .. ntiles) of pulse
+// tiles[t].pulse, whose tensor maps are maps[4 p ..] (global memory, written
+// by the host before the launch): [4p] A (box 64), [4p+1] B (box 64),
+// [4p+2] A (box 32), [4p+3] B (box 32).
 template <int A_TERMS, int BK, int ST>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc_grouped(const CUtensorMap *__restrict__ maps, const BatchPulse *__restrict__ P,
-                  const GemmTile *__restrict__ tiles, int *__restrict__ err) {
-    const GemmTile t = tiles[blockIdx.x];
-    const BatchPulse &q = P[t.pulse];
-    // maps of pulse p: [4p] A (box 64), [4p+1] B (box 64), [4p+2] A (box 32), [4p+3] B (box 32)
-    const CUtensorMap *m = maps + 4 * t.pulse + (BK == 32 ? 2 : 0);
-    gemm_tile<A_TERMS, BK, ST>(m, m + 1, q.D, q.M, q.N, q.K, t.m0, t.n0, err);
+                  const GemmTile *__restrict__ tiles, int ntiles, int *__restrict__ err) {
+    TileSource src{nullptr, nullptr, nullptr, 0, 0, 0, tiles, maps, P, BK == 32 ? 2 : 0};
+    gemm_persistent<A_TERMS, BK, ST>(src, ntiles, err);
 }
 
+// One CTA per SM at most (the stage ring and the 512 TMEM columns fill it).
+static int tc_grid(int ntiles) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1)
+            sms = 1;
+    }
+    return ntiles < sms ? ntiles : sms;
+}
+
+// Dynamic shared memory of a pipeline variant; never less than 120 KB, so two
+// CTAs of the product can not share an SM (each allocates all 512 TMEM columns).
 static size_t tc_smem_bytes(int a_terms, int bk, int stages) {
-    return (size_t)stages * (a_terms * TC_BM * bk * 2 + 2 * bk * TC_BN * 2) + 1024;
+    const size_t need = (size_t)stages * (a_terms * TC_BM * bk * 2 + 2 * bk * TC_BN * 2) + 1024;
+    return need < 120 * 1024 ? 120 * 1024 : need;
 }
 
 // variant: 0 = (BK 64, 2 stages), 1 = (BK 32, 4 stages), 2 = (BK 32, 3 stages),
@@ -313,7 +418,7 @@ cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P,
         cudaError_t e = cudaFuncSetAttribute(k_gemm_tc_grouped<AT, BK, ST>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_gemm_tc_grouped<AT, BK, ST><<<ntiles, TC_THREADS, smem, stream>>>(maps, P, tiles, err);
+        k_gemm_tc_grouped<AT, BK, ST><<<tc_grid(ntiles), TC_THREADS, smem, stream>>>(maps, P, tiles, ntiles, err);
     })
     return cudaGetLastError();
 }
@@ -321,7 +426,7 @@ cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P,
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
                            int a_terms, int variant, int *err, cudaStream_t stream) {
     if (M % TC_BM || N % TC_BN || K % 64) return cudaErrorInvalidValue;
-    const dim3 grid((M / TC_BM) * (N / TC_BN));
+    const int grid = tc_grid((M / TC_BM) * (N / TC_BN));
     TC_DISPATCH(a_terms, variant, {
         const size_t smem = tc_smem_bytes(AT, BK, ST);
         cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<AT, BK, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
