@@ -74,7 +74,10 @@ enum {
 /* Linear-operator arithmetic used by nlse_step. */
 enum {
     NLSE_MODE_PLAIN_F32 = 0,   /* FP32 SIMT Hankel products, reference order  */
-    NLSE_MODE_SPLIT_BF16 = 1   /* tcgen05 split-BF16 merged operator (I + E)  */
+    NLSE_MODE_SPLIT_BF16 = 1,  /* tcgen05 split-BF16 merged operator (I + E):
+                                  E in 3 BF16 terms, field in 2, 4 MMAs      */
+    NLSE_MODE_SPLIT_F16 = 2    /* the same product with E and the field each in
+                                  2 scaled FP16 terms (~22 bits), 3 MMAs      */
 };
 
 /*
@@ -134,8 +137,9 @@ int nlse_create(const nlse_grid_desc *desc, nlse_ctx **out);
 int nlse_half_linear(nlse_ctx *ctx, void *u, double dz, void *stream);
 
 /* half_linear with an explicit arithmetic: NLSE_MODE_PLAIN_F32 (reference
- * order: two FP32 Hankel products around the FFT pair) or NLSE_MODE_SPLIT_BF16
- * (one tcgen05 product with the merged operator Y diag(P_r) Y = I + E). */
+ * order: two FP32 Hankel products around the FFT pair), NLSE_MODE_SPLIT_BF16
+ * or NLSE_MODE_SPLIT_F16 (one tcgen05 product with the merged operator
+ * Y diag(P_r) Y = I + E). */
 int nlse_half_linear_ex(nlse_ctx *ctx, void *u, double dz, int mode, void *stream);
 
 /* (rhs, alpha) <- split(u, rho, rho_s): RK right-hand side and absorption
@@ -208,6 +212,9 @@ int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch **out);
 int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const *rho,
                          float *const *rho_s, double dz, int nsteps, void *stream);
 int nlse_batch_get_context(nlse_batch *b, int i, nlse_ctx **out);
+/* The batch's tensor-core form: NLSE_MODE_SPLIT_BF16 (default) or
+ * NLSE_MODE_SPLIT_F16. */
+int nlse_batch_set_mode(nlse_batch *b, int mode);
 int nlse_batch_set_split_terms(nlse_batch *b, int a_terms);
 int nlse_batch_device_status(nlse_batch *b, int *word);
 int nlse_batch_get_last_error(const nlse_batch *b, char *buf, size_t len);
@@ -227,7 +234,8 @@ int nlse_get_gemm_variant(const nlse_ctx *ctx);
 int nlse_set_split_terms(nlse_ctx *ctx, int a_terms);
 
 /* Synchronise and read the device status word: NLSE_ERR_TIMEOUT if a kernel
- * gave up a bounded wait since nlse_create (word receives the raw bits). */
+ * gave up a bounded wait since nlse_create (word receives the raw bits);
+ * NLSE_ERR_DEVICE_FLAG if a split-FP16 field write overflowed FP16. */
 int nlse_device_status(nlse_ctx *ctx, int *word);
 
 /* Per-radius diagnostics of one saved plane (Integrator._record,

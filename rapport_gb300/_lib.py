@@ -15,14 +15,14 @@ LIB_PATH = os.path.join(PKG, "lib", "libnlse.so")
 NLSE_OK, NLSE_ERR_INVALID_ARG, NLSE_ERR_UNSUPPORTED, NLSE_ERR_CUDA, NLSE_ERR_DEVICE_FLAG, NLSE_ERR_TIMEOUT = range(6)
 F_KERR_INSTANT, F_PHOTO_LOSS, F_PLASMA_DEFOC, F_PLASMA_ABSORB = 1, 2, 4, 8
 F_KERR_RAMAN, F_SELF_STEEP, F_SPACE_TIME, F_STE = 16, 32, 64, 128
-MODE_PLAIN_F32, MODE_SPLIT_BF16 = 0, 1
+MODE_PLAIN_F32, MODE_SPLIT_BF16, MODE_SPLIT_F16 = 0, 1, 2
 
 # every symbol include/nlse.h declares (checked by the CPU test suite)
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_rate_equation", "nlse_step", "nlse_step_batched", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
            "nlse_half_linear_noalloc", "nlse_record", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
-           "nlse_batch_set_split_terms", "nlse_batch_device_status", "nlse_batch_get_last_error",
+           "nlse_batch_set_split_terms", "nlse_batch_set_mode", "nlse_batch_device_status", "nlse_batch_get_last_error",
            "nlse_batch_destroy",
            "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
            "nlse_get_last_error", "nlse_destroy", "nlse_version")
@@ -94,6 +94,7 @@ def load():
     lib.nlse_batch_propagate.argtypes = [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), _D, _I, _P]
     lib.nlse_batch_get_context.argtypes = [_P, _I, ctypes.POINTER(_P)]
     lib.nlse_batch_set_split_terms.argtypes = [_P, _I]
+    lib.nlse_batch_set_mode.argtypes = [_P, _I]
     lib.nlse_batch_device_status.argtypes = [_P, ctypes.POINTER(_I)]
     lib.nlse_batch_get_last_error.argtypes = [_P, ctypes.c_char_p, ctypes.c_size_t]
     lib.nlse_batch_destroy.argtypes = [_P]
@@ -408,6 +409,10 @@ class Batch:
 
     def set_split_terms(self, n):
         _check(self.lib, None, self.lib.nlse_batch_set_split_terms(self.h, int(n)))
+
+    def set_mode(self, mode):
+        """MODE_SPLIT_BF16 (default) or MODE_SPLIT_F16."""
+        _check(self.lib, None, self.lib.nlse_batch_set_mode(self.h, int(mode)))
 
     def device_status(self):
         w = _I(0)

@@ -30,6 +30,7 @@
 // Every wait is bounded by %globaltimer; on timeout the kernel raises an
 // error word, drains what it issued, frees TMEM and returns.
 #include <cuda.h>
+#include <cuda_fp16.h>
 
 #include "nlse_internal.cuh"
 
@@ -134,10 +135,13 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, uint32_t (&r)[32]) {
 
 }  // namespace
 
-// Instruction descriptor, kind::f16: FP32 accumulate, BF16 A and B, A K-major,
-// B MN-major, N = 256, M = 128.
-constexpr uint32_t kIdesc = (1u << 4) | (1u << 7) | (1u << 10) | (1u << 16) | ((uint32_t)(TC_BN >> 3) << 17) |
-                            ((uint32_t)(TC_BM >> 4) << 24);
+// Instruction descriptor, kind::f16: FP32 accumulate, BF16 (F16 = false) or
+// FP16 (F16 = true) A and B, A K-major, B MN-major, N = 256, M = 128.
+template <bool F16>
+constexpr uint32_t idesc_f16() {
+    return (1u << 4) | (F16 ? 0u : (1u << 7) | (1u << 10)) | (1u << 16) | ((uint32_t)(TC_BN >> 3) << 17) |
+           ((uint32_t)(TC_BM >> 4) << 24);
+}
 
 // Where the tiles of a launch come from: one product D[M x N] = A B tiled
 // row-major (tiles == NULL), or a table of (pulse, m0, n0) over the pulses of
@@ -198,8 +202,9 @@ __device__ __forceinline__ TileJob tile_job(const TileSource &src, int t) {
 // Every wait is bounded by %globaltimer; on timeout the CTA raises an error
 // bit, stops issuing, waits (bounded) for the copies and MMAs it issued,
 // frees TMEM and returns.
-template <int A_TERMS, int TC_BK, int TC_STAGES>
+template <int A_TERMS, int TC_BK, int TC_STAGES, bool F16>
 __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntiles, int *__restrict__ err) {
+    constexpr uint32_t kIdesc = idesc_f16<F16>();
     constexpr uint32_t A_BYTES = TC_BM * TC_BK * 2;  // one term
     constexpr uint32_t B_BYTES = TC_BK * TC_BN * 2;  // one term
     constexpr uint32_t B_BOX = 64 * TC_BK * 2;       // one 64-column box
@@ -270,7 +275,7 @@ __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntile
         }
     } else if (warp == 1 && lane == 0) {
         // ------------------------------------------------ MMA issuer
-        // term pairs (a, b): Eh.wh, Eh.wl, Em.wh [, El.wh]
+        // term pairs (a, b): Eh.wh, Eh.wl, Em.wh [, El.wh]  (FP16: Eh.wh, Eh.wl, El.wh)
         const int pa[4] = {0, 0, 1, 2}, pb[4] = {0, 1, 0, 0};
         constexpr int NPAIR = A_TERMS == 3 ? 4 : 3;
         int g = 0, i = 0;
@@ -360,24 +365,24 @@ __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntile
     }
 }
 
-template <int A_TERMS, int BK, int ST>
+template <int A_TERMS, int BK, int ST, bool F16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
           float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
     TileSource src{&tmA, &tmB, D, M, N, K, nullptr, nullptr, nullptr, 0};
-    gemm_persistent<A_TERMS, BK, ST>(src, (M / TC_BM) * (N / TC_BN), err);
+    gemm_persistent<A_TERMS, BK, ST, F16>(src, (M / TC_BM) * (N / TC_BN), err);
 }
 
 // Grouped product over many pulses: the tiles of tiles[0 .. ntiles) of pulse
 // tiles[t].pulse, whose tensor maps are maps[4 p ..] (global memory, written
 // by the host before the launch): [4p] A (box 64), [4p+1] B (box 64),
 // [4p+2] A (box 32), [4p+3] B (box 32).
-template <int A_TERMS, int BK, int ST>
+template <int A_TERMS, int BK, int ST, bool F16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc_grouped(const CUtensorMap *__restrict__ maps, const BatchPulse *__restrict__ P,
                   const GemmTile *__restrict__ tiles, int ntiles, int *__restrict__ err) {
     TileSource src{nullptr, nullptr, nullptr, 0, 0, 0, tiles, maps, P, BK == 32 ? 2 : 0};
-    gemm_persistent<A_TERMS, BK, ST>(src, ntiles, err);
+    gemm_persistent<A_TERMS, BK, ST, F16>(src, ntiles, err);
 }
 
 // One CTA per SM at most (the stage ring and the 512 TMEM columns fill it).
@@ -402,37 +407,40 @@ static size_t tc_smem_bytes(int a_terms, int bk, int stages) {
 // variant: 0 = (BK 64, 2 stages), 1 = (BK 32, 4 stages), 2 = (BK 32, 3 stages),
 // 3 = (BK 32, 2 stages).  2 and 3 leave shared memory for a row-kernel CTA
 // on the same SM (169 KB / 116 KB of the 228 KB).
-#define TC_DISPATCH_AT(AT_, variant, ...)                                                   \
-    if (variant == 0) { constexpr int AT = AT_, BK = 64, ST = 2; __VA_ARGS__; }            \
-    else if (variant == 1) { constexpr int AT = AT_, BK = 32, ST = 4; __VA_ARGS__; }       \
-    else if (variant == 2) { constexpr int AT = AT_, BK = 32, ST = 3; __VA_ARGS__; }       \
-    else { constexpr int AT = AT_, BK = 32, ST = 2; __VA_ARGS__; }
-#define TC_DISPATCH(a_terms, variant, ...)                                                  \
-    if (a_terms == 3) { TC_DISPATCH_AT(3, variant, __VA_ARGS__) }                           \
-    else { TC_DISPATCH_AT(2, variant, __VA_ARGS__) }
+#define TC_DISPATCH_AT(AT_, F16_, variant, ...)                                                   \
+    if (variant == 0) { constexpr int AT = AT_, BK = 64, ST = 2; constexpr bool F16 = F16_; __VA_ARGS__; }      \
+    else if (variant == 1) { constexpr int AT = AT_, BK = 32, ST = 4; constexpr bool F16 = F16_; __VA_ARGS__; } \
+    else if (variant == 2) { constexpr int AT = AT_, BK = 32, ST = 3; constexpr bool F16 = F16_; __VA_ARGS__; } \
+    else { constexpr int AT = AT_, BK = 32, ST = 2; constexpr bool F16 = F16_; __VA_ARGS__; }
+// BF16: 3 or 2 operator terms; FP16: always 2 operator terms (3 MMAs)
+#define TC_DISPATCH(a_terms, f16, variant, ...)                                                  \
+    if (f16) { TC_DISPATCH_AT(2, true, variant, __VA_ARGS__) }                                   \
+    else if (a_terms == 3) { TC_DISPATCH_AT(3, false, variant, __VA_ARGS__) }                    \
+    else { TC_DISPATCH_AT(2, false, variant, __VA_ARGS__) }
 
 cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
-                                   int a_terms, int variant, int *err, cudaStream_t stream) {
-    TC_DISPATCH(a_terms, variant, {
+                                   int a_terms, int variant, int f16, int *err, cudaStream_t stream) {
+    TC_DISPATCH(a_terms, f16, variant, {
         const size_t smem = tc_smem_bytes(AT, BK, ST);
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc_grouped<AT, BK, ST>,
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc_grouped<AT, BK, ST, F16>,
                                              cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_gemm_tc_grouped<AT, BK, ST><<<tc_grid(ntiles), TC_THREADS, smem, stream>>>(maps, P, tiles, ntiles, err);
+        k_gemm_tc_grouped<AT, BK, ST, F16>
+            <<<tc_grid(ntiles), TC_THREADS, smem, stream>>>(maps, P, tiles, ntiles, err);
     })
     return cudaGetLastError();
 }
 
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
-                           int a_terms, int variant, int *err, cudaStream_t stream) {
+                           int a_terms, int variant, int f16, int *err, cudaStream_t stream) {
     if (M % TC_BM || N % TC_BN || K % 64) return cudaErrorInvalidValue;
     const int grid = tc_grid((M / TC_BM) * (N / TC_BN));
-    TC_DISPATCH(a_terms, variant, {
+    TC_DISPATCH(a_terms, f16, variant, {
         const size_t smem = tc_smem_bytes(AT, BK, ST);
-        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<AT, BK, ST>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+        cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<AT, BK, ST, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
-        k_gemm_tc<AT, BK, ST><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
+        k_gemm_tc<AT, BK, ST, F16><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
     })
     return cudaGetLastError();
 }
@@ -513,12 +521,57 @@ __global__ void k_split_E(const double *__restrict__ Er, const double *__restric
     }
 }
 
+// max |E| (float bits; every entry of Er and Ei) into scale[NLSE_SC_EMAX].
+__global__ void k_absmax_E(const double *__restrict__ Er, const double *__restrict__ Ei, size_t n,
+                           int *__restrict__ scale) {
+    float mx = 0.0f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x)
+        mx = fmaxf(mx, (float)fmax(fabs(Er[i]), fabs(Ei[i])));
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) mx = fmaxf(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+    if ((threadIdx.x & 31) == 0) atomicMax(&scale[NLSE_SC_EMAX], __float_as_int(mx));
+}
+
+// E' 2^sa as two FP16 terms (h + l, ~22 bits), sa = 14 - e with max |E| < 2^e:
+// the largest entry lands in [2^13, 2^14), far from FP16's 65504, and entries
+// down to 2^-11 of it keep both terms normal.  sa goes to scale[NLSE_SC_SA].
+__global__ void k_split_E16(const double *__restrict__ Er, const double *__restrict__ Ei, int Nr,
+                            __half *__restrict__ A, int *__restrict__ scale) {
+    const float emax = __int_as_float(scale[NLSE_SC_EMAX]);
+    int e = 0;
+    if (emax > 0.0f && isfinite(emax)) frexpf(emax, &e);
+    const int sa = min(max(14 - e, -100), 100);
+    if (blockIdx.x == 0 && threadIdx.x == 0) scale[NLSE_SC_SA] = sa;
+    const double sc = ldexp(1.0, sa);
+    const size_t K2 = 2 * (size_t)Nr;
+    const size_t total = K2 * K2;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
+        size_t m = i / K2, k = i % K2;
+        size_t mr = m % Nr, kr = k % Nr;
+        bool mi = m >= (size_t)Nr, ki = k >= (size_t)Nr;
+        double v = ((mi == ki) ? Er[mr * Nr + kr] : (mi ? Ei[mr * Nr + kr] : -Ei[mr * Nr + kr])) * sc;
+        const __half h = __double2half(v);
+        A[i] = h;
+        A[total + i] = __double2half(v - (double)__half2float(h));
+    }
+}
+
 cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
-                                  double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, cudaStream_t stream) {
+                                  double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, int f16, int *scale,
+                                  cudaStream_t stream) {
     dim3 grid((Nr + 31) / 32, (Nr + 31) / 32);
     k_build_E<<<grid, 256, 0, stream>>>(Y64, rho, Nr, dz, komega, Er, Ei);
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_split_E<<<1024, 256, 0, stream>>>(Er, Ei, Nr, a_terms, A);
+    if (!f16) {
+        k_split_E<<<1024, 256, 0, stream>>>(Er, Ei, Nr, a_terms, A);
+        return cudaGetLastError();
+    }
+    e = cudaMemsetAsync(scale + NLSE_SC_EMAX, 0, sizeof(int), stream);
+    if (e != cudaSuccess) return e;
+    k_absmax_E<<<304, 256, 0, stream>>>(Er, Ei, (size_t)Nr * Nr, scale);
+    e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    k_split_E16<<<1024, 256, 0, stream>>>(Er, Ei, Nr, reinterpret_cast<__half *>(A), scale);
     return cudaGetLastError();
 }

@@ -16,46 +16,110 @@
 // and writes its row once (HBM) and does the FFTs, the nonlinear block and the
 // scan in shared memory.
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 
 #include "fullnl_impl.cuh"
 #include "scan_impl.cuh"
 
 
-// FP32 planar rows + BF16 hi/lo terms of one complex row held in smem
-// (padded indexing); two points per thread per iteration.
+// Exponent sb of the FP16 field terms of GEMM input g (split-FP16 form): the
+// largest |w| of input g - 1 (one z half-step earlier) maps to below 2^7, so
+// the terms stay below FP16's 65504 unless |w| grows 512-fold in a half step
+// (an overflow is counted in scale[NLSE_SC_OVF]); values down to 2^-17 of the
+// maximum keep all 22 bits of the two terms.
+__device__ __forceinline__ int f16_field_exp(const int *scale, int g) {
+    const float prev = __int_as_float(__ldcg(&scale[NLSE_SC_MAX + (g + 2) % 3]));
+    if (!(prev > 0.0f) || !isfinite(prev)) return 0;
+    int e;
+    frexpf(prev, &e);  // prev < 2^e
+    return min(max(7 - e, -100), 100);
+}
+
+// Block-wide max of a non-negative float (all threads; result valid in thread 0).
+__device__ __forceinline__ float block_max(float v) {
+    __shared__ float red[NLSE_ROW_THREADS / 32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+    __syncthreads();
+    if (threadIdx.x == 0)
+        for (int w = 1; w < (int)(blockDim.x >> 5); ++w) v = fmaxf(v, red[w]);
+    return v;
+}
+
+// FP32 planar rows + the 16-bit hi/lo terms (the GEMM's B operand) of one
+// complex row held in smem (padded indexing); two points per thread per
+// iteration.  BF16 form: hi = bf16(w), lo = bf16(w - hi).  Split-FP16 form:
+// the same of w 2^sb in FP16, with the row's max |w| and the bookkeeping of
+// the scale cells (g_out = the index of this GEMM input).
 template <int NT>
 __device__ __forceinline__ void store_state_row(const float2 *s, int r, const RowFusedArgs &a, float *F32,
-                                                __nv_bfloat16 *Fb) {
+                                                __nv_bfloat16 *Fb, int g_out) {
     const size_t rows = 2 * (size_t)a.Nr;
     float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nr + r) * NT;
     __nv_bfloat16 *hre = Fb + (size_t)r * NT, *him = Fb + ((size_t)a.Nr + r) * NT;
     __nv_bfloat16 *lre = hre + rows * NT, *lim = him + rows * NT;
+    if (!a.f16) {
+        for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
+            const float2 v0 = s[pidx(t)], v1 = s[pidx(t + 1)];
+            *reinterpret_cast<float2 *>(re + t) = make_float2(v0.x, v1.x);
+            *reinterpret_cast<float2 *>(im + t) = make_float2(v0.y, v1.y);
+            const __nv_bfloat162 hx = __floats2bfloat162_rn(v0.x, v1.x), hy = __floats2bfloat162_rn(v0.y, v1.y);
+            *reinterpret_cast<__nv_bfloat162 *>(hre + t) = hx;
+            *reinterpret_cast<__nv_bfloat162 *>(him + t) = hy;
+            *reinterpret_cast<__nv_bfloat162 *>(lre + t) =
+                __floats2bfloat162_rn(v0.x - __low2float(hx), v1.x - __high2float(hx));
+            *reinterpret_cast<__nv_bfloat162 *>(lim + t) =
+                __floats2bfloat162_rn(v0.y - __low2float(hy), v1.y - __high2float(hy));
+        }
+        return;
+    }
+    const int sb = f16_field_exp(a.scale, g_out);
+    const float sc = ldexpf(1.0f, sb);
+    float mx = 0.0f;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
         const float2 v0 = s[pidx(t)], v1 = s[pidx(t + 1)];
         *reinterpret_cast<float2 *>(re + t) = make_float2(v0.x, v1.x);
         *reinterpret_cast<float2 *>(im + t) = make_float2(v0.y, v1.y);
-        const __nv_bfloat162 hx = __floats2bfloat162_rn(v0.x, v1.x), hy = __floats2bfloat162_rn(v0.y, v1.y);
-        *reinterpret_cast<__nv_bfloat162 *>(hre + t) = hx;
-        *reinterpret_cast<__nv_bfloat162 *>(him + t) = hy;
-        *reinterpret_cast<__nv_bfloat162 *>(lre + t) =
-            __floats2bfloat162_rn(v0.x - __low2float(hx), v1.x - __high2float(hx));
-        *reinterpret_cast<__nv_bfloat162 *>(lim + t) =
-            __floats2bfloat162_rn(v0.y - __low2float(hy), v1.y - __high2float(hy));
+        mx = fmaxf(mx, fmaxf(fmaxf(fabsf(v0.x), fabsf(v0.y)), fmaxf(fabsf(v1.x), fabsf(v1.y))));
+        const float x0 = v0.x * sc, x1 = v1.x * sc, y0 = v0.y * sc, y1 = v1.y * sc;
+        const __half2 hx = __floats2half2_rn(x0, x1), hy = __floats2half2_rn(y0, y1);
+        *reinterpret_cast<__half2 *>(hre + t) = hx;
+        *reinterpret_cast<__half2 *>(him + t) = hy;
+        *reinterpret_cast<__half2 *>(lre + t) = __floats2half2_rn(x0 - __low2float(hx), x1 - __high2float(hx));
+        *reinterpret_cast<__half2 *>(lim + t) = __floats2half2_rn(y0 - __low2float(hy), y1 - __high2float(hy));
+    }
+    // a finite value above 65504 after scaling overflowed its FP16 term
+    const int ovf = __syncthreads_or(isfinite(mx) && !(mx * sc <= 65504.0f));
+    mx = block_max(mx);
+    if (threadIdx.x == 0) {
+        atomicMax(&a.scale[NLSE_SC_MAX + g_out % 3], __float_as_int(mx));
+        if (ovf) atomicAdd(&a.scale[NLSE_SC_OVF], 1);
+        if (r == 0) {
+            a.scale[NLSE_SC_SB + g_out % 2] = sb;
+            a.scale[NLSE_SC_MAX + (g_out + 1) % 3] = 0;  // the slot input g_out + 1 will fill
+        }
     }
 }
 
-// s[t] = scale * P_t[t] * ((F32 + D) row r as complex), padded indexing.
+// s[t] = scale * P_t[t] * ((F32 + D) row r as complex), padded indexing.  In
+// the split-FP16 form D carries 2^(sa + sb) of input g_in, removed here.
 template <int NT>
 __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs &a, const float *F32,
-                                            const float *D, float scale) {
+                                            const float *D, float scale, int g_in) {
+    const float ds = a.f16 ? ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) +
+                                            __ldcg(&a.scale[NLSE_SC_SB + g_in % 2])))
+                           : 1.0f;
     const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nr + r) * NT;
     const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nr + r) * NT;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
         const float2 xr = *reinterpret_cast<const float2 *>(fr + t), xi = *reinterpret_cast<const float2 *>(fi + t);
         const float2 yr = *reinterpret_cast<const float2 *>(dr + t), yi = *reinterpret_cast<const float2 *>(di + t);
         const float4 pt = __ldg(reinterpret_cast<const float4 *>(a.Pt + t));
-        s[pidx(t)] = c_scale(c_mul(make_float2(xr.x + yr.x, xi.x + yi.x), make_float2(pt.x, pt.y)), scale);
-        s[pidx(t + 1)] = c_scale(c_mul(make_float2(xr.y + yr.y, xi.y + yi.y), make_float2(pt.z, pt.w)), scale);
+        s[pidx(t)] = c_scale(c_mul(make_float2(fmaf(yr.x, ds, xr.x), fmaf(yi.x, ds, xi.x)), make_float2(pt.x, pt.y)),
+                             scale);
+        s[pidx(t + 1)] =
+            c_scale(c_mul(make_float2(fmaf(yr.y, ds, xr.y), fmaf(yi.y, ds, xi.y)), make_float2(pt.z, pt.w)), scale);
     }
 }
 
@@ -103,7 +167,7 @@ __device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, con
     }
     __syncthreads();
     float2 *R = fft_row<NT, false>(b0, b1, a.tw);
-    store_state_row<NT>(R, r, a, F32, Fb);
+    store_state_row<NT>(R, r, a, F32, Fb, 0);
     if (!do_scan) return;
     __syncthreads();
     // the march needs the physical field: reload it into the free buffer
@@ -117,10 +181,10 @@ __device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, con
 template <int NT>
 __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
                                             __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-                                            const float *__restrict__ rho) {
+                                            const float *__restrict__ rho, int g) {
     extern __shared__ float2 sm2[];
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
-    load_mw_row<NT>(b0, r, a, F32, D, 1.0f / (float)NT);
+    load_mw_row<NT>(b0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
     float2 *R = fft_row<NT, true>(b0, b1, a.tw);
     const float *gr = rho + (size_t)r * NT;
@@ -133,7 +197,7 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
     }
     __syncthreads();
     float2 *Y = fft_row<NT, false>(R, R == b0 ? b1 : b0, a.tw);
-    store_state_row<NT>(Y, r, a, F32, Fb);
+    store_state_row<NT>(Y, r, a, F32, Fb, g + 1);
 }
 
 // Second half step's spectral end + mask_r: the next state w', and optionally
@@ -142,12 +206,12 @@ template <int NT>
 __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
                                               __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
                                               float *__restrict__ rho, float2 *__restrict__ u_out, int write_state,
-                                              int do_scan, int apply_mask) {
+                                              int do_scan, int apply_mask, int g) {
     extern __shared__ float2 sm2[];
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
-    load_mw_row<NT>(b0, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f);
+    load_mw_row<NT>(b0, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f, g);
     __syncthreads();
-    if (write_state) store_state_row<NT>(b0, r, a, F32, Fb);
+    if (write_state) store_state_row<NT>(b0, r, a, F32, Fb, g + 1);
     if (!do_scan && !u_out) return;
     float2 *R = fft_row<NT, true>(b0, b1, a.tw);
     const float inv = 1.0f / (float)NT;
@@ -167,11 +231,11 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-              const float *__restrict__ rho) {
+              const float *__restrict__ rho, int g) {
     extern __shared__ float2 sm2[];
     const FullRows m = full_rows<NT>(sm2);
     const int r = blockIdx.x;
-    load_mw_row<NT>(m.B0, r, a, F32, D, 1.0f / (float)NT);
+    load_mw_row<NT>(m.B0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
     const float2 *R = fft_row<NT, true>(m.B0, m.B1, a.tw);
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.U[t] = R[pidx(t)];
@@ -181,7 +245,7 @@ k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.B0[pidx(t)] = m.U[t];
     __syncthreads();
     float2 *Y = fft_row<NT, false>(m.B0, m.B1, a.tw);
-    store_state_row<NT>(Y, r, a, F32, Fb);
+    store_state_row<NT>(Y, r, a, F32, Fb, g + 1);
 }
 
 template <int NT>
@@ -194,15 +258,15 @@ k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F3
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-         const float *__restrict__ rho) {
-    row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho);
+         const float *__restrict__ rho, int g) {
+    row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
 }
 
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
 k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-           float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask) {
-    row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask);
+           float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask, int g) {
+    row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
 }
 
 // ------------------------------------------------------------------ batched (many pulses, one time-grid class)
@@ -217,18 +281,18 @@ k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, i
 
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
-k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work) {
+k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
-    row_nl_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho);
+    row_nl_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, g);
 }
 
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
-k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last) {
+k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
-    row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1);
+    row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1, g);
 }
 
 template <typename K>
@@ -250,41 +314,41 @@ cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32,
 }
 
 cudaError_t launch_row_nl_full(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
-                               const float *rho, cudaStream_t st) {
+                               const float *rho, int g, cudaStream_t st) {
     NLSE_DISPATCH_NT_FULL(a.logNt, {
         const size_t smem = full_smem_bytes<NT>();
         cudaError_t e = set_smem(k_row_nl_full<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_nl_full<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho);
+        k_row_nl_full<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, g);
     });
     return cudaGetLastError();
 }
 
 cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,
-                          cudaStream_t st) {
+                          int g, cudaStream_t st) {
     NLSE_DISPATCH_NT(a.logNt, {
         const size_t smem = row_smem_bytes<NT>(false);
         cudaError_t e = set_smem(k_row_nl<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_nl<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho);
+        k_row_nl<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, g);
     });
     return cudaGetLastError();
 }
 
 cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, float *rho,
-                            float2 *u_out, int write_state, int do_scan, int apply_mask, cudaStream_t st) {
+                            float2 *u_out, int write_state, int do_scan, int apply_mask, int g, cudaStream_t st) {
     NLSE_DISPATCH_NT(a.logNt, {
         const size_t smem = row_smem_bytes<NT>(true);
         cudaError_t e = set_smem(k_row_next<NT>, smem);
         if (e != cudaSuccess) return e;
         k_row_next<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan,
-                                                              apply_mask);
+                                                              apply_mask, g);
     });
     return cudaGetLastError();
 }
 
 cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
-                             cudaStream_t st) {
+                             int g, cudaStream_t st) {
     NLSE_DISPATCH_NT(logNt, {
         const size_t smem = row_smem_bytes<NT>(kind != 1);
         cudaError_t e;
@@ -295,13 +359,33 @@ cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int
         } else if (kind == 1) {
             e = set_smem(k_row_nl_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work);
+            k_row_nl_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, g);
         } else {
             e = set_smem(k_row_next_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_next_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, flag);
+            k_row_next_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, flag, g);
         }
     });
+    return cudaGetLastError();
+}
+
+// Split-FP16 form: before the entry kernel writes GEMM input 0 = F[u], its
+// "previous maximum" is the bound Nt max |u| >= max |F[u]| (slot 2), and the
+// slot input 0 fills is cleared.
+__global__ void k_field_bound(const float2 *__restrict__ u, size_t n, int Nt, int *__restrict__ scale) {
+    float mx = 0.0f;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        const float2 v = u[i];
+        mx = fmaxf(mx, fmaxf(fabsf(v.x), fabsf(v.y)));
+    }
+    mx = block_max(mx);
+    if (threadIdx.x == 0) atomicMax(&scale[NLSE_SC_MAX + 2], __float_as_int(mx * (float)Nt * 1.5f));
+}
+
+cudaError_t launch_field_bound(const float2 *u, size_t n, int Nt, int *scale, cudaStream_t st) {
+    cudaError_t e = cudaMemsetAsync(scale + NLSE_SC_MAX, 0, 3 * sizeof(int), st);
+    if (e != cudaSuccess) return e;
+    k_field_bound<<<2 * 152, NLSE_ROW_THREADS, 0, st>>>(u, n, Nt, scale);
     return cudaGetLastError();
 }
 

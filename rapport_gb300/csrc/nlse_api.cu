@@ -60,7 +60,7 @@ static void free_ctx(nlse_ctx *c) {
     prof_free(c);
     void *ptrs[] = {c->d_tw,    c->d_Y,   c->d_Y64, c->d_rho_modes, c->d_delta_k, c->d_spec_mask,
                     c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_lut_s_dt, c->d_Rf, c->d_Tss, c->d_invUnl, c->d_invUop, c->d_P2, c->d_Pt,   c->d_Pr,     c->d_work,
-                    c->d_flag,  c->d_Er,  c->d_Ei,  c->d_A,  c->d_F32, c->d_Fb,  c->d_D,   c->d_Ptf};
+                    c->d_flag,  c->d_scale, c->d_Er,  c->d_Ei,  c->d_A,  c->d_F32, c->d_Fb,  c->d_D,   c->d_Ptf};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free(c);
@@ -321,6 +321,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     NLSE_TRY(dev_upload<float2>(err, &c->d_Pr, nullptr, Nr));
     NLSE_TRY(dev_upload<float2>(err, &c->d_work, nullptr, (size_t)Nr * Nt));
     NLSE_TRY(dev_upload<int>(err, &c->d_flag, nullptr, 4));
+    NLSE_TRY(dev_upload<int>(err, &c->d_scale, nullptr, NLSE_SC_N));
     // split-BF16 path: operator terms, Omega-domain state, tensor maps
     c->a_terms = 3;
     c->cached_dz_op = NAN;
@@ -401,6 +402,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
         }
     }
     ce = cudaMemset(c->d_flag, 0, 4 * sizeof(int));
+    if (ce == cudaSuccess) ce = cudaMemset(c->d_scale, 0, NLSE_SC_N * sizeof(int));
     if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
     if (ce != cudaSuccess) {
         nlse_set_error(err, NLSE_ERR_CUDA, "context init: %s", cudaGetErrorString(ce));
@@ -505,7 +507,7 @@ static int half_linear_impl(nlse_ctx *c, float2 *u, double dz, const float *row_
 // ---------------------------------------------------------------- split-BF16 path
 static int autotune_gemm(nlse_ctx *c, cudaStream_t st);
 
-static int split_ready(nlse_ctx *c, double dz, cudaStream_t st) {
+static int split_ready(nlse_ctx *c, double dz, int f16, cudaStream_t st) {
     if (!c->split_ok)
         return bad(c, NLSE_ERR_UNSUPPORTED,
                    "split-BF16 mode needs Nr % 64 == 0 and Nt % 256 == 0 (this grid: use the plain mode)");
@@ -515,14 +517,17 @@ static int split_ready(nlse_ctx *c, double dz, cudaStream_t st) {
                    "single radial operator for the split-BF16 product: use the plain mode");
     int s = ensure_tables(c, dz, st);
     if (s) return s;
-    if (dz == c->cached_dz_op) return NLSE_OK;
+    if (dz == c->cached_dz_op && f16 == c->op_f16) return NLSE_OK;
     {
         PROF(K_BUILD_OP);
         s = launched(c, launch_build_operator(c->d_Y64, c->d_rho_modes, c->Nr, dz, c->komega, c->d_Er, c->d_Ei, 3,
-                                              c->d_A, st),
+                                              c->d_A, f16, c->d_scale, st),
                      "operator build");
     }
-    if (s == NLSE_OK) c->cached_dz_op = dz;
+    if (s == NLSE_OK) {
+        c->cached_dz_op = dz;
+        c->op_f16 = f16;
+    }
     if (s == NLSE_OK) s = autotune_gemm(c, st);
     return s;
 }
@@ -543,13 +548,15 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
     a.stats = c->d_flag;
     a.rho_s = nullptr;
     a.ft = FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf};
+    a.f16 = c->op_f16;
+    a.scale = c->d_scale;
     return a;
 }
 
 static cudaError_t tc_gemm_raw(nlse_ctx *c, int variant, cudaStream_t st) {
     const int K2 = 2 * c->Nr;
     const CUtensorMap *a = variant ? &c->tmA32 : &c->tmA, *b = variant ? &c->tmB32 : &c->tmB;
-    return launch_gemm_tc(a, b, c->d_D, K2, c->Nt, K2, c->a_terms, variant, c->d_flag, st);
+    return launch_gemm_tc(a, b, c->d_D, K2, c->Nt, K2, c->a_terms, variant, c->op_f16, c->d_flag, st);
 }
 
 static int tc_gemm(nlse_ctx *c, cudaStream_t st) {
@@ -594,47 +601,58 @@ static int autotune_gemm(nlse_ctx *c, cudaStream_t st) {
     return NLSE_OK;
 }
 
-static int row_entry(nlse_ctx *c, const RowFusedArgs &a, const float2 *u, float *rho, int scan, cudaStream_t st) {
-    PROF(K_ROW_ENTRY);
-    return launched(c, launch_row_entry(a, u, c->d_F32, c->d_Fb, rho, scan, st), "row entry");
-}
-
-static int row_nl(nlse_ctx *c, const RowFusedArgs &a, const float *rho, cudaStream_t st) {
-    PROF(K_ROW_NL);
-    if (c->full_nl) return launched(c, launch_row_nl_full(a, c->d_F32, c->d_Fb, c->d_D, rho, st), "row nonlinear");
-    return launched(c, launch_row_nl(a, c->d_F32, c->d_Fb, c->d_D, rho, st), "row nonlinear");
-}
-
-static int row_next(nlse_ctx *c, const RowFusedArgs &a, float *rho, float2 *u_out, int write_state, int scan,
-                    int mask, cudaStream_t st) {
-    PROF(K_ROW_NEXT);
-    return launched(c, launch_row_next(a, c->d_F32, c->d_Fb, c->d_D, rho, u_out, write_state, scan, mask, st),
-                    "row next");
-}
-
 #define NLSE_SEQ(x)              \
     do {                         \
         int s_ = (x);            \
         if (s_) return s_;       \
     } while (0)
 
-static int half_linear_split(nlse_ctx *c, float2 *u, double dz, cudaStream_t st) {
-    NLSE_SEQ(split_ready(c, dz, st));
+// The entry writes GEMM input 0; in the split-FP16 form its scale comes from
+// a bound of the physical field computed just before.
+static int row_entry(nlse_ctx *c, const RowFusedArgs &a, const float2 *u, float *rho, int scan, cudaStream_t st) {
+    if (a.f16)
+        NLSE_SEQ(launched(c, launch_field_bound(u, (size_t)c->Nr * c->Nt, c->Nt, c->d_scale, st), "field bound"));
+    PROF(K_ROW_ENTRY);
+    return launched(c, launch_row_entry(a, u, c->d_F32, c->d_Fb, rho, scan, st), "row entry");
+}
+
+// g: the GEMM input whose product the kernel consumes (it writes input g + 1)
+static int row_nl(nlse_ctx *c, const RowFusedArgs &a, const float *rho, int g, cudaStream_t st) {
+    PROF(K_ROW_NL);
+    if (c->full_nl)
+        return launched(c, launch_row_nl_full(a, c->d_F32, c->d_Fb, c->d_D, rho, g, st), "row nonlinear");
+    return launched(c, launch_row_nl(a, c->d_F32, c->d_Fb, c->d_D, rho, g, st), "row nonlinear");
+}
+
+static int row_next(nlse_ctx *c, const RowFusedArgs &a, float *rho, float2 *u_out, int write_state, int scan,
+                    int mask, int g, cudaStream_t st) {
+    PROF(K_ROW_NEXT);
+    return launched(c, launch_row_next(a, c->d_F32, c->d_Fb, c->d_D, rho, u_out, write_state, scan, mask, g, st),
+                    "row next");
+}
+
+
+// f16: the split-FP16 form (otherwise split-BF16).  GEMM inputs are numbered
+// per call: the entry writes input 0, each row_nl / row_next consumes input g
+// and (when it writes the state) produces g + 1.
+static int half_linear_split(nlse_ctx *c, float2 *u, double dz, int f16, cudaStream_t st) {
+    NLSE_SEQ(split_ready(c, dz, f16, st));
     RowFusedArgs a = row_args(c, dz);
     NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
     NLSE_SEQ(tc_gemm(c, st));
-    return row_next(c, a, nullptr, u, 0, 0, 0, st);
+    return row_next(c, a, nullptr, u, 0, 0, 0, 0, st);
 }
 
-static int step_split(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, double dz, cudaStream_t st) {
-    NLSE_SEQ(split_ready(c, dz, st));
+static int step_split(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, double dz, int f16,
+                      cudaStream_t st) {
+    NLSE_SEQ(split_ready(c, dz, f16, st));
     RowFusedArgs a = row_args(c, dz);
     a.rho_s = c->sc.ste ? rho_s : nullptr;
     NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
     NLSE_SEQ(tc_gemm(c, st));
-    NLSE_SEQ(row_nl(c, a, rho, st));
+    NLSE_SEQ(row_nl(c, a, rho, 0, st));
     NLSE_SEQ(tc_gemm(c, st));
-    return row_next(c, a, nullptr, u, 0, 0, 1, st);
+    return row_next(c, a, nullptr, u, 0, 0, 1, 1, st);
 }
 
 static int rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s, cudaStream_t st) {
@@ -654,17 +672,18 @@ static int propagate_split_ste(nlse_ctx *c, float2 *u, float *rho, float *rho_s,
     for (int i = 0; i < n; ++i) {
         const bool last = i == n - 1;
         NLSE_SEQ(tc_gemm(c, st));
-        NLSE_SEQ(row_nl(c, a, rho, st));
+        NLSE_SEQ(row_nl(c, a, rho, 2 * i, st));
         NLSE_SEQ(tc_gemm(c, st));
-        NLSE_SEQ(row_next(c, a, nullptr, last ? u : c->d_work, last ? 0 : 1, 0, 1, st));
+        NLSE_SEQ(row_next(c, a, nullptr, last ? u : c->d_work, last ? 0 : 1, 0, 1, 2 * i + 1, st));
         if (!last) NLSE_SEQ(rate_scan(c, c->d_work, rho, rho_s, st));
     }
     return NLSE_OK;
 }
 
-static int propagate_split(nlse_ctx *c, float2 *u, float *rho, float *rho_s, double dz, int n, cudaStream_t st) {
+static int propagate_split(nlse_ctx *c, float2 *u, float *rho, float *rho_s, double dz, int n, int f16,
+                           cudaStream_t st) {
     if (n == 0) return NLSE_OK;
-    NLSE_SEQ(split_ready(c, dz, st));
+    NLSE_SEQ(split_ready(c, dz, f16, st));
     if (c->sc.ste) return propagate_split_ste(c, u, rho, rho_s, dz, n, st);
     RowFusedArgs a = row_args(c, dz);
     if (rho_s)
@@ -673,9 +692,9 @@ static int propagate_split(nlse_ctx *c, float2 *u, float *rho, float *rho_s, dou
     for (int i = 0; i < n; ++i) {
         const bool last = i == n - 1;
         NLSE_SEQ(tc_gemm(c, st));
-        NLSE_SEQ(row_nl(c, a, rho, st));
+        NLSE_SEQ(row_nl(c, a, rho, 2 * i, st));
         NLSE_SEQ(tc_gemm(c, st));
-        NLSE_SEQ(row_next(c, a, rho, last ? u : nullptr, last ? 0 : 1, last ? 0 : 1, 1, st));
+        NLSE_SEQ(row_next(c, a, rho, last ? u : nullptr, last ? 0 : 1, last ? 0 : 1, 1, 2 * i + 1, st));
     }
     return NLSE_OK;
 }
@@ -688,7 +707,8 @@ extern "C" int nlse_half_linear(nlse_ctx *c, void *u, double dz, void *stream) {
 extern "C" int nlse_half_linear_ex(nlse_ctx *c, void *u, double dz, int mode, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u")) return NLSE_ERR_INVALID_ARG;
-    if (mode == NLSE_MODE_SPLIT_BF16) return half_linear_split(c, (float2 *)u, dz, (cudaStream_t)stream);
+    if (mode == NLSE_MODE_SPLIT_BF16 || mode == NLSE_MODE_SPLIT_F16)
+        return half_linear_split(c, (float2 *)u, dz, mode == NLSE_MODE_SPLIT_F16, (cudaStream_t)stream);
     if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
     return half_linear_impl(c, (float2 *)u, dz, nullptr, (cudaStream_t)stream);
 }
@@ -768,7 +788,8 @@ extern "C" int nlse_step(nlse_ctx *c, void *u, const float *rho, const float *rh
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho")) return NLSE_ERR_INVALID_ARG;
     if (c->sc.ste && rho_s && !field_ok(c, rho_s, "rho_s")) return NLSE_ERR_INVALID_ARG;
-    if (mode == NLSE_MODE_SPLIT_BF16) return step_split(c, (float2 *)u, rho, rho_s, dz, (cudaStream_t)stream);
+    if (mode == NLSE_MODE_SPLIT_BF16 || mode == NLSE_MODE_SPLIT_F16)
+        return step_split(c, (float2 *)u, rho, rho_s, dz, mode == NLSE_MODE_SPLIT_F16, (cudaStream_t)stream);
     if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
     return step_plain(c, (float2 *)u, rho, rho_s, dz, (cudaStream_t)stream);
 }
@@ -779,7 +800,8 @@ extern "C" int nlse_propagate(nlse_ctx *c, void *u, float *rho, float *rho_s, do
     if (!field_ok(c, u, "u") || !field_ok(c, rho, "rho") || !ste_ok(c, rho_s)) return NLSE_ERR_INVALID_ARG;
     if (nsteps < 0) return bad(c, NLSE_ERR_INVALID_ARG, "nsteps < 0");
     cudaStream_t st = (cudaStream_t)stream;
-    if (mode == NLSE_MODE_SPLIT_BF16) return propagate_split(c, (float2 *)u, rho, rho_s, dz, nsteps, st);
+    if (mode == NLSE_MODE_SPLIT_BF16 || mode == NLSE_MODE_SPLIT_F16)
+        return propagate_split(c, (float2 *)u, rho, rho_s, dz, nsteps, mode == NLSE_MODE_SPLIT_F16, st);
     if (mode != NLSE_MODE_PLAIN_F32) return bad(c, NLSE_ERR_INVALID_ARG, "unknown mode");
     for (int i = 0; i < nsteps; ++i) {
         NLSE_SEQ(rate_scan(c, (const float2 *)u, rho, rho_s, st));
@@ -807,7 +829,7 @@ extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *o
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, w, "w") || !field_ok(c, out, "out")) return NLSE_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
-    NLSE_SEQ(split_ready(c, dz, st));
+    NLSE_SEQ(split_ready(c, dz, 0, st));
     const size_t n = 2 * (size_t)c->Nr * c->Nt;
     NLSE_SEQ(launched(c, launch_split_field(w, c->d_Fb, n, st), "split field"));
     NLSE_SEQ(tc_gemm(c, st));
@@ -845,10 +867,19 @@ extern "C" int nlse_device_status(nlse_ctx *c, int *word) {
     if (!c) return NLSE_ERR_INVALID_ARG;
     int h[4];
     NLSE_CUDA_TRY(&c->err, cudaMemcpy(h, c->d_flag, sizeof(h), cudaMemcpyDeviceToHost));
+    int sc[NLSE_SC_N];
+    NLSE_CUDA_TRY(&c->err, cudaMemcpy(sc, c->d_scale, sizeof(sc), cudaMemcpyDeviceToHost));
     if (word) *word = h[0];
     if (h[0]) {
         nlse_set_error(&c->err, NLSE_ERR_TIMEOUT, "a bounded device wait gave up (status word 0x%x)", h[0]);
         return NLSE_ERR_TIMEOUT;
+    }
+    if (sc[NLSE_SC_OVF]) {
+        nlse_set_error(&c->err, NLSE_ERR_DEVICE_FLAG,
+                       "split-FP16 form: %d row writes overflowed FP16 (the field grew more than 512-fold in a half "
+                       "step); use the split-BF16 form",
+                       sc[NLSE_SC_OVF]);
+        return NLSE_ERR_DEVICE_FLAG;
     }
     return NLSE_OK;
 }
@@ -922,6 +953,8 @@ extern "C" const char *nlse_kernel_name(int kid) {
 struct nlse_batch {
     nlse_error_slot err;
     int n, a_terms;
+    int f16;                 // split-FP16 form (nlse_batch_set_mode)
+    int last_f16;            // form of the last upload
     nlse_ctx **ctx;          // one context per pulse (tables, operator, state buffers)
     BatchPulse *h_pulses;    // pinned staging of the per-pulse table
     BatchPulse *d_pulses;
@@ -1055,6 +1088,12 @@ extern "C" int nlse_batch_get_context(nlse_batch *b, int i, nlse_ctx **out) {
     return NLSE_OK;
 }
 
+extern "C" int nlse_batch_set_mode(nlse_batch *b, int mode) {
+    if (!b || (mode != NLSE_MODE_SPLIT_BF16 && mode != NLSE_MODE_SPLIT_F16)) return NLSE_ERR_INVALID_ARG;
+    b->f16 = mode == NLSE_MODE_SPLIT_F16;
+    return NLSE_OK;
+}
+
 extern "C" int nlse_batch_set_split_terms(nlse_batch *b, int a_terms) {
     if (!b || (a_terms != 2 && a_terms != 3)) return NLSE_ERR_INVALID_ARG;
     b->a_terms = a_terms;
@@ -1088,13 +1127,13 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
     if (nsteps == 0) return NLSE_OK;
     cudaStream_t st = (cudaStream_t)stream;
     nlse_ctx *c = b->ctx[0];  // profiling records go to the first pulse's context
-    bool changed = !(dz == b->last_dz) || !b->uploaded;
+    bool changed = !(dz == b->last_dz) || !b->uploaded || b->last_f16 != b->f16;
     for (int i = 0; i < b->n; ++i) {
         if (!field_ok(b->ctx[i], u[i], "u") || !field_ok(b->ctx[i], rho[i], "rho")) {
             nlse_set_error(&b->err, NLSE_ERR_INVALID_ARG, "pulse %d: %s", i, b->ctx[i]->err.msg);
             return NLSE_ERR_INVALID_ARG;
         }
-        int s = split_ready(b->ctx[i], dz, st);
+        int s = split_ready(b->ctx[i], dz, b->f16, st);
         if (s) {
             nlse_set_error(&b->err, s, "pulse %d: %s", i, b->ctx[i]->err.msg);
             return s;
@@ -1121,6 +1160,7 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
                                                cudaMemcpyHostToDevice, st));
         NLSE_CUDA_TRY(&b->err, cudaEventRecord(b->staged, st));
         b->last_dz = dz;
+        b->last_f16 = b->f16;
         b->uploaded = 1;
     }
     if (rho_s)
@@ -1137,26 +1177,35 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
             return NLSE_ERR_CUDA;                                                      \
         }                                                                              \
     } while (0)
+    if (b->f16)
+        for (int i = 0; i < b->n; ++i)
+            BSEQ(K_ROW_ENTRY,
+                 launch_field_bound((const float2 *)u[i], (size_t)b->ctx[i]->Nr * b->ctx[i]->Nt, b->ctx[i]->Nt,
+                                    b->ctx[i]->d_scale, st),
+                 "batch field bound");
     for (int k = 0; k < b->ncls; ++k)
         BSEQ(K_ROW_ENTRY,
-             launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, st),
+             launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, -1, st),
              "batch row entry");
     for (int it = 0; it < nsteps; ++it) {
         const int last = it == nsteps - 1;
         BSEQ(K_GEMM_TC,
              launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
-                                    b->d_flag, st),
+                                    b->f16, b->d_flag, st),
              "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
-            BSEQ(K_ROW_NL, launch_row_batch(1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 0, st),
+            BSEQ(K_ROW_NL,
+                 launch_row_batch(1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 0, 2 * it,
+                                  st),
                  "batch row nonlinear");
         BSEQ(K_GEMM_TC,
              launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
-                                    b->d_flag, st),
+                                    b->f16, b->d_flag, st),
              "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NEXT,
-                 launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last, st),
+                 launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last,
+                                  2 * it + 1, st),
                  "batch row next");
     }
 #undef BSEQ

@@ -83,7 +83,23 @@ struct RowFusedArgs {
     int *stats;
     const float *rho_s;   // exciton density for the nonlinear step (NULL: channel off)
     FullTabs ft;          // full-physics split tables (all NULL: the measured toggles)
+    int f16;              // split-FP16 form: scaled FP16 field terms (see NLSE_SC_*)
+    int *scale;           // the pulse's scale cells (split-FP16 form)
 };
+
+// Scale cells of the split-FP16 form (int each, per pulse):
+//   [0..2]  ring of row-maxima |w| (float bits) of the GEMM inputs g = 0, 1, ...
+//           (input g's max goes to slot g % 3; input g + 1 picks its scale from it)
+//   [3..4]  exponent sb of the field terms of input g (slot 3 + g % 2)
+//   [5]     exponent sa of the operator terms
+//   [6]     count of field values that overflowed FP16 (an error)
+//   [7]     scratch of the operator build (max |E|)
+#define NLSE_SC_MAX 0
+#define NLSE_SC_SB 3
+#define NLSE_SC_SA 5
+#define NLSE_SC_OVF 6
+#define NLSE_SC_EMAX 7
+#define NLSE_SC_N 8
 
 // One pulse of a batch, as the batched kernels see it (device memory).
 struct BatchPulse {
@@ -136,6 +152,8 @@ struct nlse_ctx {
     int *d_flag;           // device status word
     // split-BF16 path (allocated when Nr % 64 == 0 and Nt % 256 == 0)
     int split_ok, a_terms;
+    int op_f16;            // format of the operator in d_A (0: 3 BF16 terms, 1: 2 scaled FP16 terms)
+    int *d_scale;          // NLSE_SC_N scale cells of the split-FP16 form
     double cached_dz_op;   // dz of the operator currently in d_A
     double *d_Er, *d_Ei;   // Nr*Nr FP64 scratch of the builder
     __nv_bfloat16 *d_A;    // 3 x (2Nr x 2Nr) BF16 terms of E'
@@ -187,14 +205,20 @@ cudaError_t launch_nl_full(nlse_ctx *c, float2 *u, const float *rho, const float
 cudaError_t launch_split_full(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, float2 *rhs,
                               float *alpha, cudaStream_t stream);
 cudaError_t launch_row_nl_full(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
-                               const float *rho, cudaStream_t st);
+                               const float *rho, int g, cudaStream_t st);
 cudaError_t launch_phase_table_2d(nlse_ctx *c, double dz, cudaStream_t stream);
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s,
                              int zero_first, cudaStream_t stream);
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
-                           int a_terms, int variant, int *err, cudaStream_t stream);
+                           int a_terms, int variant, int f16, int *err, cudaStream_t stream);
+// Builds E in FP64 and splits it: 3 (or a_terms) BF16 terms, or with f16 two
+// FP16 terms of E 2^sa (sa from max |E|, stored in scale[NLSE_SC_SA]).
 cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
-                                  double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, cudaStream_t stream);
+                                  double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, int f16, int *scale,
+                                  cudaStream_t stream);
+// Split-FP16 form, before the entry kernel: scale[NLSE_SC_MAX + 2] = a bound of
+// max |F[u]| (Nt max |u|, the "previous input" of input 0), slot 0 cleared.
+cudaError_t launch_field_bound(const float2 *u, size_t n, int Nt, int *scale, cudaStream_t st);
 
 cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, const float2 *tw, const float2 *Pt,
                                          const float2 *Pr, cudaStream_t stream);
@@ -202,17 +226,19 @@ void nlse_set_thread_error(int status, const char *msg);
 cudaError_t launch_record(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, const int *bin_of_t,
                           int nbins, double *out, cudaStream_t st);
 cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st);
-// kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call)
+// kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call);
+// g = index of the GEMM input the kernel consumes (the split-FP16 scales; -1 for the entry)
 cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
-                             cudaStream_t st);
+                             int g, cudaStream_t st);
 cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
-                                   int a_terms, int variant, int *err, cudaStream_t stream);
+                                   int a_terms, int variant, int f16, int *err, cudaStream_t stream);
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
                              int do_scan, cudaStream_t st);
+// g: index of the GEMM input whose product D the kernel consumes; it writes input g + 1
 cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,
-                          cudaStream_t st);
+                          int g, cudaStream_t st);
 cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, float *rho,
-                            float2 *u_out, int write_state, int do_scan, int apply_mask, cudaStream_t st);
+                            float2 *u_out, int write_state, int do_scan, int apply_mask, int g, cudaStream_t st);
 
 // ---------------------------------------------------------------- complex
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }

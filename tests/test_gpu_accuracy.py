@@ -5,7 +5,8 @@
   1e-11 over several steps -- only then is it used as the long-run reference.
 * test_one_cm_accuracy (set NLSE_LONG=1; ~3 min): the 1024 x 2048 workload
   propagated 4000 z-steps of 2.5 um (1 cm) by the FP64 reference, the plain
-  FP32 form and the split-BF16 form (3-term and 2-term operator).  Reports the
+  FP32 form, the split-BF16 form (3-term and 2-term operator) and the
+  split-FP16 form.  Reports the
   relative L2 field error, peak-fluence error and peak-rho error at 0.125,
   0.25, 0.5 and 1 cm, writes them to gpurun_out/accuracy_1cm.json when that
   folder exists, and asserts the benchmark spec's bounds for the split-BF16 form:
@@ -47,12 +48,12 @@ def _metrics(u, rho, uref, rref, dt, invE2):
 def test_one_cm_accuracy():
     import torch
     import fp64_gpu
-    from rapport_gb300._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16
+    from rapport_gb300._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16, MODE_SPLIT_F16
 
     c = Case(**CONFIG2)
     ref = fp64_gpu.FP64GPU(c.og)
     forms = {"split_bf16_3term": (MODE_SPLIT_BF16, 3), "split_bf16_2term": (MODE_SPLIT_BF16, 2),
-             "plain_fp32": (MODE_PLAIN_F32, 3)}
+             "split_f16": (MODE_SPLIT_F16, 3), "plain_fp32": (MODE_PLAIN_F32, 3)}
     state = {k: (dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))) for k in forms}
     ur = torch.tensor(c.u0, dtype=torch.complex128, device="cuda")
     rr = torch.zeros(c.u0.shape, dtype=torch.float64, device="cuda")

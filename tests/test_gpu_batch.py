@@ -116,3 +116,23 @@ def test_step_batched_equals_propagate_per_pulse(mode):
         assert np.array_equal(host(br[i]), host(rho)), i
     with pytest.raises(_lib.NLSEError, match="pulse 0: dz"):
         ctx.step_batched([(bu[0], br[0], None), (bu[1], br[1], None)], -1.0, 1, mode)
+
+
+def test_batch_f16_equals_single_contexts():
+    """The split-FP16 form in a batch: every pulse bit-identical to its single-context run."""
+    from rapport_gb300 import _lib
+    cfgs, grids, u0s, ogs = _setup()
+    b = _lib.Batch(cfgs, grids)
+    b.set_mode(_lib.MODE_SPLIT_F16)
+    us = [dev(u) for u in u0s]
+    rhos = [dev(np.zeros(u.shape)) for u in u0s]
+    b.propagate(us, rhos, None, DZ, STEPS)
+    for i, (cfg, g, u0, og) in enumerate(zip(cfgs, grids, u0s, ogs)):
+        ctx = _lib.Context(cfg, g)
+        u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+        ctx.propagate(u, rho, rs, DZ, STEPS, _lib.MODE_SPLIT_F16)
+        assert np.array_equal(host(us[i]), host(u)), i
+        assert np.array_equal(host(rhos[i]), host(rho)), i
+        uo, _, _ = og.propagate(u0.copy(), STEPS, DZ)
+        assert rel_l2(host(us[i]), uo) < 5e-5, i
+        assert ctx.device_status() == 0

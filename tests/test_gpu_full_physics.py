@@ -121,13 +121,14 @@ def test_split_bf16_without_space_time_focusing(full):
     m = meta_case(full)
     # the split form tiles Nr by 64 and Nt by 256
     c = Case(64, 256, m["R_max"], m["w0"], m["T_half"], m["fwhm"], m["E"], m["f"], m["dz"], 4, 0, **NO_STF)
-    u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
-    c.ctx.propagate(u, rho, rs, c.dz, 4, _lib.MODE_SPLIT_BF16)
     uo, ro, so = c.og.propagate(c.u0.copy(), 4, c.dz)
-    assert rel_l2(host(u), uo) < 5e-5
-    assert np.abs(host(rho) - ro).max() <= 1e-3 * ro.max()
-    assert np.abs(host(rs) - so).max() <= 1e-3 * so.max()
-    assert c.ctx.device_status() == 0
+    for mode in (_lib.MODE_SPLIT_BF16, _lib.MODE_SPLIT_F16):
+        u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+        c.ctx.propagate(u, rho, rs, c.dz, 4, mode)
+        assert rel_l2(host(u), uo) < 5e-5, mode
+        assert np.abs(host(rho) - ro).max() <= 1e-3 * ro.max(), mode
+        assert np.abs(host(rs) - so).max() <= 1e-3 * so.max(), mode
+        assert c.ctx.device_status() == 0
     s = Case(64, 256, m["R_max"], m["w0"], m["T_half"], m["fwhm"], m["E"], m["f"], m["dz"], 1, 0, **FULL_PHYSICS)
     with pytest.raises(_lib.NLSEError, match="space-time focusing"):
         s.ctx.propagate(dev(s.u0), dev(np.zeros(s.u0.shape)), dev(np.zeros(s.u0.shape)), s.dz, 1,

@@ -1,16 +1,21 @@
-"""The split-BF16 tensor-core path (tcgen05 + TMA) against FP64.
+"""The tensor-core split forms (tcgen05 + TMA) against FP64: split-BF16
+(3-term operator, hi/lo field, 4 MMAs) and split-FP16 (operator and field
+each in 2 scaled FP16 terms, 3 MMAs).
 
 Tolerances: the operator product E'w is exact to ~2^-17 of |E'||w| per
 element (BF16 hi/lo field, 3-term operator); whole half steps and z-steps
 must stay within 2e-5 relative L2 of the FP64 oracle (the FP32 plain path's
-bar), and the device status word must stay clear (no bounded wait gave up).
+bar), and the device status word must stay clear (no bounded wait gave up,
+no FP16 overflow).
 """
 import numpy as np
 import pytest
 
 from conftest import rel_l2
 from gpu_util import CONFIG2, Case, dev, host
-from rapport_gb300._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16
+from rapport_gb300._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16, MODE_SPLIT_F16
+
+SPLIT_MODES = [MODE_SPLIT_BF16, MODE_SPLIT_F16]
 
 pytestmark = pytest.mark.gpu
 
@@ -71,11 +76,12 @@ def test_gemm_variants_agree_bitwise(c1):
     assert np.array_equal(outs[0], outs[1])
 
 
+@pytest.mark.parametrize("mode", SPLIT_MODES)
 @pytest.mark.parametrize("name", ["small", "c1"])
-def test_half_linear_split(name, small, c1):
+def test_half_linear_split(name, mode, small, c1):
     c = small if name == "small" else c1
     u = dev(c.u0)
-    c.ctx.half_linear(u, c.dz, MODE_SPLIT_BF16)
+    c.ctx.half_linear(u, c.dz, mode)
     assert rel_l2(host(u), c.og.half_linear(c.u0, c.dz)) < 2e-5
     assert c.ctx.device_status() == 0
 
@@ -96,13 +102,37 @@ def test_propagate_split_vs_oracle(small, terms):
         c.ctx.set_split_terms(3)
 
 
-def test_step_split_equals_plain_within_fp32(small):
+def test_propagate_split_f16_vs_oracle(small, c1):
+    for c in (small, c1):
+        u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.ones(c.u0.shape))
+        c.ctx.propagate(u, rho, rs, c.dz, 10, MODE_SPLIT_F16)
+        uo, rho_o, _ = c.og.propagate(c.u0.copy(), 10, c.dz)
+        assert rel_l2(host(u), uo) < 5e-5
+        assert np.abs(host(rho) - rho_o).max() <= 1e-3 * rho_o.max()
+        assert np.all(host(rs) == 0)
+        assert c.ctx.device_status() == 0
+
+
+def test_split_forms_switch_on_one_context(small):
+    """The operator is rebuilt when the form changes; results do not depend on the order."""
+    c = small
+    outs = {}
+    for mode in (MODE_SPLIT_F16, MODE_SPLIT_BF16, MODE_SPLIT_F16):
+        u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+        c.ctx.propagate(u, rho, rs, c.dz, 3, mode)
+        outs.setdefault(mode, []).append(host(u))
+    assert np.array_equal(outs[MODE_SPLIT_F16][0], outs[MODE_SPLIT_F16][1])
+    assert rel_l2(outs[MODE_SPLIT_F16][0], outs[MODE_SPLIT_BF16][0]) < 2e-5
+
+
+@pytest.mark.parametrize("mode", SPLIT_MODES)
+def test_step_split_equals_plain_within_fp32(small, mode):
     c = small
     rho = np.zeros(c.u0.shape)
     c.og.update_plasma(c.u0, rho, np.zeros(c.u0.shape))
     u1, u2 = dev(c.u0), dev(c.u0)
     c.ctx.step(u1, dev(rho), c.dz, MODE_PLAIN_F32)
-    c.ctx.step(u2, dev(rho), c.dz, MODE_SPLIT_BF16)
+    c.ctx.step(u2, dev(rho), c.dz, mode)
     ref = c.og.step(c.u0, rho, np.zeros(c.u0.shape), c.dz)
     assert rel_l2(host(u1), ref) < 2e-5
     assert rel_l2(host(u2), ref) < 2e-5
@@ -117,9 +147,10 @@ def test_split_rejects_unsupported_grid(tiny):
 
 def test_config2_z_steps_split_vs_oracle():
     c = Case(**CONFIG2)
-    u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
-    c.ctx.propagate(u, rho, rs, c.dz, 2, MODE_SPLIT_BF16)
     uo, rho_o, _ = c.og.propagate(c.u0.copy(), 2, c.dz)
-    assert rel_l2(host(u), uo) < 2e-5
-    assert np.abs(host(rho) - rho_o).max() <= 1e-3 * max(rho_o.max(), 1e-30)
-    assert c.ctx.device_status() == 0
+    for mode in SPLIT_MODES:
+        u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+        c.ctx.propagate(u, rho, rs, c.dz, 2, mode)
+        assert rel_l2(host(u), uo) < 2e-5, mode
+        assert np.abs(host(rho) - rho_o).max() <= 1e-3 * max(rho_o.max(), 1e-30), mode
+        assert c.ctx.device_status() == 0
