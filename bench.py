@@ -111,8 +111,8 @@ def run_ours(args, rank, world, local_rank):
     ctx = _lib.Context(cfg, g)
     u0 = R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"])(g["rr"], g["tt"], cfg, g)
     u0 = np.ascontiguousarray(u0.astype(np.complex64))
-    modes = {"plain": _lib.MODE_PLAIN_F32, "split_bf16": _lib.MODE_SPLIT_BF16}
-    want = ["split_bf16", "plain"] if args.mode == "auto" else [args.mode]
+    modes = {"plain": _lib.MODE_PLAIN_F32, "split_bf16": _lib.MODE_SPLIT_BF16, "split_f16": _lib.MODE_SPLIT_F16}
+    want = ["split_bf16", "split_f16", "plain"] if args.mode == "auto" else [args.mode]
 
     def barrier():
         if world > 1:
@@ -175,11 +175,14 @@ def run_ours(args, rank, world, local_rank):
     # one grouped tensor-core launch per half step over all their tiles.
     hbm, bf16, bf16_s, src = peaks()
     Nr, Nt = w["Nr"], w["Nt"]
-    B = args.batch if head == "split_bf16" else 0
+    B = args.batch if head in ("split_bf16", "split_f16") else 0
+    bmode = args.batch_mode if args.mode == "auto" else head
+    other_batched = {}
     if B > 0:
         envs = [np.ascontiguousarray(R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"] + i)(
             g["rr"], g["tt"], cfg, g).astype(np.complex64)) for i in range(B)]
         bt = _lib.Batch([cfg] * B, [g] * B)
+        bt.set_mode(modes[bmode])
         bu = [torch.from_numpy(e).to(dev) for e in envs]
         br = [torch.zeros(u0.shape, dtype=torch.float32, device=dev) for _ in range(B)]
         bt.propagate(bu, br, None, w["dz"], 1)
@@ -237,9 +240,25 @@ def run_ours(args, rank, world, local_rank):
         e2e = {"value": world * B * K * Z / (e_ms * 1e-3), "unit": "z-steps/s",
                "h2d_bytes_per_step": int(sum(x.numel() * 8 for x in uh)),
                "d2h_bytes_per_step": int(sum(x.numel() * 8 for x in uo) + sum(x.numel() * 4 for x in rh))}
+        # the other tensor-core form on the same batch, for the forms table
+        for oname in [m for m in ("split_bf16", "split_f16") if m != bmode and args.mode == "auto"]:
+            bt.set_mode(modes[oname])
+            bt.propagate(bu, br, None, w["dz"], Z)
+            K2 = max(2, K // 2)
+            oev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K2)]
+            torch.cuda.synchronize()
+            for i in range(K2):
+                flush.fill_(float(i))
+                oev[i][0].record()
+                bt.propagate(bu, br, None, w["dz"], Z)
+                oev[i][1].record()
+            torch.cuda.synchronize()
+            assert bt.device_status() == 0
+            o_ms = sum(a.elapsed_time(b_) for a, b_ in oev)
+            other_batched[oname + "_batched"] = round(world * B * K2 * Z / (o_ms * 1e-3), 1)
         del bt, bu, br
         gemm_flops = B * 8.0 * Nr * Nr * Nt          # one grouped launch, algorithmic
-        form = f"split_bf16 batched ({B} pulses of {Nr}x{Nt})"
+        form = f"{bmode} batched ({B} pulses of {Nr}x{Nt})"
         ms_per_step = t_ms / K
     else:
         # single-pulse form only (split-BF16 unavailable): e2e through the single-context call
@@ -266,8 +285,9 @@ def run_ours(args, rank, world, local_rank):
         e2e = {"value": world * K * Z / (e_ms * 1e-3), "unit": "z-steps/s",
                "h2d_bytes_per_step": int(uh.numel() * 8),
                "d2h_bytes_per_step": int(uo.numel() * 8 + rho_h.numel() * 4)}
-        gemm_flops = (8.0 if head == "split_bf16" else 4.0) * Nr * Nr * Nt
+        gemm_flops = (8.0 if head.startswith("split") else 4.0) * Nr * Nr * Nt
         form = head
+        bmode = head
         ms_per_step = r["t_ms"] / r["K"]
 
     # ---------------------------------------------------------- roofline of the dominant kernel
@@ -285,7 +305,7 @@ def run_ours(args, rank, world, local_rank):
         roof = {"kernel": top, "bound": "tensor", "achieved": ach, "peak": bf16_s, "unit": "TFLOP/s",
                 "frac": ach / bf16_s, "traffic": traffic, "peak_source": f"bf16_tflops_sustained ({src})",
                 "per_launch": f"{gemm_flops:.3e} algorithmic FLOPs, avg {avg_s * 1e6:.1f} us over {n_launch} launches",
-                "executed_bf16_tflops": 4 * ach if top == "k_gemm_tc" else None}
+                "executed_tensor_tflops": (3 if bmode == "split_f16" else 4) * ach if top == "k_gemm_tc" else None}
     else:
         npts = (B if B > 0 else 1) * Nr * Nt
         byts = {"k_row_nl": 36.0, "k_row_next": 36.0, "k_rate_scan": 12.0, "k_nonlinear_step": 20.0,
@@ -298,7 +318,8 @@ def run_ours(args, rank, world, local_rank):
     line = {
         "metric": METRIC, "value": value, "unit": "z-steps/s", "n_gpus": world, "steps": K,
         "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "bf16x3-split + f32" if head == "split_bf16" else "f32",
+        "vs_baseline": None,
+        "dtype": {"split_bf16": "bf16x3-split + f32", "split_f16": "f16x2-split + f32"}.get(bmode, "f32"),
         "data": "synthetic (seeded lens-focused Gaussian pulses with 1% noise)",
         "config": dict(CONFIG, form=form, pulses=max(B, 1), z_steps_per_step=Z, parallelism=f"replicas{world}",
                        l2="256 MB flush before each timed step (outside its events); per pulse 24 MB",
@@ -308,7 +329,7 @@ def run_ours(args, rank, world, local_rank):
         "clocks": clocks,
         "forms": dict({k + "_single_pulse": (round(v["zsteps_per_s"], 1) if "zsteps_per_s" in v else v)
                        for k, v in results.items()},
-                      **({"split_bf16_batched": round(value, 1)} if B > 0 else {})),
+                      **({bmode + "_batched": round(value, 1)} if B > 0 else {}), **other_batched),
         "speedup_vs_plain_fp32": (value / results["plain"]["zsteps_per_s"])
         if "zsteps_per_s" in results.get("plain", {}) else None,
     }
@@ -468,7 +489,9 @@ def main():
     ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--mode", default="auto", choices=["auto", "plain", "split_bf16"])
+    ap.add_argument("--mode", default="auto", choices=["auto", "plain", "split_bf16", "split_f16"])
+    ap.add_argument("--batch-mode", default="split_bf16", choices=["split_bf16", "split_f16"],
+                    help="tensor-core form of the batched headline (auto mode)")
     ap.add_argument("--zsteps", type=int, default=50, help="z-steps per bench step")
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -274,7 +274,7 @@ const char *nlse_kernel_name(int kind);
  *   Pr  device, Nr complex64: exp(-i rho_m^2 dz / (4 k0)),
  *   u   device, Nr x Nt complex64, transformed in place (16-byte aligned).
  * Its intermediate field and twiddles live in a static device array of
- * 4 MiB + 101 KiB that each GPU loading the library holds until exit, so
+ * 4 MiB + 201 KiB that each GPU loading the library holds until exit, so
  * Nr * Nt must not exceed 524288 (larger sizes are rejected with
  * NLSE_ERR_INVALID_ARG).  The array's address is looked up on the first call
  * on each device (make that call before any stream capture); all calls share

@@ -197,7 +197,7 @@ __device__ __forceinline__ void nl_block_full(const FullRows &m, const float *__
         const float2 u = U[t];
         const float r = __ldg(&rho[t]);
         const float al = alpha_from(photo_term(fmaf(u.x, u.x, u.y * u.y), r, p, tab), r, p);
-        U[t] = S[t] = c_scale(u, expf(-hdz * al));
+        U[t] = S[t] = c_damp(u, -hdz * al);
     }
     // k1..k4; KS = k1 + 2 k2 + 2 k3 + k4 (each thread touches only its points)
     rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) {
@@ -218,7 +218,7 @@ __device__ __forceinline__ void nl_block_full(const FullRows &m, const float *__
         float2 u = make_float2(fmaf(s6, KS[t].x, U[t].x), fmaf(s6, KS[t].y, U[t].y));
         const float r = __ldg(&rho[t]);
         const float al = alpha_from(photo_term(fmaf(u.x, u.x, u.y * u.y), r, p, tab), r, p);
-        U[t] = c_scale(u, expf(-hdz * al));
+        U[t] = c_damp(u, -hdz * al);
     }
     __syncthreads();
 }

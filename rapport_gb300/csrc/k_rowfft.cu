@@ -11,7 +11,8 @@
 
 // Per-dz phase tables, computed in FP64 on the device and rounded once:
 //   Pt[k]  = exp(i delta_k[k] dz/2) * spec_mask[k] * Rk*iRk / Nt   (1/Nt = ifft norm)
-//   Ptf[k] = the same without 1/Nt (split-BF16 path; may be NULL)
+//   Ptf[k] = the same without 1/Nt (split path; may be NULL), and in
+//            Ptf[Nt + k] its FP32 rounding remainder (P - (float)P)
 //   Pr[m]  = exp(-i rho_m^2 dz / (4 k0))
 __global__ void k_phase_tables(const double *__restrict__ delta_k, const double *__restrict__ spec_mask,
                                const double *__restrict__ rho_modes, int Nt, int Nr, double dz,
@@ -24,8 +25,11 @@ __global__ void k_phase_tables(const double *__restrict__ delta_k, const double 
         double m = spec_mask[i] * scale / (double)Nt;
         Pt[i] = make_float2((float)(c * m), (float)(s * m));
         if (Ptf) {
-            double mf = spec_mask[i] * scale;
-            Ptf[i] = make_float2((float)(c * mf), (float)(s * mf));
+            // split-BF16 path: FP32 value and its rounding remainder (Ptf[Nt + i])
+            const double mf = spec_mask[i] * scale, pr = c * mf, pi = s * mf;
+            const float2 h = make_float2((float)pr, (float)pi);
+            Ptf[i] = h;
+            Ptf[Nt + i] = make_float2((float)(pr - (double)h.x), (float)(pi - (double)h.y));
         }
     }
     if (i < Nr) {

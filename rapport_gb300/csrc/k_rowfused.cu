@@ -116,10 +116,20 @@ __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs
         const float2 xr = *reinterpret_cast<const float2 *>(fr + t), xi = *reinterpret_cast<const float2 *>(fi + t);
         const float2 yr = *reinterpret_cast<const float2 *>(dr + t), yi = *reinterpret_cast<const float2 *>(di + t);
         const float4 pt = __ldg(reinterpret_cast<const float4 *>(a.Pt + t));
+#if NLSE_COMP_TWIDDLE
+        const float4 pl = __ldg(reinterpret_cast<const float4 *>(a.Pt + NT + t));
+        s[pidx(t)] = c_scale(c_mul_comp(make_float2(fmaf(yr.x, ds, xr.x), fmaf(yi.x, ds, xi.x)),
+                                        make_float2(pt.x, pt.y), make_float2(pl.x, pl.y)),
+                             scale);
+        s[pidx(t + 1)] = c_scale(c_mul_comp(make_float2(fmaf(yr.y, ds, xr.y), fmaf(yi.y, ds, xi.y)),
+                                            make_float2(pt.z, pt.w), make_float2(pl.z, pl.w)),
+                                 scale);
+#else
         s[pidx(t)] = c_scale(c_mul(make_float2(fmaf(yr.x, ds, xr.x), fmaf(yi.x, ds, xi.x)), make_float2(pt.x, pt.y)),
                              scale);
         s[pidx(t + 1)] =
             c_scale(c_mul(make_float2(fmaf(yr.y, ds, xr.y), fmaf(yi.y, ds, xi.y)), make_float2(pt.z, pt.w)), scale);
+#endif
     }
 }
 

@@ -30,6 +30,14 @@ __device__ __forceinline__ float photo_rate(float I, const NLParams &p, const fl
     return V * __fdividef(xi, I + p.tiny_I);
 }
 
+// u e^{x} for x <= 0 (the alpha/2 damping) as u + u (e^{x} - 1): the factor's
+// error is then relative to e^{x} - 1, not to 1, so a weakly absorbed point
+// is not biased by the same expf rounding every z-step.
+__device__ __forceinline__ float2 c_damp(float2 u, float x) {
+    const float m = expm1f(x);
+    return make_float2(fmaf(u.x, m, u.x), fmaf(u.y, m, u.y));
+}
+
 // alpha(u, rho) and the raw sum it clamps, as split() computes them.
 __device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p,
                                           const float4 *__restrict__ tab, float *raw) {
@@ -70,7 +78,7 @@ __device__ __forceinline__ float2 nl_point(float2 u, float rho, float rho_s, flo
     const float hdz = 0.5f * dz;
     float raw;
     float a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
-    u = c_scale(u, expf(-hdz * a));
+    u = c_damp(u, -hdz * a);
     float2 k1 = nl_rhs(u, rho, rho_s, p, tab);
     float2 k2 = nl_rhs(make_float2(fmaf(hdz, k1.x, u.x), fmaf(hdz, k1.y, u.y)), rho, rho_s, p, tab);
     float2 k3 = nl_rhs(make_float2(fmaf(hdz, k2.x, u.x), fmaf(hdz, k2.y, u.y)), rho, rho_s, p, tab);
@@ -79,6 +87,6 @@ __device__ __forceinline__ float2 nl_point(float2 u, float rho, float rho_s, flo
     u.x = fmaf(s6, fmaf(2.0f, k2.x + k3.x, k1.x) + k4.x, u.x);
     u.y = fmaf(s6, fmaf(2.0f, k2.y + k3.y, k1.y) + k4.y, u.y);
     a = alpha_of(fmaf(u.x, u.x, u.y * u.y), rho, p, tab, &raw);
-    return c_scale(u, expf(-hdz * a));
+    return c_damp(u, -hdz * a);
 }
 

@@ -232,16 +232,14 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     // twiddles exp(-2 pi i m / Nt) in the per-pass row layout, FP64 then rounded
     {
         const int n = fft_tw_size(Nt);
-        std::vector<float2> tw(n > 0 ? n : 1);
+        std::vector<float2> tw(n > 0 ? 2 * n : 2, make_float2(0.0f, 0.0f));
         for (int e = 0; e < n; ++e) {
             int m;
             fft_tw_entry(Nt, e, &m);
-            if (m < 0) {
-                tw[e] = make_float2(0.0f, 0.0f);
-                continue;
-            }
-            double a = -2.0 * M_PI * (double)m / (double)Nt;
-            tw[e] = make_float2((float)cos(a), (float)sin(a));
+            if (m < 0) continue;
+            const double a = -2.0 * M_PI * (double)m / (double)Nt, cr = cos(a), ci = sin(a);
+            tw[e] = make_float2((float)cr, (float)ci);
+            tw[n + e] = make_float2((float)(cr - (double)tw[e].x), (float)(ci - (double)tw[e].y));
         }
         NLSE_TRY(dev_upload(err, &c->d_tw, tw.data(), tw.size()));
     }
@@ -335,7 +333,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
         NLSE_TRY(dev_upload<float>(err, &c->d_F32, nullptr, K2 * Nt));
         NLSE_TRY(dev_upload<__nv_bfloat16>(err, &c->d_Fb, nullptr, 2 * K2 * Nt));
         NLSE_TRY(dev_upload<float>(err, &c->d_D, nullptr, K2 * Nt));
-        NLSE_TRY(dev_upload<float2>(err, &c->d_Ptf, nullptr, Nt));
+        NLSE_TRY(dev_upload<float2>(err, &c->d_Ptf, nullptr, 2 * (size_t)Nt));
         alignas(64) CUtensorMap m;
         cuuint32_t estr[2] = {1, 1};
         EncodeTiledFn cuTensorMapEncodeTiled = encode_tiled();
@@ -955,6 +953,12 @@ struct nlse_batch {
     int n, a_terms;
     int f16;                 // split-FP16 form (nlse_batch_set_mode)
     int last_f16;            // form of the last upload
+    // CUDA graph of three non-final z-steps (GEMM inputs g = 0..5 modulo 6:
+    // the kernels use g only modulo 2 and 3), replayed for the bulk of a call
+    cudaStream_t cap_stream;
+    cudaGraphExec_t graph;
+    int graph_key[3];        // (variant, a_terms, f16) it was captured for
+    int graph_off;           // capture failed once: launch directly
     nlse_ctx **ctx;          // one context per pulse (tables, operator, state buffers)
     BatchPulse *h_pulses;    // pinned staging of the per-pulse table
     BatchPulse *d_pulses;
@@ -985,7 +989,58 @@ static void batch_free(nlse_batch *b) {
     for (int c = 0; c < b->ncls; ++c)
         if (b->cls[c].d_work) cudaFree(b->cls[c].d_work);
     if (b->staged) cudaEventDestroy(b->staged);
+    if (b->graph) cudaGraphExecDestroy(b->graph);
+    if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     free(b);
+}
+
+// One non-final or final z-step of the batch on stream st: GEMM, row_nl
+// (consumes input g), GEMM, row_next (consumes g + 1; writes input g + 2 and
+// marches the carriers unless last).
+static cudaError_t batch_zstep(nlse_batch *b, int g, int last, cudaStream_t st) {
+    nlse_ctx *c = b->ctx[0];
+    cudaError_t e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms,
+                                           c->gemm_variant, b->f16, b->d_flag, st);
+    for (int k = 0; k < b->ncls && e == cudaSuccess; ++k)
+        e = launch_row_batch(1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 0, g, st);
+    if (e == cudaSuccess)
+        e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
+                                   b->f16, b->d_flag, st);
+    for (int k = 0; k < b->ncls && e == cudaSuccess; ++k)
+        e = launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last, g + 1,
+                             st);
+    return e;
+}
+
+// The graph of three non-final z-steps for the batch's current launch
+// configuration; NULL (and direct launches from then on) if capture fails.
+static cudaGraphExec_t batch_graph(nlse_batch *b) {
+    const int key[3] = {b->ctx[0]->gemm_variant, b->a_terms, b->f16};
+    if (b->graph && !memcmp(key, b->graph_key, sizeof(key))) return b->graph;
+    if (b->graph_off) return nullptr;
+    if (b->graph) {
+        cudaGraphExecDestroy(b->graph);
+        b->graph = nullptr;
+    }
+    if (!b->cap_stream && cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+        b->graph_off = 1;
+        return nullptr;
+    }
+    cudaGraph_t g = nullptr;
+    cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed);
+    for (int j = 0; j < 3 && e == cudaSuccess; ++j) e = batch_zstep(b, 2 * j, 0, b->cap_stream);
+    cudaError_t e2 = cudaStreamEndCapture(b->cap_stream, &g);
+    if (e == cudaSuccess) e = e2;
+    if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
+    if (g) cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        b->graph = nullptr;
+        b->graph_off = 1;
+        return nullptr;
+    }
+    memcpy(b->graph_key, key, sizeof(key));
+    return b->graph;
 }
 
 extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch **out) {
@@ -1187,7 +1242,15 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
         BSEQ(K_ROW_ENTRY,
              launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, -1, st),
              "batch row entry");
-    for (int it = 0; it < nsteps; ++it) {
+    int it = 0;
+    // the bulk of the non-final steps as graph launches of three steps each
+    // (not while per-launch profiling records the individual kernels)
+    if (!c->prof_on && nsteps - 1 >= 3) {
+        cudaGraphExec_t gx = batch_graph(b);
+        for (; gx && it + 3 <= nsteps - 1; it += 3)
+            BSEQ(K_GEMM_TC, cudaGraphLaunch(gx, st), "batch graph");
+    }
+    for (; it < nsteps; ++it) {
         const int last = it == nsteps - 1;
         BSEQ(K_GEMM_TC,
              launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,

@@ -73,7 +73,7 @@ struct ScanParams {
 struct RowFusedArgs {
     int Nr, Nt, logNt;
     const float2 *tw;     // forward twiddles
-    const float2 *Pt;     // e^{i dk dz/2} spec_mask (no 1/Nt)
+    const float2 *Pt;     // e^{i dk dz/2} spec_mask (no 1/Nt); Pt[Nt + k]: its rounding remainder
     const float *mask_r;  // Nr
     const float *lut;     // W * dt table for the march
     const float4 *pchip;  // photo-ionisation spline
@@ -160,7 +160,7 @@ struct nlse_ctx {
     float *d_F32;          // 2Nr x Nt planar Omega-domain state
     __nv_bfloat16 *d_Fb;   // 2 x (2Nr x Nt) BF16 hi/lo of the state
     float *d_D;            // 2Nr x Nt tensor-core product
-    float2 *d_Ptf;         // Nt  exp(i dk dz/2) mask Rk iRk  (no 1/Nt)
+    float2 *d_Ptf;         // 2Nt exp(i dk dz/2) mask Rk iRk (no 1/Nt), then its FP32 rounding remainder
     CUtensorMap tmA;       // A operand: d_A as [3 * 2Nr][2Nr], box 64 x 128, 128-byte swizzle
     CUtensorMap tmB;       // B operand: d_Fb as [2 * 2Nr][Nt], box 64 x 64
     CUtensorMap tmA32;     // A operand, box 32 x 128, 64-byte swizzle
@@ -248,10 +248,44 @@ __device__ __forceinline__ float2 c_mul(float2 a, float2 b) {
 }
 __device__ __forceinline__ float2 c_scale(float2 a, float s) { return make_float2(a.x * s, a.y * s); }
 
+// x (ph + pl) folding the remainder pl = p - ph of a rounded factor into the
+// products before their last rounding: the factor table's own rounding no
+// longer biases the result (what remains are roundings of data-dependent
+// values); 8 operations instead of c_mul's 4.
+__device__ __forceinline__ float2 c_mul_comp(float2 x, float2 ph, float2 pl) {
+    return make_float2(fmaf(x.x, ph.x, fmaf(-x.y, ph.y, fmaf(x.x, pl.x, -x.y * pl.y))),
+                       fmaf(x.x, ph.y, fmaf(x.y, ph.x, fmaf(x.x, pl.y, x.y * pl.x))));
+}
+
+// x (ph + pl) for a factor p held as its FP32 value ph and remainder pl = p - ph:
+// both products of each component are formed with their exact rounding errors
+// (fmaf) and summed with the remainder terms before the one final rounding, so
+// the result is the nearly correctly rounded x p.  A factor table applied every
+// z-step then adds no systematic error of its own (a plain product with the
+// rounded ph would repeat the same relative error every step).
+__device__ __forceinline__ float2 c_mul_exact(float2 x, float2 ph, float2 pl) {
+    const float a = x.x * ph.x, b = x.y * ph.y, c = x.x * ph.y, d = x.y * ph.x;
+    const float ea = fmaf(x.x, ph.x, -a), eb = fmaf(x.y, ph.y, -b);
+    const float ec = fmaf(x.x, ph.y, -c), ed = fmaf(x.y, ph.x, -d);
+    const float re = a - b, im = c + d;
+    // two-sum errors of re and im
+    const float bre = re - a, ere = (a - (re - bre)) + (-b - bre);
+    const float bim = im - c, eim = (c - (im - bim)) + (d - bim);
+    const float cre = fmaf(x.x, pl.x, -x.y * pl.y) + (ea - eb) + ere;
+    const float cim = fmaf(x.x, pl.y, x.y * pl.x) + (ec + ed) + eim;
+    return make_float2(re + cre, im + cim);
+}
+
 // multiply by the quarter-turn exp(-+ i pi/2): forward (-i), inverse (+i)
 template <bool INV>
 __device__ __forceinline__ float2 c_quarter(float2 a) {
     return INV ? make_float2(-a.y, a.x) : make_float2(a.y, -a.x);
+}
+
+// x / sqrt(2) with the constant's FP32 rounding remainder folded in before the
+// one rounding (the plain product would bias every radix-8 pass the same way).
+__device__ __forceinline__ float mul_rsqrt2(float x) {
+    return fmaf(x, 0.70710676908493041992f, x * 1.2101617104e-08f);
 }
 
 // ---------------------------------------------------------------- small DFTs
@@ -276,7 +310,6 @@ __device__ __forceinline__ void dft4(float2 *v) {
 
 template <bool INV>
 __device__ __forceinline__ void dft8(float2 *v) {
-    const float h = 0.70710678118654752f;
     float2 a[4], b[4];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
@@ -284,11 +317,11 @@ __device__ __forceinline__ void dft8(float2 *v) {
         b[r] = c_sub(v[r], v[r + 4]);
     }
     // b_r *= w8^r, w8 = exp(-+ i pi / 4)
-    b[1] = INV ? make_float2(h * (b[1].x - b[1].y), h * (b[1].x + b[1].y))
-               : make_float2(h * (b[1].x + b[1].y), h * (b[1].y - b[1].x));
+    b[1] = INV ? make_float2(mul_rsqrt2(b[1].x - b[1].y), mul_rsqrt2(b[1].x + b[1].y))
+               : make_float2(mul_rsqrt2(b[1].x + b[1].y), mul_rsqrt2(b[1].y - b[1].x));
     b[2] = c_quarter<INV>(b[2]);
-    b[3] = INV ? make_float2(-h * (b[3].x + b[3].y), h * (b[3].x - b[3].y))
-               : make_float2(h * (b[3].y - b[3].x), -h * (b[3].x + b[3].y));
+    b[3] = INV ? make_float2(-mul_rsqrt2(b[3].x + b[3].y), mul_rsqrt2(b[3].x - b[3].y))
+               : make_float2(mul_rsqrt2(b[3].y - b[3].x), -mul_rsqrt2(b[3].x + b[3].y));
     dft4<INV>(a);
     dft4<INV>(b);
 #pragma unroll
@@ -332,8 +365,17 @@ __host__ __device__ constexpr int fft_tw_offset(int N, int NS) {
     return off;
 }
 
-// float2 entries of the whole table of an N-point row.
+// float2 entries of the whole table of an N-point row (the table is followed
+// by as many entries of its FP32 rounding remainders).
 __host__ __device__ constexpr int fft_tw_size(int N) { return fft_tw_offset(N, N); }
+
+// Twiddle and spectral-phase products with the tables' rounding remainders
+// folded in (c_mul_comp; 2: the nearly correctly rounded c_mul_exact; 0: plain
+// products).  Over 4000 z-steps the plain products' fixed rounding of each
+// table entry adds up coherently to ~3e-4 of the field.
+#ifndef NLSE_COMP_TWIDDLE
+#define NLSE_COMP_TWIDDLE 1
+#endif
 
 // One Stockham autosort pass of radix R over a row of N points (compile-time
 // sizes): reads src, writes dst (padded indexing).  NS = product of the
@@ -360,12 +402,37 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
                     w[2 * q] = make_float2(p.x, p.y);
                     w[2 * q + 1] = make_float2(p.z, p.w);
                 }
+#if NLSE_COMP_TWIDDLE
+                // the table's rounding remainders follow the table
+                const float4 *l4 = w4 + fft_tw_size(N) / 2;
+                float2 wl[fft_tw_row(R)];
+#pragma unroll
+                for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
+                    const float4 p = __ldg(&l4[q]);
+                    wl[2 * q] = make_float2(p.x, p.y);
+                    wl[2 * q + 1] = make_float2(p.z, p.w);
+                }
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    float2 x = w[r - 1], xl = wl[r - 1];
+                    if (INV) {
+                        x.y = -x.y;
+                        xl.y = -xl.y;
+                    }
+#if NLSE_COMP_TWIDDLE == 2
+                    v[r] = c_mul_exact(v[r], x, xl);
+#else
+                    v[r] = c_mul_comp(v[r], x, xl);
+#endif
+                }
+#else
 #pragma unroll
                 for (int r = 1; r < R; ++r) {
                     float2 x = w[r - 1];
                     if (INV) x.y = -x.y;
                     v[r] = c_mul(v[r], x);
                 }
+#endif
             }
             dft_small<R, INV>(v);
             const int d0 = (j - k) * R + k;

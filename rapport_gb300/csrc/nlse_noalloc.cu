@@ -8,7 +8,7 @@
 // field as caller-owned device pointers, needs no nlse_ctx, and keeps its
 // intermediate field and twiddle table in the file-scope array below.
 //
-// The array is a fixed 4 MiB + 101 KiB of device memory that every GPU which
+// The array is a fixed 4 MiB + 201 KiB of device memory that every GPU which
 // loads this library holds until the process exits.  Its address is looked up
 // once per device (cudaGetSymbolAddress, with that device current) on the
 // first call made on that device; make that first call before any stream
@@ -24,7 +24,7 @@
 
 #define NLSE_NOALLOC_MAX_POINTS (1 << 19)  // Nr * Nt complex64 points: 4 MiB
 
-static __device__ __align__(256) float2 g_noalloc_scratch[NLSE_NOALLOC_MAX_POINTS + fft_tw_size(NLSE_MAX_NT)];
+static __device__ __align__(256) float2 g_noalloc_scratch[NLSE_NOALLOC_MAX_POINTS + 2 * fft_tw_size(NLSE_MAX_NT)];
 
 static float2 *g_scratch_ptr[64];
 static std::mutex g_scratch_mu;
@@ -49,13 +49,16 @@ static cudaError_t scratch_for_current_device(float2 **out) {
 // The row FFT's twiddle table (per-pass row layout), FP64 then rounded: the
 // same values as a context's table.
 __global__ void k_noalloc_twiddles(float2 *__restrict__ tw, int Nt) {
+    const int n = fft_tw_size(Nt);
     int e = blockIdx.x * blockDim.x + threadIdx.x;
-    if (e < fft_tw_size(Nt)) {
+    if (e < n) {
         int m;
         fft_tw_entry(Nt, e, &m);
         double s = 0.0, c = 0.0;
         if (m >= 0) sincospi(-2.0 * (double)m / (double)Nt, &s, &c);
-        tw[e] = make_float2((float)c, (float)s);
+        const float2 h = make_float2((float)c, (float)s);
+        tw[e] = h;
+        tw[n + e] = make_float2((float)(c - (double)h.x), (float)(s - (double)h.y));
     }
 }
 

@@ -55,7 +55,10 @@ __device__ __forceinline__ float step_map(float x, float a, float b, const ScanP
     float em1 = expm1f(z);
     float az = fabsf(z);
     float ph = az > 1e-4f ? em1 / z : fmaf(z, fmaf(z, fmaf(z, 1.0f / 24.0f, 1.0f / 6.0f), 0.5f), 1.0f);
-    float y = fmaf(e, x, b * d * ph);
+    // e^z x + b d phi1(z) as x + (expm1(z) x + b d phi1(z)): the decay factor's
+    // rounding then scales only the change, not x, so it does not bias the
+    // density the same way at every one of the row's steps
+    float y = x + fmaf(em1, x, b * d * ph);
     float dd = (x >= p.x_tiny && x < p.na) ? -p.inv_na : 0.0f;
     float dph;  // phi1'(z) = (z e^z - (e^z - 1)) / z^2
     if (az < 0.1f)
@@ -307,8 +310,8 @@ __device__ __forceinline__ void step_map2(float e, float s, float a, float as, f
     phi1_d(zs, es, esm1, &phs, &dphs);
     const float sn = s * p.inv_na;
     const float qe = fmaf(b, d, r * sn), qs = p.c_rec * e;
-    float y0 = fmaf(ee, e, qe * phe);
-    float y1 = fmaf(es, s, qs * phs);
+    float y0 = e + fmaf(eem1, e, qe * phe);
+    float y1 = s + fmaf(esm1, s, qs * phs);
     const float ze_e = a * dd, zs_e = -as * p.inv_na;
     const float qe_e = fmaf(b, dd, as * sn), qe_s = r * p.inv_na;
     Aff2 j;

@@ -9,8 +9,8 @@
   split-FP16 form.  Reports the
   relative L2 field error, peak-fluence error and peak-rho error at 0.125,
   0.25, 0.5 and 1 cm, writes them to gpurun_out/accuracy_1cm.json when that
-  folder exists, and asserts the benchmark spec's bounds for the split-BF16 form:
-  L2 <= 1e-4 and peak-rho <= 1e-3 after 1 cm.
+  folder exists, and asserts the bounds L2 <= 1e-4 and peak-rho <= 1e-3
+  after 1 cm for the split-BF16 (3-term) and split-FP16 forms.
 """
 import json
 import os
@@ -81,5 +81,6 @@ def test_one_cm_accuracy():
     if os.path.isdir(out):
         with open(os.path.join(out, "accuracy_1cm.json"), "w") as f:
             json.dump(report, f, indent=1)
-    last = report["checkpoints"]["1.000 cm"]["split_bf16_3term"]
-    assert last["l2"] <= 1e-4 and last["peak_rho"] <= 1e-3, last
+    for name in ("split_bf16_3term", "split_f16"):
+        last = report["checkpoints"]["1.000 cm"][name]
+        assert last["l2"] <= 1e-4 and last["peak_rho"] <= 1e-3, (name, last)
