@@ -5,11 +5,11 @@ fused silica, 5 uJ, w0 150 um, f 10 cm, dz 2.5 um, seeded 1 % noise) and calls,
 in order: the plain half step, split(), the nonlinear block, update_plasma,
 one z-step and a 2-step propagate in each arithmetic (plain FP32, split-BF16,
 split-FP16), a 2-step propagate of 8 such pulses in one batch (both split
-forms), the record reductions, the exciton-channel march and the full-physics
+forms), the record reductions, the exciton-channel march, the full-physics
 split / nonlinear block (Raman, self-steepening, space-time focusing) and the
-fused full-physics row kernel of the split form on the same grid.  Under a profiler the launch list then holds every kernel kind at
-full size; the program checks only that every call succeeds and the fields
-stay finite.
+fused full-physics row kernel of the split form on the same grid.  Under a
+profiler the launch list then holds every kernel kind at full size; the
+program checks only that every call succeeds and the fields stay finite.
 """
 import numpy as np
 import torch
