@@ -55,6 +55,7 @@ __device__ __forceinline__ float photo_term(float a2, float rho, const NLParams 
     if (!p.photo_on) return 0.0f;
     const float I = a2 * p.invE2;
     if (isfinite(I)) {
+        if (I < p.I_skip) return isnan(rho) ? rho : 0.0f;
         const float dep = isnan(rho) ? rho : fminf(fmaxf((p.rho_max - rho) * p.inv_rho_max, 0.0f), 1.0f);
         return photo_rate(I, p, tab) * dep;
     }

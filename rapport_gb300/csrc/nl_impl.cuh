@@ -34,6 +34,7 @@ __device__ __forceinline__ float photo_rate(float I, const NLParams &p, const fl
 // error is then relative to e^{x} - 1, not to 1, so a weakly absorbed point
 // is not biased by the same expf rounding every z-step.
 __device__ __forceinline__ float2 c_damp(float2 u, float x) {
+    if (x == 0.0f) return u;  // no absorption (no carriers, negligible photo-ionisation)
     const float m = expm1f(x);
     return make_float2(fmaf(u.x, m, u.x), fmaf(u.y, m, u.y));
 }
@@ -45,8 +46,10 @@ __device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p
     if (p.photo_on) {
         float I = a2 * p.invE2;
         if (isfinite(I)) {
-            float dep = fminf(fmaxf((p.rho_max - rho) * p.inv_rho_max, 0.0f), 1.0f);
-            photo = photo_rate(I, p, tab) * dep;
+            if (!(I < p.I_skip)) {
+                float dep = fminf(fmaxf((p.rho_max - rho) * p.inv_rho_max, 0.0f), 1.0f);
+                photo = photo_rate(I, p, tab) * dep;
+            }
         } else if (isnan(I)) {
             photo = I;  // NaN: split() turns the sum into alpha = 0 (nan_to_num)
         }             // +Inf: W(Imax) / Inf = 0 in split()

@@ -276,6 +276,22 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
             }
             tab[i] = make_float4(f[0], f[1], f[2], f[3]);
         }
+        // Below I_skip the rate is bounded by 1e-20 / m: alpha dz / 2 is then
+        // far below FP32 resolution, and the kernels skip the spline there.
+        // Interval i bounds the rate by the sum of its coefficients' magnitudes
+        // (x_i / I <= 1 on it); below Imin the rate is |c0| Imin / (I + tiny).
+        const double eps = 1e-20;
+        double skip = 0.0;
+        if (fabs((double)tab[0].x) * d->pchip_x[0] / (1e-30 * d->invE2) < eps) {
+            skip = d->pchip_x[0];
+            for (int i = 0; i < ni; ++i) {
+                const double b = fabs((double)tab[i].x) + fabs((double)tab[i].y) + fabs((double)tab[i].z) +
+                                 fabs((double)tab[i].w);
+                if (!(b < eps)) break;
+                skip = d->pchip_x[i + 1];
+            }
+        }
+        c->nl.I_skip = (float)skip;
         NLSE_TRY(dev_upload(err, &c->d_pchip, tab.data(), ni));
     }
     {

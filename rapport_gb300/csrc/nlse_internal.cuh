@@ -45,6 +45,7 @@ struct NLParams {
     int n_int;          // spline intervals
     float ste_pref;     // exciton index term: rhs += i ste_pref rho_s u
     float kp_raman;     // kerr_pref * f_R (0 if Raman off)
+    float I_skip;       // below this intensity the photo-ionisation rate is < 1e-20 / m (taken as 0)
 };
 
 // Tables of the full-physics split() (device, FFT order; NULL = that term off).
