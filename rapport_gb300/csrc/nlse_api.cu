@@ -971,7 +971,8 @@ struct nlse_batch {
     int last_f16;            // form of the last upload
     // CUDA graph of three non-final z-steps (GEMM inputs g = 0..5 modulo 6:
     // the kernels use g only modulo 2 and 3), replayed for the bulk of a call
-    cudaStream_t cap_stream;
+    cudaStream_t cap_stream, cap_stream2;
+    cudaEvent_t cap_fork, cap_join;
     cudaGraphExec_t graph;
     int graph_key[3];        // (variant, a_terms, f16) it was captured for
     int graph_off;           // capture failed once: launch directly
@@ -984,7 +985,11 @@ struct nlse_batch {
     struct Class {
         int logNt, nblocks;
         int2 *d_work;
+        int split;           // work entries of lane 0 (pulses [0, lane_pulse))
     } cls[16];
+    // two lanes (pulses [0, lane_pulse) and the rest) run as parallel branches
+    // of the z-step graph, so one lane's row kernels fill the other's GEMM tail
+    int lane_pulse, lane_tiles;  // lane 0's pulses / tiles (tiles are in pulse order)
     int ncls;
     int *d_flag;
     cudaEvent_t staged;      // the last upload of h_pulses has been consumed
@@ -1007,24 +1012,36 @@ static void batch_free(nlse_batch *b) {
     if (b->staged) cudaEventDestroy(b->staged);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
+    if (b->cap_stream2) cudaStreamDestroy(b->cap_stream2);
+    if (b->cap_fork) cudaEventDestroy(b->cap_fork);
+    if (b->cap_join) cudaEventDestroy(b->cap_join);
     free(b);
 }
 
 // One non-final or final z-step of the batch on stream st: GEMM, row_nl
 // (consumes input g), GEMM, row_next (consumes g + 1; writes input g + 2 and
 // marches the carriers unless last).
-static cudaError_t batch_zstep(nlse_batch *b, int g, int last, cudaStream_t st) {
+// One z-step of one lane (0 or 1; -1: all pulses) on stream st: GEMM, row_nl
+// (consumes input g), GEMM, row_next (consumes g + 1; writes input g + 2 and
+// marches the carriers unless last).
+static cudaError_t batch_zstep(nlse_batch *b, int g, int last, int lane, cudaStream_t st) {
     nlse_ctx *c = b->ctx[0];
-    cudaError_t e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms,
-                                           c->gemm_variant, b->f16, b->d_flag, st);
-    for (int k = 0; k < b->ncls && e == cudaSuccess; ++k)
-        e = launch_row_batch(1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 0, g, st);
-    if (e == cudaSuccess)
-        e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
-                                   b->f16, b->d_flag, st);
-    for (int k = 0; k < b->ncls && e == cudaSuccess; ++k)
-        e = launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last, g + 1,
-                             st);
+    const int t0 = lane == 1 ? b->lane_tiles : 0;
+    const int nt = lane < 0 ? b->ntiles : (lane == 0 ? b->lane_tiles : b->ntiles - b->lane_tiles);
+    cudaError_t e = cudaSuccess;
+    for (int half = 0; half < 2 && e == cudaSuccess; ++half) {
+        if (nt > 0)
+            e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + t0, nt, b->a_terms, c->gemm_variant,
+                                       b->f16, b->d_flag, st);
+        for (int k = 0; k < b->ncls && e == cudaSuccess; ++k) {
+            const int w0 = lane == 1 ? b->cls[k].split : 0;
+            const int nw = lane < 0 ? b->cls[k].nblocks
+                                    : (lane == 0 ? b->cls[k].split : b->cls[k].nblocks - b->cls[k].split);
+            if (nw > 0)
+                e = launch_row_batch(half == 0 ? 1 : 2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work + w0, nw,
+                                     half == 0 ? 0 : last, g + half, st);
+        }
+    }
     return e;
 }
 
@@ -1038,13 +1055,28 @@ static cudaGraphExec_t batch_graph(nlse_batch *b) {
         cudaGraphExecDestroy(b->graph);
         b->graph = nullptr;
     }
-    if (!b->cap_stream && cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess) {
+    if (!b->cap_stream &&
+        (cudaStreamCreateWithFlags(&b->cap_stream, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaStreamCreateWithFlags(&b->cap_stream2, cudaStreamNonBlocking) != cudaSuccess ||
+         cudaEventCreateWithFlags(&b->cap_fork, cudaEventDisableTiming) != cudaSuccess ||
+         cudaEventCreateWithFlags(&b->cap_join, cudaEventDisableTiming) != cudaSuccess)) {
         b->graph_off = 1;
         return nullptr;
     }
     cudaGraph_t g = nullptr;
     cudaError_t e = cudaStreamBeginCapture(b->cap_stream, cudaStreamCaptureModeRelaxed);
-    for (int j = 0; j < 3 && e == cudaSuccess; ++j) e = batch_zstep(b, 2 * j, 0, b->cap_stream);
+    const bool two = b->lane_tiles > 0 && b->lane_tiles < b->ntiles;
+    if (two) {
+        // lane 1 forks onto the second stream and joins before the capture ends
+        if (e == cudaSuccess) e = cudaEventRecord(b->cap_fork, b->cap_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->cap_stream2, b->cap_fork, 0);
+        for (int j = 0; j < 3 && e == cudaSuccess; ++j) e = batch_zstep(b, 2 * j, 0, 0, b->cap_stream);
+        for (int j = 0; j < 3 && e == cudaSuccess; ++j) e = batch_zstep(b, 2 * j, 0, 1, b->cap_stream2);
+        if (e == cudaSuccess) e = cudaEventRecord(b->cap_join, b->cap_stream2);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(b->cap_stream, b->cap_join, 0);
+    } else {
+        for (int j = 0; j < 3 && e == cudaSuccess; ++j) e = batch_zstep(b, 2 * j, 0, -1, b->cap_stream);
+    }
     cudaError_t e2 = cudaStreamEndCapture(b->cap_stream, &g);
     if (e == cudaSuccess) e = e2;
     if (e == cudaSuccess) e = cudaGraphInstantiate(&b->graph, g, 0);
@@ -1120,8 +1152,19 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         if (k == nlog) logs[nlog++] = c->logNt;
         for (int r = 0; r < c->Nr; ++r) work[k].push_back(make_int2(i, r));
     }
-    // large tiles first: the big pulses' tiles start in the first waves
     b->ntiles = (int)tiles.size();
+    // lane 0 = the first pulses up to about half of the tiles
+    b->lane_pulse = 0;
+    b->lane_tiles = 0;
+    if (n >= 2) {
+        int acc = 0, p = 0;
+        while (p < n - 1 && 2 * acc < b->ntiles) {
+            acc += (2 * b->ctx[p]->Nr / 128) * (b->ctx[p]->Nt / 256);
+            ++p;
+        }
+        b->lane_pulse = p;
+        b->lane_tiles = acc;
+    }
     cudaError_t e = cudaMalloc((void **)&b->d_tiles, tiles.size() * sizeof(GemmTile));
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice);
@@ -1137,6 +1180,8 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
     for (int k = 0; k < nlog && e == cudaSuccess; ++k) {
         b->cls[k].logNt = logs[k];
         b->cls[k].nblocks = (int)work[k].size();
+        b->cls[k].split = 0;
+        for (const int2 &w : work[k]) b->cls[k].split += w.x < b->lane_pulse;
         e = cudaMalloc((void **)&b->cls[k].d_work, work[k].size() * sizeof(int2));
         if (e == cudaSuccess)
             e = cudaMemcpy(b->cls[k].d_work, work[k].data(), work[k].size() * sizeof(int2), cudaMemcpyHostToDevice);
