@@ -133,23 +133,34 @@ __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs
     }
 }
 
+// Carrier march of the intensities already written to sI (scan layout): scan
+// in the scratch Rb (a complex row buffer no thread reads any more) and X;
+// writes rho row r.
+template <int NT>
+__device__ __forceinline__ void march_scan(float *sI, float2 *Rb, float *X, int r, const RowFusedArgs &a,
+                                           float *rho) {
+    constexpr int S = scan_span(NT, NLSE_ROW_THREADS);
+    const ScanLayout L = scan_layout(NT);
+    float *sW = sI + S;
+    __syncthreads();
+    float *sx = reinterpret_cast<float *>(Rb), *sJ = sx + S;
+    scan_row(sI, sW, sx, sJ, X, NT, a.sc, a.lut, 0.0f, a.stats);
+    float *gr = rho + (size_t)r * NT;
+    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[scan_slot(t, L)];
+}
+
 // Carrier march of the physical row held (unnormalised by inv) in R; scratch
 // in the other FFT buffer O and the extra float area X; writes rho row r.
 template <int NT>
 __device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float inv, int r, const RowFusedArgs &a,
                                           float *rho) {
-    constexpr int S = scan_span(NT, NLSE_ROW_THREADS);
     const ScanLayout L = scan_layout(NT);
-    float *sI = reinterpret_cast<float *>(O), *sW = sI + S;
+    float *sI = reinterpret_cast<float *>(O);
     for (int t = threadIdx.x; t < NT; t += blockDim.x) {
         const float2 v = c_scale(R[pidx(t)], inv);
         sI[scan_slot(t, L)] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
     }
-    __syncthreads();
-    float *sx = reinterpret_cast<float *>(R), *sJ = sx + S;
-    scan_row(sI, sW, sx, sJ, X, NT, a.sc, a.lut, 0.0f, a.stats);
-    float *gr = rho + (size_t)r * NT;
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[scan_slot(t, L)];
+    march_scan<NT>(sI, R, X, r, a, rho);
 }
 
 // 2 padded complex row buffers (+ one float scan array, scan_span(NT) long, for the march).
@@ -160,6 +171,131 @@ __host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
     constexpr int span = scan_span(NT, NLSE_ROW_THREADS);
     static_assert(2 * span <= 2 * fft_slots(NT), "scan arrays must fit in the FFT buffers");
     return 2 * (size_t)fft_slots(NT) * sizeof(float2) + (with_march ? (size_t)span * sizeof(float) : 0);
+}
+
+// ------------------------------------------------ register-resident row_next
+// For N_t = 2048 (8 points per thread) row_next keeps its row in registers:
+// thread tid holds the points tid + 256 m.  Loads, the state stores, the
+// inverse FFT (fft_regs), the physical field and the march's intensities act
+// on those points in place, so the row crosses shared memory only inside the
+// FFT; the arithmetic per point is that of the shared-memory body (results
+// agree bit for bit), ~10 % faster at 1024 x 2048.  (For row_nl the
+// shared-memory body with its two-point vector accesses measured faster.)
+template <int NT>
+__host__ __device__ constexpr bool row_regs() {
+    return fft_regs_ok<NT, NLSE_ROW_THREADS>() && NT / NLSE_ROW_THREADS == 8;
+}
+
+template <int NT>
+__device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / NLSE_ROW_THREADS], int r, const RowFusedArgs &a,
+                                             const float *F32, const float *D, float scale, int g_in) {
+    const float ds = a.f16 ? ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) +
+                                            __ldcg(&a.scale[NLSE_SC_SB + g_in % 2])))
+                           : 1.0f;
+    const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nr + r) * NT;
+    const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nr + r) * NT;
+#pragma unroll
+    for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
+        const int t = (int)threadIdx.x + m * NLSE_ROW_THREADS;
+        const float2 x = make_float2(fmaf(dr[t], ds, fr[t]), fmaf(di[t], ds, fi[t]));
+        const float2 pt = __ldg(a.Pt + t);
+#if NLSE_COMP_TWIDDLE
+        v[m] = c_scale(c_mul_comp(x, pt, __ldg(a.Pt + NT + t)), scale);
+#else
+        v[m] = c_scale(c_mul(x, pt), scale);
+#endif
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / NLSE_ROW_THREADS], int r,
+                                                 const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, int g_out) {
+    const size_t rows = 2 * (size_t)a.Nr;
+    float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nr + r) * NT;
+    __nv_bfloat16 *hre = Fb + (size_t)r * NT, *him = Fb + ((size_t)a.Nr + r) * NT;
+    __nv_bfloat16 *lre = hre + rows * NT, *lim = him + rows * NT;
+    if (!a.f16) {
+#pragma unroll
+        for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
+            const int t = (int)threadIdx.x + m * NLSE_ROW_THREADS;
+            re[t] = v[m].x;
+            im[t] = v[m].y;
+            const __nv_bfloat16 hx = __float2bfloat16_rn(v[m].x), hy = __float2bfloat16_rn(v[m].y);
+            hre[t] = hx;
+            him[t] = hy;
+            lre[t] = __float2bfloat16_rn(v[m].x - __bfloat162float(hx));
+            lim[t] = __float2bfloat16_rn(v[m].y - __bfloat162float(hy));
+        }
+        return;
+    }
+    __half *fre = reinterpret_cast<__half *>(hre), *fim = reinterpret_cast<__half *>(him);
+    __half *gre = reinterpret_cast<__half *>(lre), *gim = reinterpret_cast<__half *>(lim);
+    const int sb = f16_field_exp(a.scale, g_out);
+    const float sc = ldexpf(1.0f, sb);
+    float mx = 0.0f;
+#pragma unroll
+    for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
+        const int t = (int)threadIdx.x + m * NLSE_ROW_THREADS;
+        re[t] = v[m].x;
+        im[t] = v[m].y;
+        mx = fmaxf(mx, fmaxf(fabsf(v[m].x), fabsf(v[m].y)));
+        const float x = v[m].x * sc, y = v[m].y * sc;
+        const __half hx = __float2half_rn(x), hy = __float2half_rn(y);
+        fre[t] = hx;
+        fim[t] = hy;
+        gre[t] = __float2half_rn(x - __half2float(hx));
+        gim[t] = __float2half_rn(y - __half2float(hy));
+    }
+    // a finite value above 65504 after scaling overflowed its FP16 term
+    const int ovf = __syncthreads_or(isfinite(mx) && !(mx * sc <= 65504.0f));
+    mx = block_max(mx);
+    if (threadIdx.x == 0) {
+        atomicMax(&a.scale[NLSE_SC_MAX + g_out % 3], __float_as_int(mx));
+        if (ovf) atomicAdd(&a.scale[NLSE_SC_OVF], 1);
+        if (r == 0) {
+            a.scale[NLSE_SC_SB + g_out % 2] = sb;
+            a.scale[NLSE_SC_MAX + (g_out + 1) % 3] = 0;  // the slot input g_out + 1 will fill
+        }
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void row_next_regs(const RowFusedArgs &a, int r, float *__restrict__ F32,
+                                              __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+                                              float *__restrict__ rho, float2 *__restrict__ u_out, int write_state,
+                                              int do_scan, int apply_mask, int g) {
+    extern __shared__ float2 sm2[];
+    float2 *A = sm2, *B = sm2 + fft_slots(NT);
+    float2 v[NT / NLSE_ROW_THREADS];
+    load_mw_regs<NT>(v, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f, g);
+    if (write_state) store_state_regs<NT>(v, r, a, F32, Fb, g + 1);
+    if (!do_scan && !u_out) return;
+    float2 *F = fft_regs<NT, true>(v, A, B, a.tw);
+    const float inv = 1.0f / (float)NT;
+    if (u_out) {
+        float2 *gu = u_out + (size_t)r * NT;
+#pragma unroll
+        for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) gu[threadIdx.x + m * NLSE_ROW_THREADS] = c_scale(v[m], inv);
+    }
+    if (!do_scan) return;
+    const ScanLayout L = scan_layout(NT);
+    float *sI = reinterpret_cast<float *>(F);
+#pragma unroll
+    for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
+        const float2 w = c_scale(v[m], inv);
+        sI[scan_slot((int)threadIdx.x + m * NLSE_ROW_THREADS, L)] = fmaf(w.x, w.x, w.y * w.y) * a.sc.invE2;
+    }
+    march_scan<NT>(sI, F == A ? B : A, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), r, a, rho);
+}
+
+// CTAs per SM the row kernels are compiled for: 5, or as many as their
+// shared memory admits (228 KB per SM, 1 KB reserved per CTA) when fewer --
+// N_t = 4096 then gets 80-128 registers instead of spilling at 48.
+template <int NT>
+__host__ __device__ constexpr int row_min_blocks(bool with_march) {
+    return (228 * 1024) / (int)(row_smem_bytes<NT>(with_march) + 1024) < 5
+               ? (228 * 1024) / (int)(row_smem_bytes<NT>(with_march) + 1024)
+               : 5;
 }
 
 // Entry: physical u (interleaved) -> w = F[u] (state); optionally rho = march(|u|^2).
@@ -217,6 +353,10 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
                                               __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
                                               float *__restrict__ rho, float2 *__restrict__ u_out, int write_state,
                                               int do_scan, int apply_mask, int g) {
+    if constexpr (row_regs<NT>()) {
+        row_next_regs<NT>(a, r, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
+        return;
+    }
     extern __shared__ float2 sm2[];
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
     load_mw_row<NT>(b0, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f, g);
@@ -266,14 +406,14 @@ k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F3
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(false))
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
          const float *__restrict__ rho, int g) {
     row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(true))
 k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
            float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask, int g) {
     row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
@@ -290,7 +430,7 @@ k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, i
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(false))
 k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
@@ -298,7 +438,7 @@ k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int 
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, 5)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(true))
 k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];

@@ -378,6 +378,52 @@ __host__ __device__ constexpr int fft_tw_size(int N) { return fft_tw_offset(N, N
 #define NLSE_COMP_TWIDDLE 1
 #endif
 
+// Twiddle products of butterfly k of the pass at NS (radix R) of an N-point
+// row: v[r] *= exp(-+ 2 pi i r k (N / (NS R)) / N), r = 1 .. R-1, from table
+// row k of the pass (and its rounding remainders).
+template <int R, bool INV, int N, int NS>
+__device__ __forceinline__ void apply_twiddles(float2 *v, int k, const float2 *__restrict__ tw) {
+    const float4 *w4 = reinterpret_cast<const float4 *>(tw + fft_tw_offset(N, NS) + k * fft_tw_row(R));
+    float2 w[fft_tw_row(R)];
+#pragma unroll
+    for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
+        const float4 p = __ldg(&w4[q]);
+        w[2 * q] = make_float2(p.x, p.y);
+        w[2 * q + 1] = make_float2(p.z, p.w);
+    }
+#if NLSE_COMP_TWIDDLE
+    // the table's rounding remainders follow the table
+    const float4 *l4 = w4 + fft_tw_size(N) / 2;
+    float2 wl[fft_tw_row(R)];
+#pragma unroll
+    for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
+        const float4 p = __ldg(&l4[q]);
+        wl[2 * q] = make_float2(p.x, p.y);
+        wl[2 * q + 1] = make_float2(p.z, p.w);
+    }
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+        float2 x = w[r - 1], xl = wl[r - 1];
+        if (INV) {
+            x.y = -x.y;
+            xl.y = -xl.y;
+        }
+#if NLSE_COMP_TWIDDLE == 2
+        v[r] = c_mul_exact(v[r], x, xl);
+#else
+        v[r] = c_mul_comp(v[r], x, xl);
+#endif
+    }
+#else
+#pragma unroll
+    for (int r = 1; r < R; ++r) {
+        float2 x = w[r - 1];
+        if (INV) x.y = -x.y;
+        v[r] = c_mul(v[r], x);
+    }
+#endif
+}
+
 // One Stockham autosort pass of radix R over a row of N points (compile-time
 // sizes): reads src, writes dst (padded indexing).  NS = product of the
 // radices already applied; tw = the twiddle table above.
@@ -393,48 +439,7 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
             float2 v[R];
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = src[pidx(j + r * nb)];
-            if (NS > 1) {
-                const float4 *w4 =
-                    reinterpret_cast<const float4 *>(tw + fft_tw_offset(N, NS) + k * fft_tw_row(R));
-                float2 w[fft_tw_row(R)];
-#pragma unroll
-                for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
-                    const float4 p = __ldg(&w4[q]);
-                    w[2 * q] = make_float2(p.x, p.y);
-                    w[2 * q + 1] = make_float2(p.z, p.w);
-                }
-#if NLSE_COMP_TWIDDLE
-                // the table's rounding remainders follow the table
-                const float4 *l4 = w4 + fft_tw_size(N) / 2;
-                float2 wl[fft_tw_row(R)];
-#pragma unroll
-                for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
-                    const float4 p = __ldg(&l4[q]);
-                    wl[2 * q] = make_float2(p.x, p.y);
-                    wl[2 * q + 1] = make_float2(p.z, p.w);
-                }
-#pragma unroll
-                for (int r = 1; r < R; ++r) {
-                    float2 x = w[r - 1], xl = wl[r - 1];
-                    if (INV) {
-                        x.y = -x.y;
-                        xl.y = -xl.y;
-                    }
-#if NLSE_COMP_TWIDDLE == 2
-                    v[r] = c_mul_exact(v[r], x, xl);
-#else
-                    v[r] = c_mul_comp(v[r], x, xl);
-#endif
-                }
-#else
-#pragma unroll
-                for (int r = 1; r < R; ++r) {
-                    float2 x = w[r - 1];
-                    if (INV) x.y = -x.y;
-                    v[r] = c_mul(v[r], x);
-                }
-#endif
-            }
+            if (NS > 1) apply_twiddles<R, INV, N, NS>(v, k, tw);
             dft_small<R, INV>(v);
             const int d0 = (j - k) * R + k;
 #pragma unroll
@@ -462,6 +467,69 @@ __device__ __forceinline__ float2 *fft_passes(float2 *src, float2 *dst, const fl
 template <int N, bool INV, int T = NLSE_ROW_THREADS>
 __device__ __forceinline__ float2 *fft_row(float2 *buf0, float2 *buf1, const float2 *__restrict__ tw) {
     return fft_passes<N, 1, INV, T>(buf0, buf1, tw);
+}
+
+// ------------------------------------------------ register-resident row FFT
+// The same Stockham plan, butterflies and twiddle products as fft_row (the
+// results agree bit for bit) with the row held in registers: each of the T
+// threads keeps P = N / T points, v[m] = point threadIdx.x + T m, on entry and
+// on exit.  Butterfly j = threadIdx.x + T q of a pass takes its inputs
+// j + r N / R: in the first pass they are the thread's own v[q + r P / R], and
+// the last pass's outputs j + r N / R land in v[q + r P / R] again, so the row
+// crosses shared memory only between passes (padded buffers A, B, A, ...; one
+// barrier each).  Every radix of the plan must divide P.
+template <int N, int T>
+__host__ __device__ constexpr bool fft_regs_ok() {
+    if (N % T != 0 || N / T < 2) return false;
+    int passes = 0;
+    for (int s = 1; s < N; s *= fft_radix(N, s)) {
+        if ((N / T) % fft_radix(N, s) != 0) return false;
+        ++passes;
+    }
+    return passes >= 3;  // at least two exchanges (see fft_regs)
+}
+
+template <int N, int NS, bool INV, int T>
+__device__ __forceinline__ float2 *fft_regs_pass(float2 (&v)[N / T], float2 *src, float2 *dst,
+                                                 const float2 *__restrict__ tw) {
+    constexpr int P = N / T, R = fft_radix(N, NS), Q = P / R, nb = N / R;
+    constexpr bool first = NS == 1, last = NS * R == N;
+    static_assert(P % R == 0, "every radix must divide the points per thread");
+#pragma unroll
+    for (int q = 0; q < Q; ++q) {
+        const int j = (int)threadIdx.x + q * T;
+        const int k = j & (NS - 1);
+        float2 y[R];
+#pragma unroll
+        for (int r = 0; r < R; ++r) y[r] = first ? v[q + r * Q] : src[pidx(j + r * nb)];
+        if (NS > 1) apply_twiddles<R, INV, N, NS>(y, k, tw);
+        dft_small<R, INV>(y);
+        if constexpr (last) {
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[q + r * Q] = y[r];
+        } else {
+            const int d0 = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[pidx(d0 + r * NS)] = y[r];
+        }
+    }
+    if constexpr (!last) {
+        __syncthreads();
+        return fft_regs_pass<N, NS * R, INV, T>(v, dst, src, tw);
+    } else {
+        return dst;
+    }
+}
+
+// Unnormalised FFT of the row in v (layout above).  The first pass writes A
+// without a barrier, so no thread may still read A.  Returns a buffer that was
+// last read before the final barrier: free to write at once (the other one
+// only after a barrier).
+template <int N, bool INV, int T = NLSE_ROW_THREADS>
+__device__ __forceinline__ float2 *fft_regs(float2 (&v)[N / T], float2 *A, float2 *B,
+                                            const float2 *__restrict__ tw) {
+    static_assert(fft_regs_ok<N, T>(), "row length not supported by the register FFT");
+    return fft_regs_pass<N, 1, INV, T>(v, B, A, tw);
 }
 
 // Entry e of the twiddle table of an N-point row (host or device, FP64 then
