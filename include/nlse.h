@@ -203,12 +203,17 @@ int nlse_debug_operator_product(nlse_ctx *ctx, const float *w, float *out, doubl
  * Batches: many pulses, each with its own grid (Nr % 64 == 0, Nt % 256 == 0)
  * and tables, advanced together in the split-BF16 form: per z-step ONE
  * grouped tensor-core launch per half step over every pulse's tiles, and one
- * row-kernel launch per distinct Nt.  The batch owns one context per pulse.
+ * row-kernel launch per distinct (Nt, full-physics terms).  The batch owns one
+ * context per pulse.  Pulses may carry the Raman / self-steepening terms
+ * (Nt <= 4096) and the exciton channel (its two-population march runs as one
+ * launch per such pulse); space-time focusing is refused (NLSE_ERR_UNSUPPORTED:
+ * its half step has no single radial operator).
  */
 typedef struct nlse_batch nlse_batch;
 int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch **out);
 /* u[i], rho[i], rho_s[i]: device pointers of pulse i (rho_s may be NULL or
- * hold NULLs); same semantics as nlse_propagate for every pulse. */
+ * hold NULLs, except for pulses with the exciton channel); same semantics as
+ * nlse_propagate for every pulse. */
 int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const *rho,
                          float *const *rho_s, double dz, int nsteps, void *stream);
 int nlse_batch_get_context(nlse_batch *b, int i, nlse_ctx **out);

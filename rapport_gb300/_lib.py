@@ -415,8 +415,15 @@ class Batch:
         _check(self.lib, None, self.lib.nlse_batch_set_mode(self.h, int(mode)))
 
     def device_status(self):
+        """The status word of the batch's bounded waits (0: none gave up);
+        raises NLSEError when a wait gave up or a pulse's own device flags
+        report an error (e.g. a split-FP16 overflow)."""
         w = _I(0)
-        self.lib.nlse_batch_device_status(self.h, ctypes.byref(w))
+        status = self.lib.nlse_batch_device_status(self.h, ctypes.byref(w))
+        if status != NLSE_OK:
+            buf = ctypes.create_string_buffer(512)
+            self.lib.nlse_batch_get_last_error(self.h, buf, 512)
+            raise NLSEError(status, buf.value.decode(errors="replace"))
         return w.value
 
     def context(self, i):

@@ -379,12 +379,11 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
 // row_nl with the full-physics nonlinear block (Raman / self-steepening in
 // split(); three row buffers).
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
-k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-              const float *__restrict__ rho, int g) {
+__device__ __forceinline__ void row_nl_full_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
+                                                 __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+                                                 const float *__restrict__ rho, int g) {
     extern __shared__ float2 sm2[];
     const FullRows m = full_rows<NT>(sm2);
-    const int r = blockIdx.x;
     load_mw_row<NT>(m.B0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
     const float2 *R = fft_row<NT, true>(m.B0, m.B1, a.tw);
@@ -396,6 +395,13 @@ k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict
     __syncthreads();
     float2 *Y = fft_row<NT, false>(m.B0, m.B1, a.tw);
     store_state_row<NT>(Y, r, a, F32, Fb, g + 1);
+}
+
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+              const float *__restrict__ rho, int g) {
+    row_nl_full_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
 }
 
 template <int NT>
@@ -426,7 +432,8 @@ __global__ void __launch_bounds__(NLSE_ROW_THREADS)
 k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int do_scan) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
-    row_entry_body<NT>(q.a, w.y, q.u, q.F32, q.Fb, q.rho, do_scan);
+    // exciton channel: its two-population march runs as a kernel of its own
+    row_entry_body<NT>(q.a, w.y, q.u, q.F32, q.Fb, q.rho, do_scan && !q.ste_work);
 }
 
 template <int NT>
@@ -442,7 +449,19 @@ __global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(true))
 k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
-    row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1, g);
+    if (q.ste_work)  // exciton channel: hand the physical field to the two-population march
+        row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : q.ste_work, !last, 0, 1, g);
+    else
+        row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1, g);
+}
+
+// Pulses with the full-physics terms (Raman / self-steepening; one time-grid class).
+template <int NT>
+__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+k_row_nl_full_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
+    const int2 w = work[blockIdx.x];
+    const BatchPulse &q = P[w.x];
+    row_nl_full_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, g);
 }
 
 template <typename K>
@@ -499,6 +518,15 @@ cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb
 
 cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
                              int g, cudaStream_t st) {
+    if (kind == 3) {
+        NLSE_DISPATCH_NT_FULL(logNt, {
+            const size_t smem = full_smem_bytes<NT>();
+            cudaError_t e = set_smem(k_row_nl_full_b<NT>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_nl_full_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, g);
+        });
+        return cudaGetLastError();
+    }
     NLSE_DISPATCH_NT(logNt, {
         const size_t smem = row_smem_bytes<NT>(kind != 1);
         cudaError_t e;

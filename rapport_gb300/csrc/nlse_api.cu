@@ -974,7 +974,7 @@ struct nlse_batch {
     cudaStream_t cap_stream, cap_stream2;
     cudaEvent_t cap_fork, cap_join;
     cudaGraphExec_t graph;
-    int graph_key[3];        // (variant, a_terms, f16) it was captured for
+    int graph_key[4];        // (variant, a_terms, f16, buffer generation) it was captured for
     int graph_off;           // capture failed once: launch directly
     nlse_ctx **ctx;          // one context per pulse (tables, operator, state buffers)
     BatchPulse *h_pulses;    // pinned staging of the per-pulse table
@@ -984,9 +984,15 @@ struct nlse_batch {
     int ntiles;
     struct Class {
         int logNt, nblocks;
+        int full;            // its pulses have the full-physics terms (row_nl kind 3)
         int2 *d_work;
         int split;           // work entries of lane 0 (pulses [0, lane_pulse))
-    } cls[16];
+    } cls[32];
+    // pulses with the exciton channel: their two-population march runs as a
+    // kernel of its own after row_next (its pointers are launch arguments, so
+    // a change of buffers re-captures the graph: ptr_gen)
+    int *ste_idx, nste;
+    int ptr_gen, graph_gen;
     // two lanes (pulses [0, lane_pulse) and the rest) run as parallel branches
     // of the z-step graph, so one lane's row kernels fill the other's GEMM tail
     int lane_pulse, lane_tiles;  // lane 0's pulses / tiles (tiles are in pulse order)
@@ -1003,6 +1009,7 @@ static void batch_free(nlse_batch *b) {
     if (b->ctx)
         for (int i = 0; i < b->n; ++i) nlse_destroy(b->ctx[i]);
     free(b->ctx);
+    free(b->ste_idx);
     if (b->h_pulses) cudaFreeHost(b->h_pulses);
     void *ptrs[] = {b->d_pulses, b->d_maps, b->d_tiles, b->d_flag};
     for (void *p : ptrs)
@@ -1018,9 +1025,31 @@ static void batch_free(nlse_batch *b) {
     free(b);
 }
 
-// One non-final or final z-step of the batch on stream st: GEMM, row_nl
-// (consumes input g), GEMM, row_next (consumes g + 1; writes input g + 2 and
-// marches the carriers unless last).
+// The two-population march of the exciton-channel pulses of a lane (0 or 1;
+// -1: all) on the physical fields row_next left in their workspaces.
+static cudaError_t batch_ste_marches(nlse_batch *b, int lane, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < b->nste && e == cudaSuccess; ++j) {
+        const int i = b->ste_idx[j];
+        if (lane >= 0 && (i < b->lane_pulse) != (lane == 0)) continue;
+        const BatchPulse &P = b->h_pulses[i];
+        // a.rho_s is the caller's writable rho_s[i] (const only for the row kernels)
+        e = launch_rate_scan(b->ctx[i], P.ste_work, P.rho, const_cast<float *>(P.a.rho_s), 1, st);
+    }
+    return e;
+}
+
+// The first march of the exciton-channel pulses, on the input fields u.
+static cudaError_t batch_ste_marches_on(nlse_batch *b, void *const *u, cudaStream_t st) {
+    cudaError_t e = cudaSuccess;
+    for (int j = 0; j < b->nste && e == cudaSuccess; ++j) {
+        const int i = b->ste_idx[j];
+        e = launch_rate_scan(b->ctx[i], (const float2 *)u[i], b->h_pulses[i].rho,
+                             const_cast<float *>(b->h_pulses[i].a.rho_s), 1, st);
+    }
+    return e;
+}
+
 // One z-step of one lane (0 or 1; -1: all pulses) on stream st: GEMM, row_nl
 // (consumes input g), GEMM, row_next (consumes g + 1; writes input g + 2 and
 // marches the carriers unless last).
@@ -1037,18 +1066,20 @@ static cudaError_t batch_zstep(nlse_batch *b, int g, int last, int lane, cudaStr
             const int w0 = lane == 1 ? b->cls[k].split : 0;
             const int nw = lane < 0 ? b->cls[k].nblocks
                                     : (lane == 0 ? b->cls[k].split : b->cls[k].nblocks - b->cls[k].split);
+            const int kind = half == 1 ? 2 : (b->cls[k].full ? 3 : 1);
             if (nw > 0)
-                e = launch_row_batch(half == 0 ? 1 : 2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work + w0, nw,
+                e = launch_row_batch(kind, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work + w0, nw,
                                      half == 0 ? 0 : last, g + half, st);
         }
     }
+    if (e == cudaSuccess && !last) e = batch_ste_marches(b, lane, st);
     return e;
 }
 
 // The graph of three non-final z-steps for the batch's current launch
 // configuration; NULL (and direct launches from then on) if capture fails.
 static cudaGraphExec_t batch_graph(nlse_batch *b) {
-    const int key[3] = {b->ctx[0]->gemm_variant, b->a_terms, b->f16};
+    const int key[4] = {b->ctx[0]->gemm_variant, b->a_terms, b->f16, b->nste ? b->ptr_gen : 0};
     if (b->graph && !memcmp(key, b->graph_key, sizeof(key))) return b->graph;
     if (b->graph_off) return nullptr;
     if (b->graph) {
@@ -1121,14 +1152,17 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
             BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: batches run the split-BF16 form, which needs Nr %% 64 == 0 "
                                              "and Nt %% 256 == 0",
                        i);
-        if (b->ctx[i]->sc.ste || b->ctx[i]->full_nl)
+        if (b->ctx[i]->d_P2)
             BATCH_FAIL(NLSE_ERR_UNSUPPORTED,
-                       "pulse %d: the exciton channel and the full-physics split run on single contexts only", i);
+                       "pulse %d: space-time focusing makes the diffraction phase depend on Omega (no single radial "
+                       "operator for the tensor-core product): run it on its own context in the plain mode",
+                       i);
     }
     std::vector<GemmTile> tiles;
     std::vector<CUtensorMap> maps(4 * (size_t)n);
-    int logs[16], nlog = 0;
-    std::vector<std::vector<int2>> work(16);
+    int logs[32], fulls[32], nlog = 0;
+    std::vector<std::vector<int2>> work(32);
+    std::vector<int> ste;
     for (int i = 0; i < n; ++i) {
         nlse_ctx *c = b->ctx[i];
         // pulses built from the same QDHT tables and k0 have the same operator
@@ -1147,10 +1181,21 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         const int M = 2 * c->Nr;
         for (int m0 = 0; m0 < M; m0 += 128)
             for (int n0 = 0; n0 < c->Nt; n0 += 256) tiles.push_back(GemmTile{i, m0, n0, 0});
+        // row classes: one per (N_t, full-physics terms)
         int k = 0;
-        while (k < nlog && logs[k] != c->logNt) ++k;
-        if (k == nlog) logs[nlog++] = c->logNt;
+        while (k < nlog && (logs[k] != c->logNt || fulls[k] != c->full_nl)) ++k;
+        if (k == nlog) {
+            logs[nlog] = c->logNt;
+            fulls[nlog++] = c->full_nl;
+        }
         for (int r = 0; r < c->Nr; ++r) work[k].push_back(make_int2(i, r));
+        if (c->sc.ste) ste.push_back(i);
+    }
+    b->nste = (int)ste.size();
+    if (b->nste) {
+        b->ste_idx = (int *)malloc(ste.size() * sizeof(int));
+        if (!b->ste_idx) BATCH_FAIL(NLSE_ERR_INVALID_ARG, "out of host memory");
+        memcpy(b->ste_idx, ste.data(), ste.size() * sizeof(int));
     }
     b->ntiles = (int)tiles.size();
     // lane 0 = the first pulses up to about half of the tiles
@@ -1179,6 +1224,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
     b->ncls = nlog;
     for (int k = 0; k < nlog && e == cudaSuccess; ++k) {
         b->cls[k].logNt = logs[k];
+        b->cls[k].full = fulls[k];
         b->cls[k].nblocks = (int)work[k].size();
         b->cls[k].split = 0;
         for (const int2 &w : work[k]) b->cls[k].split += w.x < b->lane_pulse;
@@ -1221,7 +1267,19 @@ extern "C" int nlse_batch_device_status(nlse_batch *b, int *word) {
     int h[4];
     NLSE_CUDA_TRY(&b->err, cudaMemcpy(h, b->d_flag, sizeof(h), cudaMemcpyDeviceToHost));
     if (word) *word = h[0];
-    return h[0] ? NLSE_ERR_TIMEOUT : NLSE_OK;
+    if (h[0]) {
+        nlse_set_error(&b->err, NLSE_ERR_TIMEOUT, "a bounded device wait gave up (status word 0x%x)", h[0]);
+        return NLSE_ERR_TIMEOUT;
+    }
+    // every pulse's own flags (its exciton march, the split-FP16 overflow count)
+    for (int i = 0; i < b->n; ++i) {
+        const int s = nlse_device_status(b->ctx[i], nullptr);
+        if (s != NLSE_OK) {
+            nlse_set_error(&b->err, s, "pulse %d: %s", i, b->ctx[i]->err.msg);
+            return s;
+        }
+    }
+    return NLSE_OK;
 }
 
 extern "C" int nlse_batch_get_last_error(const nlse_batch *b, char *buf, size_t len) {
@@ -1245,7 +1303,8 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
     nlse_ctx *c = b->ctx[0];  // profiling records go to the first pulse's context
     bool changed = !(dz == b->last_dz) || !b->uploaded || b->last_f16 != b->f16;
     for (int i = 0; i < b->n; ++i) {
-        if (!field_ok(b->ctx[i], u[i], "u") || !field_ok(b->ctx[i], rho[i], "rho")) {
+        if (!field_ok(b->ctx[i], u[i], "u") || !field_ok(b->ctx[i], rho[i], "rho") ||
+            !ste_ok(b->ctx[i], rho_s ? rho_s[i] : nullptr)) {
             nlse_set_error(&b->err, NLSE_ERR_INVALID_ARG, "pulse %d: %s", i, b->ctx[i]->err.msg);
             return NLSE_ERR_INVALID_ARG;
         }
@@ -1254,7 +1313,10 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
             nlse_set_error(&b->err, s, "pulse %d: %s", i, b->ctx[i]->err.msg);
             return s;
         }
-        if (b->uploaded && (b->h_pulses[i].u != (float2 *)u[i] || b->h_pulses[i].rho != rho[i])) changed = true;
+        const float *rs_i = b->ctx[i]->sc.ste ? rho_s[i] : nullptr;
+        if (b->uploaded && (b->h_pulses[i].u != (float2 *)u[i] || b->h_pulses[i].rho != rho[i] ||
+                            b->h_pulses[i].a.rho_s != rs_i))
+            changed = true;
     }
     if (changed) {
         // the previous upload must be consumed before the staging buffer is rewritten
@@ -1268,6 +1330,8 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
             P.D = q->d_D;
             P.rho = rho[i];
             P.u = (float2 *)u[i];
+            P.a.rho_s = q->sc.ste ? rho_s[i] : nullptr;
+            P.ste_work = q->sc.ste ? q->d_work : nullptr;
             P.M = 2 * q->Nr;
             P.N = q->Nt;
             P.K = 2 * q->Nr;
@@ -1278,10 +1342,12 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
         b->last_dz = dz;
         b->last_f16 = b->f16;
         b->uploaded = 1;
+        ++b->ptr_gen;
     }
+    // rho_s of a pulse without the exciton channel stays zero (its march writes none)
     if (rho_s)
         for (int i = 0; i < b->n; ++i)
-            if (rho_s[i])
+            if (rho_s[i] && !b->ctx[i]->sc.ste)
                 NLSE_CUDA_TRY(&b->err, cudaMemsetAsync(rho_s[i], 0,
                                                        (size_t)b->ctx[i]->Nr * b->ctx[i]->Nt * sizeof(float), st));
 #define BSEQ(kid, call, what)                                                          \
@@ -1299,6 +1365,8 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
                  launch_field_bound((const float2 *)u[i], (size_t)b->ctx[i]->Nr * b->ctx[i]->Nt, b->ctx[i]->Nt,
                                     b->ctx[i]->d_scale, st),
                  "batch field bound");
+    // the exciton-channel pulses' first march (the entry kernel skips theirs)
+    if (b->nste) BSEQ(K_RATE_SCAN, batch_ste_marches_on(b, u, st), "batch exciton march");
     for (int k = 0; k < b->ncls; ++k)
         BSEQ(K_ROW_ENTRY,
              launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, -1, st),
@@ -1319,8 +1387,8 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
              "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NL,
-                 launch_row_batch(1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 0, 2 * it,
-                                  st),
+                 launch_row_batch(b->cls[k].full ? 3 : 1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work,
+                                  b->cls[k].nblocks, 0, 2 * it, st),
                  "batch row nonlinear");
         BSEQ(K_GEMM_TC,
              launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
@@ -1331,6 +1399,7 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
                  launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last,
                                   2 * it + 1, st),
                  "batch row next");
+        if (!last && b->nste) BSEQ(K_RATE_SCAN, batch_ste_marches(b, -1, st), "batch exciton march");
     }
 #undef BSEQ
     return NLSE_OK;

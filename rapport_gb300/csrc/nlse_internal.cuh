@@ -104,12 +104,14 @@ struct RowFusedArgs {
 
 // One pulse of a batch, as the batched kernels see it (device memory).
 struct BatchPulse {
-    RowFusedArgs a;
+    RowFusedArgs a;       // a.rho_s: the exciton density (channel on) or NULL
     float *F32;
     __nv_bfloat16 *Fb;
     float *D;
     float *rho;
     float2 *u;
+    float2 *ste_work;     // exciton channel: row_next writes the physical field here and
+                          // the two-population march runs as its own kernel (else NULL)
     int M, N, K;  // GEMM sizes: 2Nr, Nt, 2Nr
 };
 
@@ -227,7 +229,8 @@ void nlse_set_thread_error(int status, const char *msg);
 cudaError_t launch_record(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, const int *bin_of_t,
                           int nbins, double *out, cudaStream_t st);
 cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st);
-// kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call);
+// kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call),
+// 3 = nonlinear with the full-physics block (N_t <= 4096);
 // g = index of the GEMM input the kernel consumes (the split-FP16 scales; -1 for the entry)
 cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
                              int g, cudaStream_t st);

@@ -80,8 +80,10 @@ def summarize(results):
 
 
 def _batchable(cfg):
-    return (cfg.linear_mode == "split_bf16" and (cfg.N - 1) % 64 == 0 and cfg.Nt % 256 == 0 and not cfg.enable_ste
-            and not cfg.enable_kerr_raman and not cfg.enable_self_steepening and not cfg.enable_space_time_focusing)
+    # a batch takes the Raman / self-steepening terms and the exciton channel;
+    # space-time focusing has no single radial operator (plain mode, own context)
+    return (cfg.linear_mode == "split_bf16" and (cfg.N - 1) % 64 == 0 and cfg.Nt % 256 == 0
+            and not cfg.enable_space_time_focusing)
 
 
 class _Group:

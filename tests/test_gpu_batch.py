@@ -1,4 +1,4 @@
-"""Batches of pulses with uneven grids (nlse_batch_*), split-BF16 form.
+"""Batches of pulses with uneven grids (nlse_batch_*), split-BF16 / split-FP16 forms.
 
 A batch runs the same per-pulse arithmetic as a single-pulse context (grouped
 tensor-core launch over every pulse's tiles, one row launch per time-grid
@@ -136,3 +136,81 @@ def test_batch_f16_equals_single_contexts():
         uo, _, _ = og.propagate(u0.copy(), STEPS, DZ)
         assert rel_l2(host(us[i]), uo) < 5e-5, i
         assert ctx.device_status() == 0
+
+
+# (Nr, Nt, overrides): the measured toggles, Raman + self-steepening, the
+# exciton channel, and both -- one batch, three row classes
+MIXED = [(64, 256, {}),
+         (64, 256, dict(f_R=0.18, enable_kerr_raman=True, enable_self_steepening=True)),
+         (128, 512, dict(enable_ste=True, tau_ste=1e-12)),
+         (64, 512, dict(enable_ste=True, tau_ste=5e-13, f_R=0.18, enable_kerr_raman=True))]
+
+
+def _mixed_setup():
+    import rapport_gb300 as R
+    cfgs, grids, u0s = [], [], []
+    for i, (Nr, Nt, over) in enumerate(MIXED):
+        # ~1 uJ at w0 15 um: at 5 uJ / 10 um self-steepening on this 256-point
+        # window already diverges in the FP64 oracle within six steps
+        cfg = R.workload_config(Nr, Nt, 1e-4 * Nr / 64, 1.5e-5, 3e-13 * Nt / 256, DZ, STEPS, **over)
+        g = R.build_grids(cfg)
+        cfgs.append(cfg)
+        grids.append(g)
+        u0s.append(R.envelope_lens(1.5e-5, 100e-15, 1.0 + 0.1 * i, 1e-2, 20 + i)(g["rr"], g["tt"], cfg, g))
+    return cfgs, grids, u0s
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_full_physics_and_exciton_pulses_equal_single_contexts(mode):
+    """Raman / self-steepening pulses (their own row class) and exciton-channel
+    pulses (their two-population march launched per pulse, also inside the
+    z-step graph) in one batch: each bit-identical to its single-context run,
+    including after a second call on new buffers (the graph is re-captured)."""
+    from rapport_gb300 import _lib
+    cfgs, grids, u0s = _mixed_setup()
+    b = _lib.Batch(cfgs, grids)
+    b.set_mode(mode)
+    runs = []
+    for _ in range(2):  # the second call passes new tensors (new pointers)
+        us = [dev(u) for u in u0s]
+        rhos = [dev(np.zeros(u.shape)) for u in u0s]
+        rss = [dev(np.ones(u.shape)) for u in u0s]
+        b.propagate(us, rhos, rss, DZ, STEPS)
+        assert b.device_status() == 0
+        runs.append(([host(x) for x in us], [host(x) for x in rhos], [host(x) for x in rss]))
+    for i, (cfg, g, u0) in enumerate(zip(cfgs, grids, u0s)):
+        ctx = _lib.Context(cfg, g)
+        u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+        ctx.propagate(u, rho, rs, DZ, STEPS, mode)
+        assert ctx.device_status() == 0
+        for bu, brho, brs in runs:
+            assert np.array_equal(bu[i], host(u)), i
+            assert np.array_equal(brho[i], host(rho)), i
+            assert np.array_equal(brs[i], host(rs)), i
+        ste = bool(MIXED[i][2].get("enable_ste"))
+        assert (host(rs).max() > 0) == ste, i  # exciton density only where the channel is on
+        Nr, Nt, over = MIXED[i]
+        og = O.OracleGrid(O.workload_config(Nr, Nt, 1e-4 * Nr / 64, 1.5e-5, 3e-13 * Nt / 256, **over))
+        uo, rho_o, rs_o = og.propagate(O.lens_gaussian(og, 1.5e-5, 100e-15, 1.0 + 0.1 * i, 1e-2, 20 + i), STEPS, DZ)
+        assert rel_l2(host(u), uo) < 5e-5, i
+        assert np.abs(host(rho) - rho_o).max() <= 1e-3 * rho_o.max(), i
+        if ste:
+            assert np.abs(host(rs) - rs_o).max() <= 1e-3 * rs_o.max(), i
+
+
+def test_batch_exciton_pulse_needs_rho_s():
+    from rapport_gb300 import _lib
+    cfgs, grids, u0s = _mixed_setup()
+    b = _lib.Batch(cfgs, grids)
+    us = [dev(u) for u in u0s]
+    rhos = [dev(np.zeros(u.shape)) for u in u0s]
+    with pytest.raises(_lib.NLSEError, match="rho_s is required"):
+        b.propagate(us, rhos, None, DZ, STEPS)
+
+
+def test_batch_rejects_space_time_focusing():
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, DZ, 1, enable_space_time_focusing=True)
+    with pytest.raises(_lib.NLSEError, match="space-time focusing"):
+        _lib.Batch([cfg], [R.build_grids(cfg)])

@@ -141,6 +141,7 @@ def test_full_physics_limits():
     cfg = R.workload_config(16, 8192, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_self_steepening=True)
     with pytest.raises(_lib.NLSEError, match="4096"):
         _lib.Context(cfg, R.build_grids(cfg))
-    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, 5e-6, 1, f_R=0.18, enable_kerr_raman=True)
-    with pytest.raises(_lib.NLSEError, match="single contexts"):
+    # a batch takes Raman / self-steepening pulses but not space-time focusing
+    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_space_time_focusing=True)
+    with pytest.raises(_lib.NLSEError, match="space-time focusing"):
         _lib.Batch([cfg], [R.build_grids(cfg)])

@@ -149,11 +149,3 @@ def test_propagate_equals_update_plus_step(ste):
             assert rel_l2(host(u1), host(u2)) < 1e-6
         assert rel_l2(host(r1), host(r2)) < 1e-5
         assert rel_l2(host(s1), host(s2)) < 1e-5
-
-
-def test_batch_rejects_ste():
-    import rapport_gb300 as R
-    from rapport_gb300 import _lib
-    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_ste=True)
-    with pytest.raises(_lib.NLSEError, match="exciton"):
-        _lib.Batch([cfg], [R.build_grids(cfg)])

@@ -1,6 +1,7 @@
 """The scenario-sweep driver on the GPU: scenarios run together (one batch for
-the batchable ones, own streams for the rest) give exactly what run() gives
-for each alone, and cached results are reused."""
+the batchable ones -- the exciton channel and the Raman / self-steepening terms
+included -- own streams for the rest) give exactly what run() gives for each
+alone, and cached results are reused."""
 import os
 
 import numpy as np
@@ -20,7 +21,11 @@ KEYS = ("fluence_rz", "rho_rz", "Imax_z", "absorbed_rz", "E_total_z", "rho_onaxi
 def test_sweep_equals_individual_runs(tmp_path):
     sc = R.energy_scenarios([1.0, 2.0, 3.0], prefix="e")
     sc["plain_2uJ"] = {"energy_uJ": 2.0, "linear_mode": "plain"}            # own stream
-    sc["ste_2uJ"] = {"energy_uJ": 2.0, "enable_ste": True}                  # not batchable
+    sc["ste_2uJ"] = {"energy_uJ": 2.0, "enable_ste": True}                  # batched: own march launch
+    sc["raman_2uJ"] = {"energy_uJ": 2.0, "f_R": 0.18, "enable_kerr_raman": True,
+                       "enable_self_steepening": True}                      # batched: own row class
+    sc["stf_2uJ"] = {"energy_uJ": 2.0, "enable_space_time_focusing": True,
+                     "linear_mode": "plain"}                                # own stream
     got = R.run_scenarios(BASE, sc, tmp_path / "sweep")
     for name, over in sc.items():
         ref = R.run(**{**BASE, **over, "out_dir": str(tmp_path / "single" / name)})
