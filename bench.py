@@ -483,6 +483,92 @@ def run_reference(args, rank):
     }), flush=True)
 
 
+# ------------------------------------------------------------------ config 5: one large pulse
+CONFIG5 = dict(Nr=2048, Nt=8192, R_max=3e-3, w0=200e-6, T_half=1.5e-12, fwhm=80e-15, E=20.0, f=0.15, dz=1.25e-6,
+               seed=0)
+# algorithmic bytes per point of the row / elementwise kernels, FLOPs per launch of the products
+ROW_BYTES = {"k_row_nl": 36.0, "k_row_next": 36.0, "k_row_entry": 28.0, "k_fft_phase_ifft": 16.0,
+             "k_nonlinear_step": 20.0, "k_rate_scan": 12.0, "k_split": 24.0}
+
+
+def run_config5(args, rank, world, local_rank):
+    """One 2048 x 8192 pulse (20 uJ, 80 fs, w0 200 um, f 15 cm, dz 1.25 um): z-steps/s of each
+    arithmetic and the roofline fraction of every kernel (per-launch CUDA events)."""
+    import torch
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    c5 = CONFIG5
+    Z = args.zsteps
+    cfg = R.workload_config(c5["Nr"], c5["Nt"], c5["R_max"], c5["w0"], c5["T_half"], c5["dz"], Z)
+    g = R.build_grids(cfg)
+    ctx = _lib.Context(cfg, g)
+    u0 = R.envelope_lens(c5["w0"], c5["fwhm"], c5["E"], c5["f"], c5["seed"])(g["rr"], g["tt"], cfg, g)
+    u0 = np.ascontiguousarray(u0.astype(np.complex64))
+    hbm, bf16, bf16_s, src = peaks()
+    Nr, Nt = c5["Nr"], c5["Nt"]
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    modes = [("split_bf16", _lib.MODE_SPLIT_BF16), ("split_f16", _lib.MODE_SPLIT_F16), ("plain", _lib.MODE_PLAIN_F32)]
+    forms, kernels, clocks = {}, {}, None
+    for name, mode in modes:
+        u = torch.from_numpy(u0).to(dev)
+        rho = torch.zeros(u.shape, dtype=torch.float32, device=dev)
+        rs = torch.zeros_like(rho)
+        K = args.steps if name != "plain" else max(2, args.steps // 3)
+        for _ in range(args.warmup):
+            ctx.propagate(u, rho, rs, c5["dz"], Z, mode)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
+        clk = ClockSampler(local_rank) if name == "split_bf16" else None
+        for i in range(K):
+            flush.fill_(float(i))
+            ev[i][0].record()
+            ctx.propagate(u, rho, rs, c5["dz"], Z, mode)
+            ev[i][1].record()
+        torch.cuda.synchronize()
+        if clk:
+            clocks = clk.stop()
+        t_ms = sum(a.elapsed_time(b) for a, b in ev)
+        forms[name] = round(K * Z / (t_ms * 1e-3), 2)
+        ctx.profile_start(K * Z * 16 + 64)
+        for i in range(K):
+            flush.fill_(float(i))
+            ctx.propagate(u, rho, rs, c5["dz"], Z, mode)
+        prof = ctx.profile_read()
+        assert ctx.device_status() == 0 and bool(torch.isfinite(u).all().item())
+        per = {}
+        for k, (n, ms) in prof.items():
+            avg_s = ms / n * 1e-3
+            e = {"launches": n, "avg_us": round(avg_s * 1e6, 1), "share": round(ms / sum(v[1] for v in
+                                                                                         prof.values()), 3)}
+            if k == "k_gemm_tc":
+                ach = 8.0 * Nr * Nr * Nt / avg_s / 1e12
+                e.update(bound="tensor", achieved_tflops=round(ach, 1), frac=round(ach / bf16_s, 3),
+                         executed_tflops=round((3 if name == "split_f16" else 4) * ach, 1))
+            elif k == "k_gemm_f32":
+                e.update(bound="fp32 SIMT", achieved_tflops=round(4.0 * Nr * Nr * Nt / avg_s / 1e12, 1))
+            elif k in ROW_BYTES:
+                ach = ROW_BYTES[k] * Nr * Nt / avg_s / 1e9
+                e.update(bound="hbm", achieved_gbs=round(ach, 1), frac=round(ach / hbm, 3))
+            per[k] = e
+        kernels[name] = per
+        del u, rho, rs
+    line = {
+        "metric": "z-steps/s (1 GB300), config 5: one 2048x8192 pulse", "value": forms["split_bf16"],
+        "unit": "z-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
+        "scaling": "weak", "dtype": "bf16x3-split + f32", "data": "synthetic (seeded lens-focused Gaussian, 1% noise)",
+        "config": {"workload": "single pulse, N_r=2048 (R_max 3 mm) x N_t=8192 (+-1.5 ps), 20 uJ, 80 fs, w0 200 um, "
+                               "f 15 cm, 1% noise seed 0, K=6 MPI + avalanche + recombination, dz 1.25 um",
+                   "z_steps_per_step": Z, "l2": "256 MB flush before each timed step; field 134 MB"},
+        "forms": forms, "speedup_vs_plain_fp32": forms["split_bf16"] / forms["plain"],
+        "peaks": {"hbm_gbs": hbm, "bf16_tflops_sustained": bf16_s, "source": src},
+        "kernels": kernels, "clocks": clocks,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -496,7 +582,7 @@ def main():
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=8, help="pulses of the batched (headline) form; 0 = single pulse")
-    ap.add_argument("--workload", default="single", choices=["single", "config4"])
+    ap.add_argument("--workload", default="single", choices=["single", "config4", "config5"])
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -506,6 +592,9 @@ def main():
         return
     if args.workload == "config4":
         run_config4(args, rank, world, local_rank)
+        return
+    if args.workload == "config5":
+        run_config5(args, rank, world, local_rank)
         return
     run_ours(args, rank, world, local_rank)
 

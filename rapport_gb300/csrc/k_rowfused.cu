@@ -35,9 +35,18 @@ __device__ __forceinline__ int f16_field_exp(const int *scale, int g) {
     return min(max(7 - e, -100), 100);
 }
 
-// Block-wide max of a non-negative float (all threads; result valid in thread 0).
+// Threads per CTA of the split-form row kernels: 256 (8 points each at
+// N_t = 2048), 1024 at N_t = 8192, whose 139 KB of row buffers admit one CTA
+// per SM (256 threads would leave the SM with 8 warps).  The full-physics
+// row kernels (N_t <= 4096) keep 256.
+template <int NT>
+__host__ __device__ constexpr int row_threads() {
+    return NT >= 8192 ? 1024 : NLSE_ROW_THREADS;
+}
+
+// Block-wide max of a non-negative float (all threads, up to 1024; result valid in thread 0).
 __device__ __forceinline__ float block_max(float v) {
-    __shared__ float red[NLSE_ROW_THREADS / 32];
+    __shared__ float red[32];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
     if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
@@ -139,7 +148,7 @@ __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs
 template <int NT>
 __device__ __forceinline__ void march_scan(float *sI, float2 *Rb, float *X, int r, const RowFusedArgs &a,
                                            float *rho) {
-    constexpr int S = scan_span(NT, NLSE_ROW_THREADS);
+    constexpr int S = scan_span(NT, row_threads<NT>());
     const ScanLayout L = scan_layout(NT);
     float *sW = sI + S;
     __syncthreads();
@@ -168,7 +177,7 @@ __device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float 
 // must fit in fft_slots(NT) float2, which holds for every NT >= 16 with 256 threads.
 template <int NT>
 __host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
-    constexpr int span = scan_span(NT, NLSE_ROW_THREADS);
+    constexpr int span = scan_span(NT, row_threads<NT>());
     static_assert(2 * span <= 2 * fft_slots(NT), "scan arrays must fit in the FFT buffers");
     return 2 * (size_t)fft_slots(NT) * sizeof(float2) + (with_march ? (size_t)span * sizeof(float) : 0);
 }
@@ -312,7 +321,7 @@ __device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, con
         b0[pidx(t + 1)] = make_float2(v.z, v.w);
     }
     __syncthreads();
-    float2 *R = fft_row<NT, false>(b0, b1, a.tw);
+    float2 *R = fft_row<NT, false, row_threads<NT>()>(b0, b1, a.tw);
     store_state_row<NT>(R, r, a, F32, Fb, 0);
     if (!do_scan) return;
     __syncthreads();
@@ -332,7 +341,7 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
     load_mw_row<NT>(b0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
-    float2 *R = fft_row<NT, true>(b0, b1, a.tw);
+    float2 *R = fft_row<NT, true, row_threads<NT>()>(b0, b1, a.tw);
     const float *gr = rho + (size_t)r * NT;
     const float *gs = a.rho_s ? a.rho_s + (size_t)r * NT : nullptr;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
@@ -342,7 +351,7 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
         R[pidx(t + 1)] = nl_point(R[pidx(t + 1)], rr.y, rs.y, a.dz, a.nl, a.pchip);
     }
     __syncthreads();
-    float2 *Y = fft_row<NT, false>(R, R == b0 ? b1 : b0, a.tw);
+    float2 *Y = fft_row<NT, false, row_threads<NT>()>(R, R == b0 ? b1 : b0, a.tw);
     store_state_row<NT>(Y, r, a, F32, Fb, g + 1);
 }
 
@@ -363,7 +372,7 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
     __syncthreads();
     if (write_state) store_state_row<NT>(b0, r, a, F32, Fb, g + 1);
     if (!do_scan && !u_out) return;
-    float2 *R = fft_row<NT, true>(b0, b1, a.tw);
+    float2 *R = fft_row<NT, true, row_threads<NT>()>(b0, b1, a.tw);
     const float inv = 1.0f / (float)NT;
     if (u_out) {
         float2 *g = u_out + (size_t)r * NT;
@@ -405,21 +414,21 @@ k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(row_threads<NT>())
 k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb,
             float *__restrict__ rho, int do_scan) {
     row_entry_body<NT>(a, blockIdx.x, u, F32, Fb, rho, do_scan);
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(false))
+__global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(false))
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
          const float *__restrict__ rho, int g) {
     row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(true))
+__global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(true))
 k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
            float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask, int g) {
     row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
@@ -428,7 +437,7 @@ k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ 
 // ------------------------------------------------------------------ batched (many pulses, one time-grid class)
 // work[b] = (pulse, row) for CTA b; every pulse of the class has the same N_t.
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(row_threads<NT>())
 k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int do_scan) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
@@ -437,7 +446,7 @@ k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, i
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(false))
+__global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(false))
 k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
@@ -445,7 +454,7 @@ k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int 
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, row_min_blocks<NT>(true))
+__global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(true))
 k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
@@ -477,7 +486,7 @@ cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32,
         const size_t smem = row_smem_bytes<NT>(true);
         cudaError_t e = set_smem(k_row_entry<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_entry<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, u, F32, Fb, rho, do_scan);
+        k_row_entry<NT><<<a.Nr, row_threads<NT>(), smem, st>>>(a, u, F32, Fb, rho, do_scan);
     });
     return cudaGetLastError();
 }
@@ -499,7 +508,7 @@ cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, 
         const size_t smem = row_smem_bytes<NT>(false);
         cudaError_t e = set_smem(k_row_nl<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_nl<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, g);
+        k_row_nl<NT><<<a.Nr, row_threads<NT>(), smem, st>>>(a, F32, Fb, D, rho, g);
     });
     return cudaGetLastError();
 }
@@ -510,7 +519,7 @@ cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb
         const size_t smem = row_smem_bytes<NT>(true);
         cudaError_t e = set_smem(k_row_next<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_next<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan,
+        k_row_next<NT><<<a.Nr, row_threads<NT>(), smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan,
                                                               apply_mask, g);
     });
     return cudaGetLastError();
@@ -533,15 +542,15 @@ cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int
         if (kind == 0) {
             e = set_smem(k_row_entry_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_entry_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, flag);
+            k_row_entry_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag);
         } else if (kind == 1) {
             e = set_smem(k_row_nl_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, g);
+            k_row_nl_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, g);
         } else {
             e = set_smem(k_row_next_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_next_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, flag, g);
+            k_row_next_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag, g);
         }
     });
     return cudaGetLastError();
