@@ -35,12 +35,19 @@ __device__ __forceinline__ int f16_field_exp(const int *scale, int g) {
     return min(max(7 - e, -100), 100);
 }
 
-// Threads per CTA of the split-form row kernels: 256 (8 points each at
-// N_t = 2048), 1024 at N_t = 8192, whose 139 KB of row buffers admit one CTA
-// per SM (256 threads would leave the SM with 8 warps).  The full-physics
-// row kernels (N_t <= 4096) keep 256.
+// Threads per CTA of row_entry / row_next: 8 points each from N_t = 2048 on
+// (256, 512 at 4096, 1024 at 8192), so rows whose buffers admit only 1-2 CTAs
+// per SM still give it 32 warps; 256 below 2048.  The full-physics row
+// kernels (N_t <= 4096) keep 256.
 template <int NT>
 __host__ __device__ constexpr int row_threads() {
+    return NT >= 8192 ? 1024 : (NT == 4096 ? 512 : NLSE_ROW_THREADS);
+}
+
+// row_nl (no march, two shared-memory row buffers) measured faster with 256
+// threads up to N_t = 4096 (three CTAs per SM there), 1024 at 8192.
+template <int NT>
+__host__ __device__ constexpr int row_threads_nl() {
     return NT >= 8192 ? 1024 : NLSE_ROW_THREADS;
 }
 
@@ -183,8 +190,8 @@ __host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
 }
 
 // ------------------------------------------------ register-resident row_next
-// For N_t = 2048 (8 points per thread) row_next keeps its row in registers:
-// thread tid holds the points tid + 256 m.  Loads, the state stores, the
+// From N_t = 2048 on (8 points per thread) row_next keeps its row in registers:
+// thread tid of T holds the points tid + T m.  Loads, the state stores, the
 // inverse FFT (fft_regs), the physical field and the march's intensities act
 // on those points in place, so the row crosses shared memory only inside the
 // FFT; the arithmetic per point is that of the shared-memory body (results
@@ -192,11 +199,11 @@ __host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
 // shared-memory body with its two-point vector accesses measured faster.)
 template <int NT>
 __host__ __device__ constexpr bool row_regs() {
-    return fft_regs_ok<NT, NLSE_ROW_THREADS>() && NT / NLSE_ROW_THREADS == 8;
+    return fft_regs_ok<NT, row_threads<NT>()>() && NT / row_threads<NT>() == 8;
 }
 
 template <int NT>
-__device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / NLSE_ROW_THREADS], int r, const RowFusedArgs &a,
+__device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / row_threads<NT>()], int r, const RowFusedArgs &a,
                                              const float *F32, const float *D, float scale, int g_in) {
     const float ds = a.f16 ? ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) +
                                             __ldcg(&a.scale[NLSE_SC_SB + g_in % 2])))
@@ -204,8 +211,8 @@ __device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / NLSE_ROW_THREADS],
     const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nr + r) * NT;
     const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nr + r) * NT;
 #pragma unroll
-    for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
-        const int t = (int)threadIdx.x + m * NLSE_ROW_THREADS;
+    for (int m = 0; m < NT / row_threads<NT>(); ++m) {
+        const int t = (int)threadIdx.x + m * row_threads<NT>();
         const float2 x = make_float2(fmaf(dr[t], ds, fr[t]), fmaf(di[t], ds, fi[t]));
         const float2 pt = __ldg(a.Pt + t);
 #if NLSE_COMP_TWIDDLE
@@ -217,7 +224,7 @@ __device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / NLSE_ROW_THREADS],
 }
 
 template <int NT>
-__device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / NLSE_ROW_THREADS], int r,
+__device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / row_threads<NT>()], int r,
                                                  const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, int g_out) {
     const size_t rows = 2 * (size_t)a.Nr;
     float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nr + r) * NT;
@@ -225,8 +232,8 @@ __device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / NLSE_ROW
     __nv_bfloat16 *lre = hre + rows * NT, *lim = him + rows * NT;
     if (!a.f16) {
 #pragma unroll
-        for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
-            const int t = (int)threadIdx.x + m * NLSE_ROW_THREADS;
+        for (int m = 0; m < NT / row_threads<NT>(); ++m) {
+            const int t = (int)threadIdx.x + m * row_threads<NT>();
             re[t] = v[m].x;
             im[t] = v[m].y;
             const __nv_bfloat16 hx = __float2bfloat16_rn(v[m].x), hy = __float2bfloat16_rn(v[m].y);
@@ -243,8 +250,8 @@ __device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / NLSE_ROW
     const float sc = ldexpf(1.0f, sb);
     float mx = 0.0f;
 #pragma unroll
-    for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
-        const int t = (int)threadIdx.x + m * NLSE_ROW_THREADS;
+    for (int m = 0; m < NT / row_threads<NT>(); ++m) {
+        const int t = (int)threadIdx.x + m * row_threads<NT>();
         re[t] = v[m].x;
         im[t] = v[m].y;
         mx = fmaxf(mx, fmaxf(fabsf(v[m].x), fabsf(v[m].y)));
@@ -275,36 +282,38 @@ __device__ __forceinline__ void row_next_regs(const RowFusedArgs &a, int r, floa
                                               int do_scan, int apply_mask, int g) {
     extern __shared__ float2 sm2[];
     float2 *A = sm2, *B = sm2 + fft_slots(NT);
-    float2 v[NT / NLSE_ROW_THREADS];
+    float2 v[NT / row_threads<NT>()];
     load_mw_regs<NT>(v, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f, g);
     if (write_state) store_state_regs<NT>(v, r, a, F32, Fb, g + 1);
     if (!do_scan && !u_out) return;
-    float2 *F = fft_regs<NT, true>(v, A, B, a.tw);
+    float2 *F = fft_regs<NT, true, row_threads<NT>()>(v, A, B, a.tw);
     const float inv = 1.0f / (float)NT;
     if (u_out) {
         float2 *gu = u_out + (size_t)r * NT;
 #pragma unroll
-        for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) gu[threadIdx.x + m * NLSE_ROW_THREADS] = c_scale(v[m], inv);
+        for (int m = 0; m < NT / row_threads<NT>(); ++m) gu[threadIdx.x + m * row_threads<NT>()] = c_scale(v[m], inv);
     }
     if (!do_scan) return;
     const ScanLayout L = scan_layout(NT);
     float *sI = reinterpret_cast<float *>(F);
 #pragma unroll
-    for (int m = 0; m < NT / NLSE_ROW_THREADS; ++m) {
+    for (int m = 0; m < NT / row_threads<NT>(); ++m) {
         const float2 w = c_scale(v[m], inv);
-        sI[scan_slot((int)threadIdx.x + m * NLSE_ROW_THREADS, L)] = fmaf(w.x, w.x, w.y * w.y) * a.sc.invE2;
+        sI[scan_slot((int)threadIdx.x + m * row_threads<NT>(), L)] = fmaf(w.x, w.x, w.y * w.y) * a.sc.invE2;
     }
     march_scan<NT>(sI, F == A ? B : A, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), r, a, rho);
 }
 
-// CTAs per SM the row kernels are compiled for: 5, or as many as their
-// shared memory admits (228 KB per SM, 1 KB reserved per CTA) when fewer --
-// N_t = 4096 then gets 80-128 registers instead of spilling at 48.
+// CTAs per SM the row kernels are compiled for: 5 (48 registers at 256
+// threads), fewer when the shared memory admits fewer (228 KB per SM, 1 KB
+// reserved per CTA), and for 512 / 1024 threads no more than leave 64
+// registers a thread.
 template <int NT>
 __host__ __device__ constexpr int row_min_blocks(bool with_march) {
-    return (228 * 1024) / (int)(row_smem_bytes<NT>(with_march) + 1024) < 5
-               ? (228 * 1024) / (int)(row_smem_bytes<NT>(with_march) + 1024)
-               : 5;
+    const int T = with_march ? row_threads<NT>() : row_threads_nl<NT>();
+    const int by_smem = (228 * 1024) / (int)(row_smem_bytes<NT>(with_march) + 1024);
+    const int cap = T >= 512 ? 65536 / (T * 64) : 5;
+    return by_smem < cap ? by_smem : cap;
 }
 
 // Entry: physical u (interleaved) -> w = F[u] (state); optionally rho = march(|u|^2).
@@ -341,7 +350,7 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
     load_mw_row<NT>(b0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
-    float2 *R = fft_row<NT, true, row_threads<NT>()>(b0, b1, a.tw);
+    float2 *R = fft_row<NT, true, row_threads_nl<NT>()>(b0, b1, a.tw);
     const float *gr = rho + (size_t)r * NT;
     const float *gs = a.rho_s ? a.rho_s + (size_t)r * NT : nullptr;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
@@ -351,7 +360,7 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
         R[pidx(t + 1)] = nl_point(R[pidx(t + 1)], rr.y, rs.y, a.dz, a.nl, a.pchip);
     }
     __syncthreads();
-    float2 *Y = fft_row<NT, false, row_threads<NT>()>(R, R == b0 ? b1 : b0, a.tw);
+    float2 *Y = fft_row<NT, false, row_threads_nl<NT>()>(R, R == b0 ? b1 : b0, a.tw);
     store_state_row<NT>(Y, r, a, F32, Fb, g + 1);
 }
 
@@ -421,7 +430,7 @@ k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F3
 }
 
 template <int NT>
-__global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(false))
+__global__ void __launch_bounds__(row_threads_nl<NT>(), row_min_blocks<NT>(false))
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
          const float *__restrict__ rho, int g) {
     row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
@@ -446,7 +455,7 @@ k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, i
 }
 
 template <int NT>
-__global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(false))
+__global__ void __launch_bounds__(row_threads_nl<NT>(), row_min_blocks<NT>(false))
 k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
@@ -508,7 +517,7 @@ cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, 
         const size_t smem = row_smem_bytes<NT>(false);
         cudaError_t e = set_smem(k_row_nl<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_nl<NT><<<a.Nr, row_threads<NT>(), smem, st>>>(a, F32, Fb, D, rho, g);
+        k_row_nl<NT><<<a.Nr, row_threads_nl<NT>(), smem, st>>>(a, F32, Fb, D, rho, g);
     });
     return cudaGetLastError();
 }
@@ -546,7 +555,7 @@ cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int
         } else if (kind == 1) {
             e = set_smem(k_row_nl_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, g);
+            k_row_nl_b<NT><<<nblocks, row_threads_nl<NT>(), smem, st>>>(P, work, g);
         } else {
             e = set_smem(k_row_next_b<NT>, smem);
             if (e != cudaSuccess) return e;
