@@ -831,7 +831,7 @@ extern "C" int nlse_step_batched(nlse_ctx *c, const nlse_pulse_desc *p, int n, v
         int s = nlse_propagate(c, p[i].u, p[i].rho, p[i].rho_s, p[i].dz, p[i].nsteps, p[i].mode, stream);
         if (s) {
             char msg[400];
-            snprintf(msg, sizeof(msg), "%s", c->err.msg);
+            snprintf(msg, sizeof(msg), "%.399s", c->err.msg);
             nlse_set_error(&c->err, s, "pulse %d: %s", i, msg);
             return s;
         }
@@ -1145,7 +1145,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         int st = nlse_create(&descs[i], &b->ctx[i]);
         if (st != NLSE_OK) {
             char msg[400];
-            snprintf(msg, sizeof(msg), "%s", gerr->msg);
+            snprintf(msg, sizeof(msg), "%.399s", gerr->msg);
             BATCH_FAIL(st, "pulse %d: %s", i, msg);
         }
         if (!b->ctx[i]->split_ok)
