@@ -443,6 +443,19 @@ k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ 
     row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
 }
 
+// The pulse's table entry staged in shared memory by the whole CTA: the body
+// then reads its arguments from there as it needs them (re-read after each
+// barrier) instead of holding them in registers across the row's passes.
+__device__ __forceinline__ const BatchPulse &stage_pulse(const BatchPulse *__restrict__ P, int i) {
+    __shared__ __align__(16) BatchPulse sq;
+    static_assert(sizeof(BatchPulse) % 4 == 0, "staged as words");
+    const int *src = reinterpret_cast<const int *>(P + i);
+    int *dst = reinterpret_cast<int *>(&sq);
+    for (int k = threadIdx.x; k < (int)(sizeof(BatchPulse) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
+    __syncthreads();
+    return sq;
+}
+
 // ------------------------------------------------------------------ batched (many pulses, one time-grid class)
 // work[b] = (pulse, row) for CTA b; every pulse of the class has the same N_t.
 template <int NT>
@@ -458,7 +471,7 @@ template <int NT>
 __global__ void __launch_bounds__(row_threads_nl<NT>(), row_min_blocks<NT>(false))
 k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
-    const BatchPulse &q = P[w.x];
+    const BatchPulse &q = stage_pulse(P, w.x);
     row_nl_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, g);
 }
 
@@ -466,7 +479,7 @@ template <int NT>
 __global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(true))
 k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last, int g) {
     const int2 w = work[blockIdx.x];
-    const BatchPulse &q = P[w.x];
+    const BatchPulse &q = stage_pulse(P, w.x);
     if (q.ste_work)  // exciton channel: hand the physical field to the two-population march
         row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : q.ste_work, !last, 0, 1, g);
     else
