@@ -1,0 +1,6 @@
+// Row kernels of the split forms instantiated for N_t = 128, 256 (one
+// translation unit per size group, compiled in parallel).
+#include "k_rowfused.cuh"
+
+template struct RowKernels<128>;
+template struct RowKernels<256>;

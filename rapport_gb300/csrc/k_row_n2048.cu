@@ -1,0 +1,5 @@
+// Row kernels of the split forms instantiated for N_t = 2048 (one
+// translation unit per size group, compiled in parallel).
+#include "k_rowfused.cuh"
+
+template struct RowKernels<2048>;
