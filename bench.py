@@ -50,6 +50,39 @@ def peaks():
     return 6800.0, 1900.0, 1700.0, "fallback"
 
 
+def measured_traffic(kernel):
+    """DRAM bytes (read + write) per launch of a kernel from the ncu capture in
+    profiles/traffic_per_launch.json, if that capture was taken of the kernel
+    sources being run (same kernel fingerprint); else (None, why)."""
+    from rapport_gb300.build import kernel_fingerprint
+    path = os.path.join(HERE, "profiles", "traffic_per_launch.json")
+    if not os.path.exists(path):
+        return None, "no capture"
+    with open(path) as f:
+        rec = json.load(f)
+    ent = rec.get("kernels", {}).get(kernel)
+    if ent is None:
+        return None, f"no capture of {kernel}"
+    fp = kernel_fingerprint()
+    if ent.get("kernel_fingerprint") != fp:
+        return None, f"capture of {kernel} is of other kernel sources ({ent.get('kernel_fingerprint')} != {fp})"
+    return ent["bytes_per_launch"], f"ncu dram__bytes_read.sum + dram__bytes_write.sum, {ent['note']}"
+
+
+def host_cores():
+    """Host threads this process may run on, and the BLAS thread count numpy uses."""
+    cores = len(os.sched_getaffinity(0))
+    blas = None
+    try:
+        from threadpoolctl import threadpool_info
+        blas = max((d.get("num_threads") or 0 for d in threadpool_info() if d.get("user_api") == "blas"),
+                   default=None)
+    except ImportError:
+        v = os.environ.get("OPENBLAS_NUM_THREADS") or os.environ.get("OMP_NUM_THREADS")
+        blas = int(v) if v else cores  # OpenBLAS default: one thread per available core
+    return cores, blas
+
+
 # ------------------------------------------------------------------ clocks
 class ClockSampler:
     Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
@@ -323,25 +356,21 @@ def run_ours(args, rank, world, local_rank):
     top = max(prof, key=lambda k: prof[k][1])
     n_launch, tot = prof[top]
     avg_s = tot / n_launch * 1e-3
-    traffic = None
-    tpath = os.path.join(HERE, "profiles", "traffic_per_launch.json")
-    if os.path.exists(tpath):
-        with open(tpath) as f:
-            tr = json.load(f)
-        traffic = tr.get(top + ("_batched" if B > 0 else ""), tr.get(top) if B == 0 else None)
+    traffic, traffic_note = measured_traffic(top + ("_batched" if B > 0 else ""))
     if top in ("k_gemm_tc", "k_gemm_f32"):
         ach = gemm_flops / avg_s / 1e12
         roof = {"kernel": top, "bound": "tensor", "achieved": ach, "peak": bf16_s, "unit": "TFLOP/s",
                 "frac": ach / bf16_s, "traffic": traffic, "peak_source": f"bf16_tflops_sustained ({src})",
                 "per_launch": f"{gemm_flops:.3e} algorithmic FLOPs, avg {avg_s * 1e6:.1f} us over {n_launch} launches",
-                "executed_tensor_tflops": (3 if bmode == "split_f16" else 4) * ach if top == "k_gemm_tc" else None}
+                "executed_tensor_tflops": (3 if bmode == "split_f16" else 4) * ach if top == "k_gemm_tc" else None,
+                "traffic_source": traffic_note}
     else:
         npts = (B if B > 0 else 1) * Nr * Nt
         byts = {"k_row_nl": 36.0, "k_row_next": 36.0, "k_rate_scan": 12.0, "k_nonlinear_step": 20.0,
                 "k_fft_phase_ifft": 16.0}.get(top, 16.0) * npts
         ach = byts / avg_s / 1e9
         roof = {"kernel": top, "bound": "hbm", "achieved": ach, "peak": hbm, "unit": "GB/s", "frac": ach / hbm,
-                "traffic": traffic, "peak_source": f"hbm_gbs ({src})",
+                "traffic": traffic, "traffic_source": traffic_note, "peak_source": f"hbm_gbs ({src})",
                 "per_launch": f"{byts:.3e} algorithmic bytes, avg {avg_s * 1e6:.1f} us over {n_launch} launches"}
 
     line = {
@@ -479,9 +508,12 @@ def cpu_baseline(nz):
         og.update_plasma(u, rho, rs)
         u = og.step(u, rho, rs, WORKLOAD["dz"])
     dt = time.perf_counter() - t
-    return {"value": nz / dt, "unit": "z-steps/s", "cores": os.cpu_count(), "kind": "port",
+    cores, blas = host_cores()
+    return {"value": nz / dt, "unit": "z-steps/s", "cores": cores, "blas_threads": blas, "kind": "port",
             "sample": f"{nz} z-steps of the 1024x2048 workload (FP64 numpy/OpenBLAS + C carrier march, "
-                      f"OpenMP over r)"}
+                      f"OpenMP over r)",
+            "what": "the oracle: an FP64 restatement of the reference path, pinned to the reference's own "
+                    "outputs bit for bit or to 1e-12 (the reference itself needs CuPy and a GPU)"}
 
 
 def run_reference(args, rank):
@@ -499,14 +531,14 @@ def run_reference(args, rank):
         u = og.step(u, rho, rs, WORKLOAD["dz"])
     dt = time.perf_counter() - t
     v = args.steps / dt
-    cores = os.cpu_count()
+    cores, blas = host_cores()
     print(json.dumps({
         "metric": METRIC, "value": v, "unit": "z-steps/s", "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic",
         "config": dict(CONFIG, form="reference CPU path (FP64 restatement)", z_steps_per_step=1),
         "impl": "reference",
-        "cpu_baseline": {"value": v, "unit": "z-steps/s", "cores": cores, "kind": "port",
+        "cpu_baseline": {"value": v, "unit": "z-steps/s", "cores": cores, "blas_threads": blas, "kind": "port",
                          "sample": f"{args.steps} z-steps of the 1024x2048 workload"},
         "e2e": {"value": v, "unit": "z-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
@@ -598,6 +630,119 @@ def run_config5(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def run_tour(args, rank, world, local_rank):
+    """Every kernel of libnlse once at the 1024 x 2048 workload, for profiling: the
+    plain half step, split(), the nonlinear block, update_plasma, a z-step and
+    a 2-step propagate in each arithmetic, a 2-step propagate of 8 pulses in one
+    batch (both split forms), the record reductions, the exciton-channel
+    march, the full-physics split / nonlinear block (Raman, self-steepening,
+    space-time focusing) and the fused full-physics row kernel of the split
+    form.  Under ncu the launch list then holds every kernel kind at full size;
+    the run checks only that every call succeeds and the fields stay finite."""
+    import torch
+    import rapport_gb300 as R
+    from rapport_gb300 import _lib
+    torch.cuda.set_device(local_rank)
+    dev = torch.device("cuda", local_rank)
+    W = WORKLOAD
+
+    def _setup(**over):
+        cfg = R.workload_config(W["Nr"], W["Nt"], W["R_max"], W["w0"], W["T_half"], W["dz"], 2, **over)
+        g = R.build_grids(cfg)
+        u0 = R.envelope_lens(W["w0"], W["fwhm"], W["E"], W["f"], 0)(g["rr"], g["tt"], cfg, g)
+        return cfg, g, np.ascontiguousarray(u0.astype(np.complex64))
+
+    cfg, g, u0 = _setup()
+    ctx = _lib.Context(cfg, g)
+    lin, nl = R.LinearOperator(cfg, g, ctx), R.NonlinearOperator(cfg, g, ctx)
+    u = torch.from_numpy(u0).to(dev)
+    rho = torch.zeros(u.shape, dtype=torch.float32, device=dev)
+    rs = torch.zeros_like(rho)
+    hl = lin.half_linear(u, W["dz"])                      # k_gemm_f32, k_fft_phase_ifft, k_phase_tables
+    nl.update_plasma(hl, rho, rs)                          # k_rate_scan
+    nl.split(hl, rho, rs)                                  # k_split
+    nl.nonlinear_step(hl.clone(), rho, W["dz"])            # k_nonlinear_step
+    rec = torch.zeros((W["Nr"], 6), dtype=torch.float64, device=dev)
+    ctx.record(hl, rho, rs, None, 0, rec)                  # k_record
+    for mode in (_lib.MODE_PLAIN_F32, _lib.MODE_SPLIT_BF16, _lib.MODE_SPLIT_F16):
+        v = u.clone()
+        ctx.step(v, rho, W["dz"], mode, rs)                # split forms: k_build_E, k_split_E*, k_row_*, k_gemm_tc
+        ctx.propagate(v, torch.zeros_like(rho), torch.zeros_like(rho), W["dz"], 2, mode)
+        assert bool(torch.isfinite(v).all())
+    envs = [R.envelope_lens(W["w0"], W["fwhm"], W["E"], W["f"], i)(g["rr"], g["tt"], cfg, g) for i in range(8)]
+    b = _lib.Batch([cfg] * 8, [g] * 8)
+    bu = [torch.from_numpy(np.ascontiguousarray(e.astype(np.complex64))).to(dev) for e in envs]
+    br = [torch.zeros(u.shape, dtype=torch.float32, device=dev) for _ in envs]
+    for mode in (_lib.MODE_SPLIT_BF16, _lib.MODE_SPLIT_F16):
+        b.set_mode(mode)
+        b.propagate(bu, br, None, W["dz"], 2)              # k_gemm_tc_grouped, k_row_*_b, k_field_bound
+    assert b.device_status() == 0 and all(bool(torch.isfinite(x).all()) for x in bu)
+    # exciton channel: the two-population march
+    cfg_s, g_s, _ = _setup(enable_ste=True, tau_ste=1e-12)
+    cs = _lib.Context(cfg_s, g_s)
+    r2, s2 = torch.zeros_like(rho), torch.zeros_like(rho)
+    cs.update_plasma(u, r2, s2)                            # k_rate_scan (two populations)
+    # full-physics split: Raman, self-steepening, space-time focusing
+    cfg_f, g_f, _ = _setup(f_R=0.18, enable_kerr_raman=True, enable_self_steepening=True,
+                           enable_space_time_focusing=True)
+    cf = _lib.Context(cfg_f, g_f)
+    out = torch.empty_like(u)
+    alpha = torch.empty_like(rho)
+    cf.split(u, rho, out, alpha)                           # k_split_full
+    v = u.clone()
+    cf.nonlinear_step(v, rho, W["dz"])                     # k_nl_full
+    cf.half_linear(v, W["dz"])                             # k_phase_table_2d, k_fft_phase_ifft (2-d phase)
+    assert bool(torch.isfinite(v).all())
+    # Raman + self-steepening in the split form: the fused full-physics row kernel
+    cfg_r, g_r, _ = _setup(f_R=0.18, enable_kerr_raman=True, enable_self_steepening=True)
+    cr = _lib.Context(cfg_r, g_r)
+    v = u.clone()
+    cr.step(v, rho, W["dz"], _lib.MODE_SPLIT_BF16)         # k_row_nl_full
+    assert bool(torch.isfinite(v).all())
+    torch.cuda.synchronize()
+    for c in (ctx, cs, cf, cr):
+        assert c.device_status() == 0
+    print("kernel tour done")
+
+
+def record_traffic(csv_path):
+    """Write profiles/traffic_per_launch.json from an ncu CSV of
+    gpu__time_duration.sum, dram__bytes_read.sum and dram__bytes_write.sum
+    (one row per launch and metric), stamped with the kernel fingerprint of the
+    sources in this tree: per kernel kind, the mean DRAM bytes per launch."""
+    import csv
+    from rapport_gb300.build import kernel_fingerprint
+    kinds = {"k_gemm_tc_grouped": "k_gemm_tc_batched", "k_row_nl_b": "k_row_nl_batched",
+             "k_row_next_b": "k_row_next_batched", "k_gemm_tc": "k_gemm_tc", "k_row_nl": "k_row_nl",
+             "k_row_next": "k_row_next"}
+    lines = open(csv_path).read().splitlines()
+    start = next(i for i, ln in enumerate(lines) if ln.startswith('"ID"'))
+    per = {}
+    for row in csv.DictReader(lines[start:]):
+        name = row["Kernel Name"].split("(")[0].split("<")[0].replace("void ", "").strip()
+        if name not in kinds:
+            continue
+        v = float(row["Metric Value"].replace(",", ""))
+        unit = row.get("Metric Unit", "")
+        scale = {"byte": 1, "Kbyte": 1e3, "Mbyte": 1e6, "Gbyte": 1e9, "KB": 1e3, "MB": 1e6, "GB": 1e9}.get(unit, 1)
+        ent = per.setdefault((kinds[name], row["ID"]), {})
+        ent[row["Metric Name"]] = v * scale
+    out = {}
+    for (kind, _), m in per.items():
+        if "dram__bytes_read.sum" in m and "dram__bytes_write.sum" in m:
+            out.setdefault(kind, []).append(m["dram__bytes_read.sum"] + m["dram__bytes_write.sum"])
+    fp = kernel_fingerprint()
+    rec = {"_what": "DRAM bytes read + written per launch (ncu dram__bytes_read.sum + dram__bytes_write.sum), "
+                    "mean over the captured launches; valid for the kernel sources with this fingerprint",
+           "kernels": {k: {"bytes_per_launch": int(sum(v) / len(v)), "launches": len(v), "kernel_fingerprint": fp,
+                           "note": f"mean of {len(v)} launches, capture {os.path.basename(csv_path)}"}
+                       for k, v in sorted(out.items())}}
+    path = os.path.join(HERE, "profiles", "traffic_per_launch.json")
+    with open(path, "w") as f:
+        json.dump(rec, f, indent=1)
+    print(json.dumps(rec, indent=1))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -611,8 +756,14 @@ def main():
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=8, help="pulses of the batched (headline) form; 0 = single pulse")
-    ap.add_argument("--workload", default="single", choices=["single", "config4", "config5"])
+    ap.add_argument("--workload", default="single", choices=["single", "config4", "config5", "tour"],
+                    help="tour: every kernel once at 1024 x 2048 (for ncu launch lists)")
+    ap.add_argument("--record-traffic", metavar="CSV",
+                    help="write profiles/traffic_per_launch.json from an ncu CSV and exit")
     args = ap.parse_args()
+    if args.record_traffic:
+        record_traffic(args.record_traffic)
+        return
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
     local_rank = int(os.environ.get("LOCAL_RANK", "0"))
@@ -624,6 +775,9 @@ def main():
         return
     if args.workload == "config5":
         run_config5(args, rank, world, local_rank)
+        return
+    if args.workload == "tour":
+        run_tour(args, rank, world, local_rank)
         return
     run_ours(args, rank, world, local_rank)
 

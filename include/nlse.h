@@ -243,6 +243,15 @@ int nlse_set_split_terms(nlse_ctx *ctx, int a_terms);
  * NLSE_ERR_DEVICE_FLAG if a split-FP16 field write overflowed FP16. */
 int nlse_device_status(nlse_ctx *ctx, int *word);
 
+/* Diagnostic of the failure path: launches one kernel that waits on an
+ * mbarrier nothing arrives on, bounded by limit_us microseconds (1 .. 1e6;
+ * the product's own waits are bounded by 2 s), then raises bit 3 of the
+ * context's status word and returns, leaving no work in flight.  Afterwards
+ * nlse_device_status (and the status of a batch holding ctx) reports
+ * NLSE_ERR_TIMEOUT; the context stays usable.  No counterpart in the
+ * reference (its failure detection is host-side only). */
+int nlse_debug_wait_timeout(nlse_ctx *ctx, int limit_us, void *stream);
+
 /* Per-radius diagnostics of one saved plane (Integrator._record,
  * integrator.py:179-224), FP64 reductions over t into out[r][6 + nbins]:
  * sum |u|^2, max rho, max rho_s, max |u|^2, sum 2 photo |u|^2,

@@ -22,7 +22,9 @@ import subprocess
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
-REF_KERNELS_PY = "/root/reference/.github/deliverable (3)/sim/kernels.py"
+# the reference checkout (RAPPORT_REFERENCE; the build container's copy by default)
+REF_ROOT = os.environ.get("RAPPORT_REFERENCE", "/root/reference")
+REF_KERNELS_PY = os.path.join(REF_ROOT, ".github", "deliverable (3)", "sim", "kernels.py")
 
 _PRELUDE = r"""
 #include <cmath>

@@ -20,7 +20,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16, MODE_SPLIT_F16 = 0, 1, 2
 # every symbol include/nlse.h declares (checked by the CPU test suite)
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_rate_equation", "nlse_step", "nlse_step_batched", "nlse_propagate", "nlse_set_split_terms",
-           "nlse_device_status", "nlse_debug_operator_product", "nlse_scan_fallback_rows",
+           "nlse_device_status", "nlse_debug_operator_product", "nlse_debug_wait_timeout", "nlse_scan_fallback_rows",
            "nlse_half_linear_noalloc", "nlse_record", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
            "nlse_batch_set_split_terms", "nlse_batch_set_mode", "nlse_batch_device_status", "nlse_batch_get_last_error",
            "nlse_batch_destroy",
@@ -71,6 +71,7 @@ def load():
     lib.nlse_half_linear_noalloc.argtypes = [_P, _P, _P, _P, _I, _I, _P]
     lib.nlse_debug_operator_product.argtypes = [_P, _P, _P, _D, _P]
     lib.nlse_device_status.argtypes = [_P, ctypes.POINTER(_I)]
+    lib.nlse_debug_wait_timeout.argtypes = [_P, _I, _P]
     lib.nlse_split.argtypes = [_P, _P, _P, _P, _P, _P, _P]
     lib.nlse_nonlinear_step.argtypes = [_P, _P, _P, _P, _D, _P]
     lib.nlse_update_plasma.argtypes = [_P, _P, _P, _P, _P]
@@ -283,6 +284,11 @@ class Context:
         w = _I(0)
         _check(self.lib, self.h, self.lib.nlse_device_status(self.h, ctypes.byref(w)))
         return w.value
+
+    def debug_wait_timeout(self, limit_us):
+        """Launch the failure-path probe: a device wait bounded by limit_us that
+        runs out and raises the context's status bit (read by device_status)."""
+        _check(self.lib, self.h, self.lib.nlse_debug_wait_timeout(self.h, int(limit_us), self._stream()))
 
     def split(self, u, rho, rhs, alpha, rho_s=None):
         a = self._rho(alpha, "alpha") if alpha is not None else None

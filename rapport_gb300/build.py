@@ -44,6 +44,20 @@ def _compile(src, extra):
     return obj, None
 
 
+def kernel_fingerprint():
+    """Short hash of the CUDA sources and the C header: a measurement of a
+    kernel (e.g. its DRAM traffic) is current only while this is unchanged."""
+    import hashlib
+    h = hashlib.sha256()
+    files = sorted(glob.glob(os.path.join(CSRC, "*.cu")) + glob.glob(os.path.join(CSRC, "*.cuh")))
+    files += sorted(glob.glob(os.path.join(INCLUDE, "*.h")))
+    for f in files:
+        h.update(os.path.basename(f).encode())
+        with open(f, "rb") as fh:
+            h.update(fh.read())
+    return h.hexdigest()[:16]
+
+
 def build(verbose=False, extra_flags=()):
     os.makedirs(BUILD, exist_ok=True)
     os.makedirs(LIBDIR, exist_ok=True)

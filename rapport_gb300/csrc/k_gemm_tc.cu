@@ -72,13 +72,14 @@ __device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, uint32_t parity) {
     return ok != 0;
 }
 
-// Wait for the phase with the given parity to complete; false after ~2 s.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity) {
+// Wait for the phase with the given parity to complete; false once limit_ns
+// (2 s for the product's waits) have passed.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, uint32_t parity, uint64_t limit_ns = TC_WAIT_NS) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (uint32_t i = 1;; ++i) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((i & 255u) == 0 && global_ns() - t0 > TC_WAIT_NS) return false;
+        if ((i & 255u) == 0 && global_ns() - t0 > limit_ns) return false;
     }
 }
 
@@ -442,6 +443,26 @@ cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float
         if (e != cudaSuccess) return e;
         k_gemm_tc<AT, BK, ST, F16><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
     })
+    return cudaGetLastError();
+}
+
+// ------------------------------------------------------------------ failure-path probe
+// The product's bounded wait and its error reporting, exercised on purpose:
+// one thread waits on an mbarrier that nothing arrives on, with the caller's
+// (short) limit instead of the product's 2 s, then raises the status bit the
+// product raises on a timeout (bit 3: the probe) and returns.  The barrier
+// lives in this CTA's shared memory and no copy or MMA is issued, so the
+// kernel leaves nothing in flight.
+__global__ void k_wait_probe(int *__restrict__ err, unsigned long long limit_ns) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x != 0) return;
+    mbar_init(&bar, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    if (!mbar_wait(&bar, 0, limit_ns)) atomicOr(err, 8);
+}
+
+cudaError_t launch_wait_probe(int *err, unsigned long long limit_ns, cudaStream_t stream) {
+    k_wait_probe<<<1, 32, 0, stream>>>(err, limit_ns);
     return cudaGetLastError();
 }
 

@@ -850,6 +850,13 @@ extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *o
     return launched(c, cudaMemcpyAsync(out, c->d_D, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
 }
 
+extern "C" int nlse_debug_wait_timeout(nlse_ctx *c, int limit_us, void *stream) {
+    if (!c) return NLSE_ERR_INVALID_ARG;
+    if (limit_us < 1 || limit_us > 1000000) return bad(c, NLSE_ERR_INVALID_ARG, "limit_us must be in [1, 1000000]");
+    return launched(c, launch_wait_probe(c->d_flag, 1000ull * (unsigned long long)limit_us, (cudaStream_t)stream),
+                    "wait probe");
+}
+
 extern "C" int nlse_record(nlse_ctx *c, const void *u, const float *rho, const float *rho_s, const int *bin_of_t,
                            int nbins, double *out, void *stream) {
     if (!c) return NLSE_ERR_INVALID_ARG;

@@ -219,6 +219,9 @@ cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float
 cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
                                   double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, int f16, int *scale,
                                   cudaStream_t stream);
+// Failure-path probe: a bounded mbarrier wait that runs out after limit_ns and
+// raises bit 3 of the status word err.
+cudaError_t launch_wait_probe(int *err, unsigned long long limit_ns, cudaStream_t stream);
 // Split-FP16 form, before the entry kernel: scale[NLSE_SC_MAX + 2] = a bound of
 // max |F[u]| (Nt max |u|, the "previous input" of input 0), slot 0 cleared.
 cudaError_t launch_field_bound(const float2 *u, size_t n, int Nt, int *scale, cudaStream_t st);

@@ -17,12 +17,12 @@ import os
 import numpy as np
 import torch
 
-from ._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16, Context
-from .config import Config
+from ._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16, MODE_SPLIT_F16, Context
+from .config import Config, resolved_linear_mode
 from .grids import ENVELOPES, build_grids
 from .operators import LinearOperator, NonlinearOperator
 
-_MODES = {"plain": MODE_PLAIN_F32, "split_bf16": MODE_SPLIT_BF16}
+_MODES = {"plain": MODE_PLAIN_F32, "split_bf16": MODE_SPLIT_BF16, "split_f16": MODE_SPLIT_F16}
 
 
 def code_fingerprint():
@@ -52,7 +52,8 @@ class Integrator:
         self.ctx = Context(cfg, g) if ctx is None else ctx
         self.lin = LinearOperator(cfg, g, self.ctx)
         self.nl = NonlinearOperator(cfg, g, self.ctx)
-        self.mode = _MODES[cfg.linear_mode]
+        self.linear_mode = resolved_linear_mode(cfg)
+        self.mode = _MODES[self.linear_mode]
         fn = envelope if callable(envelope) else ENVELOPES[envelope]
         u0 = np.asarray(fn(g["rr"], g["tt"], cfg, g), dtype=np.complex128)
         dev = torch.device("cuda", torch.cuda.current_device())
@@ -269,7 +270,7 @@ class Integrator:
                 E_tr_eV=cfg.E_tr_eV, f_ste_pump=float(self.g["f_ste"]), enable_avalanche=cfg.enable_avalanche,
                 enable_recombination=cfg.enable_recombination, enable_ste=cfg.enable_ste,
             ),
-            linear_mode=cfg.linear_mode, rate_model=cfg.rate_model,
+            linear_mode=self.linear_mode, rate_model=cfg.rate_model,
         )
         with open(os.path.join(cfg.out_dir, "params.json"), "w") as f:
             json.dump(params, f, indent=2)

@@ -24,7 +24,8 @@ from pathlib import Path
 import numpy as np
 import torch
 
-from ._lib import Batch
+from ._lib import MODE_SPLIT_F16, Batch
+from .config import resolved_linear_mode, split_supported
 from .filament_sim import FIELD_TOGGLES, run_config
 from .grids import build_grids
 from .integrator import Integrator, code_fingerprint
@@ -82,8 +83,7 @@ def summarize(results):
 def _batchable(cfg):
     # a batch takes the Raman / self-steepening terms and the exciton channel;
     # space-time focusing has no single radial operator (plain mode, own context)
-    return (cfg.linear_mode == "split_bf16" and (cfg.N - 1) % 64 == 0 and cfg.Nt % 256 == 0
-            and not cfg.enable_space_time_focusing)
+    return resolved_linear_mode(cfg) in ("split_bf16", "split_f16") and split_supported(cfg)
 
 
 class _Group:
@@ -140,7 +140,8 @@ def run_scenarios(base_params, scenarios, out_root, reuse=True, envelope="gaussi
     keyed = {}
     for name, cfg in todo:
         if batch and _batchable(cfg):
-            keyed.setdefault((cfg.dz, cfg.nz, max(1, int(cfg.save_stride))), []).append((name, cfg))
+            keyed.setdefault((cfg.dz, cfg.nz, max(1, int(cfg.save_stride)), resolved_linear_mode(cfg)),
+                             []).append((name, cfg))
         else:
             g = build_grids(cfg)
             groups.append(_Group([name], [Integrator(cfg, envelope=env, g=g)]))
@@ -152,6 +153,8 @@ def run_scenarios(base_params, scenarios, out_root, reuse=True, envelope="gaussi
         cfgs = [c for _, c in members]
         grids = [build_grids(c) for c in cfgs]
         b = Batch(cfgs, grids)
+        if resolved_linear_mode(cfgs[0]) == "split_f16":
+            b.set_mode(MODE_SPLIT_F16)
         integs = [Integrator(c, envelope=env, ctx=b.context(i), g=g) for i, (c, g) in enumerate(zip(cfgs, grids))]
         groups.append(_Group([n for n, _ in members], integs, batch=b))
     active = list(groups)

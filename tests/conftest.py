@@ -45,6 +45,12 @@ FULL_PHYSICS = dict(f_R=0.18, enable_kerr_raman=True, enable_self_steepening=Tru
 
 
 @pytest.fixture(scope="session")
+def tiny_keldysh():
+    # the reference's default rate model (Keldysh tables) with the exciton channel on
+    return load_golden("tiny_keldysh.npz")
+
+
+@pytest.fixture(scope="session")
 def k1edge():
     return load_golden("k1_edge.npz")
 

@@ -27,7 +27,8 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 REPO = os.path.abspath(os.path.join(HERE, "..", ".."))
-REF_SIM = "/root/reference/.github/deliverable (3)/sim"
+REF_ROOT = os.environ.get("RAPPORT_REFERENCE", "/root/reference")
+REF_SIM = os.path.join(REF_ROOT, ".github", "deliverable (3)", "sim")
 
 sys.path.insert(0, os.path.join(HERE, "refshim"))
 sys.path.insert(0, REF_SIM)
@@ -52,6 +53,9 @@ class MPIPowerLaw:
         return SIGMA_K * I**K_PHOTONS * RHO_NT
 
 
+import keldysh as ref_keldysh  # noqa: E402
+
+REF_KELDYSH = ref_keldysh.KeldyshSiO2  # the reference's own rate (its default table source)
 ref_grids.KeldyshSiO2 = MPIPowerLaw
 
 
@@ -100,10 +104,20 @@ def grid_arrays(integ):
 
 
 def run_case(Nr, Nt, R_max, w0, T_half, fwhm, energy_uJ, f, dz, nsteps, seed, rows,
-             keep_steps, with_Y=True, **over):
+             keep_steps, with_Y=True, keldysh=False, **over):
     cfg = make_config(Nr, Nt, R_max, w0, T_half, dz, nsteps, energy_uJ, **over)
-    integ = ref_integrator.Integrator(cfg, envelope=lens_envelope(fwhm, energy_uJ, w0, f, seed))
+    # keldysh=True: the reference's default rate model (KeldyshSiO2) fills the tables
+    ref_grids.KeldyshSiO2 = REF_KELDYSH if keldysh else MPIPowerLaw
+    try:
+        integ = ref_integrator.Integrator(cfg, envelope=lens_envelope(fwhm, energy_uJ, w0, f, seed))
+    finally:
+        ref_grids.KeldyshSiO2 = MPIPowerLaw
+    if keldysh:
+        out_extra = dict(W_LUT_s=np.asarray(integ.g["keldysh"]["W_LUT_s"]))
+    else:
+        out_extra = {}
     out = grid_arrays(integ)
+    out.update(out_extra)
     u0 = integ.u.copy()
     out["u0"] = u0[rows]
     # single-operator goldens on the initial field
@@ -180,6 +194,22 @@ def k1_edge_cases():
     return res
 
 
+def keldysh_tables():
+    """The reference's KeldyshSiO2.rate (keldysh.py:94-148, default monotone=False)
+    on the spline knots I = 10^d (1 + 0.01 m) that grids.py:140-150 evaluates it
+    at: both band gaps (9 eV valence band, 6 eV exciton) at 800 nm and at the
+    reference's default 1030 nm, with the Config-derived meff and n0."""
+    out = {"I_knots": np.ravel(10 ** (np.arange(17) + 0.0)[:, None] * (0.01 * np.arange(900) + 1)[None, :])}
+    for lam in (800e-9, 1030e-9):
+        cfg = make_config(64, 128, 1e-4, 1e-5, 3e-13, 5e-6, 1, wavelength=lam)
+        tag = f"{int(round(lam * 1e9))}"
+        out[f"n0_{tag}"], out[f"meff_{tag}"] = cfg.n0, cfg.meff
+        for gap, name in ((cfg.Ui_eV, "Ui"), (cfg.Us_eV, "Us")):
+            out[f"W_{name}_{tag}"] = REF_KELDYSH(lam, gap, cfg.meff, cfg.n0).rate(out["I_knots"])
+            out[f"gap_{name}_{tag}"] = gap
+    return out
+
+
 def record_case():
     """The reference's own Integrator.propagate() with every recording option on:
     save stride, (z, r, t) cube with r/t strides, absorption time bins, rho snapshot."""
@@ -230,6 +260,13 @@ def main():
                     enable_space_time_focusing=True, enable_ste=True, tau_ste=1e-12)
     full["flags"] = np.array([0.18, 1, 1, 1, 1, 1e-12])
     np.savez_compressed(os.path.join(HERE, "tiny_full.npz"), **full)
+    # the reference's default rate model: Keldysh tables (valence band and, with
+    # the exciton channel on, the 6 eV exciton gap) -- no power-law substitution
+    kel = run_case(Nr=64, Nt=256, R_max=100e-6, w0=10e-6, T_half=300e-15, fwhm=100e-15,
+                   energy_uJ=2.0, f=1e-2, dz=5e-6, nsteps=4, seed=0, rows=list(range(64)),
+                   keep_steps=[1, 4], with_Y=False, keldysh=True, enable_ste=True, tau_ste=1e-12)
+    np.savez_compressed(os.path.join(HERE, "tiny_keldysh.npz"), **kel)
+    np.savez_compressed(os.path.join(HERE, "keldysh_tables.npz"), **keldysh_tables())
     np.savez_compressed(os.path.join(HERE, "k1_edge.npz"), **k1_edge_cases())
     np.savez_compressed(os.path.join(HERE, "record_tiny.npz"), **record_case())
     print("wrote", sorted(f for f in os.listdir(HERE) if f.endswith(".npz")))

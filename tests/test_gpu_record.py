@@ -20,7 +20,7 @@ RHO_KEYS = ("rho_rz", "rho_rzt", "rho_onaxis_t", "rho_rz_at")
 LOSS_KEYS = ("absorbed_rz", "absorbed_rz_bins", "E_plasma_z", "E_MPI_z", "E_total_z")
 
 
-@pytest.mark.parametrize("mode", ["plain", "split_bf16"])
+@pytest.mark.parametrize("mode", ["plain", "split_bf16", "split_f16", "auto"])
 def test_propagate_results_match_reference(mode, tmp_path):
     import rapport_gb300 as R
     from conftest import load_golden
@@ -49,6 +49,8 @@ def test_propagate_results_match_reference(mode, tmp_path):
     saved = np.load(run / "result.npz", allow_pickle=True)
     assert set(saved.files) == set(out.keys())
     params = json.loads((run / "params.json").read_text())
-    assert params["toggles"]["enable_kerr_raman"] is False and params["linear_mode"] == mode
+    # "auto" runs the split-BF16 form on this tileable grid (and records it)
+    assert params["toggles"]["enable_kerr_raman"] is False
+    assert params["linear_mode"] == ("split_bf16" if mode == "auto" else mode)
     assert len(params["code_fingerprint"]) == 12
     assert not os.path.exists(run / "result.npz.tmp.npz")

@@ -72,3 +72,48 @@ def test_mpi_rate_table():
     g = R.build_grids(cfg)
     I = np.array([1e10, 3e12, 5e13])
     assert np.allclose(g["keldysh"]["f_spline"](I), 1e-71 * I**6 * 2.1e22, rtol=2e-4)
+
+
+def test_keldysh_rate_matches_reference():
+    """grids.keldysh_rate against the reference's own KeldyshSiO2.rate
+    (keldysh.py:94-148, keldysh_tables.npz) on every spline knot of
+    grids.py:140-150: both band gaps, at 800 nm and the reference's 1030 nm."""
+    from conftest import load_golden
+    k = load_golden("keldysh_tables.npz")
+    assert np.array_equal(k["I_knots"], R.grids.intensity_knots())
+    for lam in (800, 1030):
+        for gap in ("Ui", "Us"):
+            W = R.keldysh_rate(k["I_knots"], lam * 1e-9, float(k[f"gap_{gap}_{lam}"]),
+                               float(k[f"meff_{lam}"]), float(k[f"n0_{lam}"]))
+            ref = k[f"W_{gap}_{lam}"]
+            assert rel_l2(W, ref) < 1e-12, (lam, gap)
+            big = ref > 1e-300
+            assert np.max(np.abs(W[big] / ref[big] - 1)) < 1e-11, (lam, gap)
+
+
+def test_keldysh_tables_match_reference(tiny_keldysh):
+    """The reference's default rate model end to end on the host: build_grids'
+    PCHIP spline and both 4096-point carrier tables (valence band and, with the
+    exciton channel, the 6 eV gap) equal the reference's (grids.py:140-161)."""
+    m = meta_case(tiny_keldysh)
+    cfg = R.workload_config(m["Nr"], m["Nt"], m["R_max"], m["w0"], m["T_half"], m["dz"], m["nsteps"],
+                            rate_model="keldysh", enable_ste=True, tau_ste=1e-12)
+    kel = R.build_grids(cfg)["keldysh"]
+    assert rel_l2(kel["W_LUT"], tiny_keldysh["W_LUT"]) < 1e-12
+    assert rel_l2(kel["W_LUT_s"], tiny_keldysh["W_LUT_s"]) < 1e-12
+    # the raw Keldysh rate has cusps (channel closings) where PCHIP's slope
+    # limiter turns last-bit differences of the knot values into ~1e-11
+    assert rel_l2(kel["f_spline"](tiny_keldysh["I_probe"]), tiny_keldysh["W_probe"]) < 1e-10
+
+
+def test_linear_mode_resolution():
+    """auto = the split-BF16 tensor-core form where the grid tiles and the
+    physics has a single radial operator, else the plain FP32 form."""
+    from rapport_gb300.config import resolved_linear_mode, split_supported
+    mk = lambda **kw: R.Config(verbose=False, out_dir="", **kw)  # noqa: E731
+    assert mk().linear_mode == "auto"
+    assert resolved_linear_mode(mk(N=1025, Nt=2048, enable_space_time_focusing=False)) == "split_bf16"
+    assert resolved_linear_mode(mk(N=1025, Nt=2048, enable_space_time_focusing=True)) == "plain"
+    assert resolved_linear_mode(mk(N=1000, Nt=2048, enable_space_time_focusing=False)) == "plain"
+    assert resolved_linear_mode(mk(linear_mode="split_f16")) == "split_f16"
+    assert split_supported(mk(N=257, Nt=512, enable_space_time_focusing=False))

@@ -7,8 +7,10 @@ QDHT matrix, the phase tables and the field as caller-owned device buffers
 and keeps its intermediate field in a static device array shared by every
 call.  This test checks it against the context entry point nlse_half_linear
 on two calls in a row with different fields (the second call must not depend
-on what the first left in the shared array), and checks that a size beyond
-the array is refused with a clear error before anything is launched.
+on what the first left in the shared array), pins both to the FP64 oracle's
+half_linear (the reference's LinearOperator.half_linear restated), and checks
+that a size beyond the array is refused with a clear error before anything is
+launched.
 """
 import ctypes
 
@@ -48,8 +50,11 @@ def test_noalloc_half_linear_matches_context_entry():
     rng = np.random.default_rng(4)
     fields = [R.envelope_lens(100e-6, 100e-15, 1.0, 0.1, 0)(g["rr"], g["tt"], cfg, g),
               (rng.standard_normal((Nr, Nt)) + 1j * rng.standard_normal((Nr, Nt))) * 1e9]
+    import nlse_oracle as O
+    og = O.OracleGrid(O.workload_config(Nr, Nt, 1e-3, 100e-6, 400e-15))
     for f in fields:  # two calls in a row
         u = torch.from_numpy(f.astype(np.complex64)).cuda()
+        want = og.half_linear(u.cpu().numpy().astype(np.complex128), dz)
         ref = u.clone()
         ctx.half_linear(ref, dz)
         out = u.clone()
@@ -58,6 +63,8 @@ def test_noalloc_half_linear_matches_context_entry():
         torch.cuda.synchronize()
         err = float((out - ref).abs().norm() / ref.abs().norm())
         assert err < TOL, err
+        got = out.cpu().numpy().astype(np.complex128)
+        assert np.linalg.norm(got - want) / np.linalg.norm(want) < TOL
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch():
