@@ -43,10 +43,11 @@ LINEAR_MODES = ("auto", "plain", "split_bf16", "split_f16")
 
 
 def split_supported(cfg) -> bool:
-    """Whether the tensor-core (split) forms run this Config: the product tiles
-    2 N_r rows by 128 and N_t columns by 256, and with space-time focusing the
-    half step's diffraction phase depends on Omega (no single radial operator)."""
-    return (cfg.N - 1) % 64 == 0 and cfg.Nt % 256 == 0 and not cfg.enable_space_time_focusing
+    """Whether the tensor-core (split) forms run this Config: any N_t and up to
+    8192 radial points (the library pads N_r to a multiple of 64 inside the
+    context), but not space-time focusing, whose diffraction phase depends on
+    Omega (no single radial operator for the product)."""
+    return (cfg.N - 1) <= 8192 and not cfg.enable_space_time_focusing
 
 
 def resolved_linear_mode(cfg) -> str:

@@ -177,7 +177,7 @@ __device__ __forceinline__ TileJob tile_job(const TileSource &src, int t) {
         j.m0 = g.m0;
         j.n0 = g.n0;
     } else {
-        const int nt = src.N / TC_BN;
+        const int nt = (src.N + TC_BN - 1) / TC_BN;
         j.tmA = src.tmA;
         j.tmB = src.tmB;
         j.D = src.D;
@@ -335,15 +335,19 @@ __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntile
             const TileJob j = tile_job(src, t);
             float *row = j.D + (size_t)(j.m0 + q * 32 + lane) * j.N + j.n0;
             const uint32_t tq = tmem + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * TC_BN);
+            // columns of the tile inside D (N < 256: one partial tile; N is a multiple of 16)
+            const int ncol = min(TC_BN, j.N - j.n0);
 #pragma unroll 1
             for (int c = 0; c < TC_BN / 32; ++c) {
+                if (c * 32 >= ncol) break;  // warp-uniform: tcgen05.ld stays converged
                 uint32_t r[32];
                 tmem_ld32(tq + (uint32_t)(c * 32), r);
                 float4 *dst = reinterpret_cast<float4 *>(row + c * 32);
 #pragma unroll
                 for (int v = 0; v < 8; ++v)
-                    dst[v] = make_float4(__uint_as_float(r[4 * v]), __uint_as_float(r[4 * v + 1]),
-                                         __uint_as_float(r[4 * v + 2]), __uint_as_float(r[4 * v + 3]));
+                    if (c * 32 + 4 * v < ncol)
+                        dst[v] = make_float4(__uint_as_float(r[4 * v]), __uint_as_float(r[4 * v + 1]),
+                                             __uint_as_float(r[4 * v + 2]), __uint_as_float(r[4 * v + 3]));
             }
             tc_fence_before();
             __syncwarp();
@@ -371,7 +375,7 @@ __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
           float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
     TileSource src{&tmA, &tmB, D, M, N, K, nullptr, nullptr, nullptr, 0};
-    gemm_persistent<A_TERMS, BK, ST, F16>(src, (M / TC_BM) * (N / TC_BN), err);
+    gemm_persistent<A_TERMS, BK, ST, F16>(src, (M / TC_BM) * ((N + TC_BN - 1) / TC_BN), err);
 }
 
 // Grouped product over many pulses: the tiles of tiles[0 .. ntiles) of pulse
@@ -434,8 +438,8 @@ cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P,
 
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
                            int a_terms, int variant, int f16, int *err, cudaStream_t stream) {
-    if (M % TC_BM || N % TC_BN || K % 64) return cudaErrorInvalidValue;
-    const int grid = tc_grid((M / TC_BM) * (N / TC_BN));
+    if (M % TC_BM || N % 16 || K % 64) return cudaErrorInvalidValue;
+    const int grid = tc_grid((M / TC_BM) * ((N + TC_BN - 1) / TC_BN));
     TC_DISPATCH(a_terms, f16, variant, {
         const size_t smem = tc_smem_bytes(AT, BK, ST);
         cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<AT, BK, ST, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -522,17 +526,24 @@ k_build_E(const double *__restrict__ Y, const double *__restrict__ rho, int Nr, 
         }
 }
 
-// E' = [[Er, -Ei], [Ei, Er]] split into a_terms BF16 terms, stacked as
-// A[t][2Nr][2Nr] (term-major): h = bf16(v), m = bf16(v - h), l = bf16(v - h - m).
-__global__ void k_split_E(const double *__restrict__ Er, const double *__restrict__ Ei, int Nr, int a_terms,
+// Entry (m, k) of E' = [[Er, -Ei], [Ei, Er]] in the padded layout: blocks of
+// Nrp rows / columns, of which the first Nr hold E and the rest are zero.
+__device__ __forceinline__ double e_prime(const double *__restrict__ Er, const double *__restrict__ Ei, int Nr,
+                                          int Nrp, size_t m, size_t k) {
+    const size_t mr = m % Nrp, kr = k % Nrp;
+    if (mr >= (size_t)Nr || kr >= (size_t)Nr) return 0.0;
+    const bool mi = m >= (size_t)Nrp, ki = k >= (size_t)Nrp;
+    return (mi == ki) ? Er[mr * Nr + kr] : (mi ? Ei[mr * Nr + kr] : -Ei[mr * Nr + kr]);
+}
+
+// E' split into a_terms BF16 terms, stacked as A[t][2Nrp][2Nrp] (term-major):
+// h = bf16(v), m = bf16(v - h), l = bf16(v - h - m).
+__global__ void k_split_E(const double *__restrict__ Er, const double *__restrict__ Ei, int Nr, int Nrp, int a_terms,
                           __nv_bfloat16 *__restrict__ A) {
-    const size_t K2 = 2 * (size_t)Nr;
+    const size_t K2 = 2 * (size_t)Nrp;
     const size_t total = K2 * K2;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        size_t m = i / K2, k = i % K2;
-        size_t mr = m % Nr, kr = k % Nr;
-        bool mi = m >= (size_t)Nr, ki = k >= (size_t)Nr;
-        double v = (mi == ki) ? Er[mr * Nr + kr] : (mi ? Ei[mr * Nr + kr] : -Ei[mr * Nr + kr]);
+        const double v = e_prime(Er, Ei, Nr, Nrp, i / K2, i % K2);
         double rem = v;
         for (int t = 0; t < a_terms; ++t) {
             __nv_bfloat16 b = __double2bfloat16(rem);
@@ -556,7 +567,7 @@ __global__ void k_absmax_E(const double *__restrict__ Er, const double *__restri
 // E' 2^sa as two FP16 terms (h + l, ~22 bits), sa = 14 - e with max |E| < 2^e:
 // the largest entry lands in [2^13, 2^14), far from FP16's 65504, and entries
 // down to 2^-11 of it keep both terms normal.  sa goes to scale[NLSE_SC_SA].
-__global__ void k_split_E16(const double *__restrict__ Er, const double *__restrict__ Ei, int Nr,
+__global__ void k_split_E16(const double *__restrict__ Er, const double *__restrict__ Ei, int Nr, int Nrp,
                             __half *__restrict__ A, int *__restrict__ scale) {
     const float emax = __int_as_float(scale[NLSE_SC_EMAX]);
     int e = 0;
@@ -564,20 +575,17 @@ __global__ void k_split_E16(const double *__restrict__ Er, const double *__restr
     const int sa = min(max(14 - e, -100), 100);
     if (blockIdx.x == 0 && threadIdx.x == 0) scale[NLSE_SC_SA] = sa;
     const double sc = ldexp(1.0, sa);
-    const size_t K2 = 2 * (size_t)Nr;
+    const size_t K2 = 2 * (size_t)Nrp;
     const size_t total = K2 * K2;
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < total; i += (size_t)gridDim.x * blockDim.x) {
-        size_t m = i / K2, k = i % K2;
-        size_t mr = m % Nr, kr = k % Nr;
-        bool mi = m >= (size_t)Nr, ki = k >= (size_t)Nr;
-        double v = ((mi == ki) ? Er[mr * Nr + kr] : (mi ? Ei[mr * Nr + kr] : -Ei[mr * Nr + kr])) * sc;
+        const double v = e_prime(Er, Ei, Nr, Nrp, i / K2, i % K2) * sc;
         const __half h = __double2half(v);
         A[i] = h;
         A[total + i] = __double2half(v - (double)__half2float(h));
     }
 }
 
-cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
+cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, int Nrp, double dz, double komega,
                                   double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, int f16, int *scale,
                                   cudaStream_t stream) {
     dim3 grid((Nr + 31) / 32, (Nr + 31) / 32);
@@ -585,7 +593,7 @@ cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, 
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) return e;
     if (!f16) {
-        k_split_E<<<1024, 256, 0, stream>>>(Er, Ei, Nr, a_terms, A);
+        k_split_E<<<1024, 256, 0, stream>>>(Er, Ei, Nr, Nrp, a_terms, A);
         return cudaGetLastError();
     }
     e = cudaMemsetAsync(scale + NLSE_SC_EMAX, 0, sizeof(int), stream);
@@ -593,6 +601,6 @@ cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, 
     k_absmax_E<<<304, 256, 0, stream>>>(Er, Ei, (size_t)Nr * Nr, scale);
     e = cudaGetLastError();
     if (e != cudaSuccess) return e;
-    k_split_E16<<<1024, 256, 0, stream>>>(Er, Ei, Nr, reinterpret_cast<__half *>(A), scale);
+    k_split_E16<<<1024, 256, 0, stream>>>(Er, Ei, Nr, Nrp, reinterpret_cast<__half *>(A), scale);
     return cudaGetLastError();
 }

@@ -59,16 +59,17 @@ cudaError_t launch_field_bound(const float2 *u, size_t n, int Nt, int *scale, cu
 }
 
 // FP32 planar field -> BF16 hi/lo terms (diagnostic path of nlse_debug_operator_product).
-__global__ void k_split_field(const float *__restrict__ w, __nv_bfloat16 *__restrict__ Fb, size_t n) {
+__global__ void k_split_field(const float *__restrict__ w, __nv_bfloat16 *__restrict__ hi, size_t lo_off,
+                              size_t n) {
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
         float v = w[i];
         __nv_bfloat16 h = __float2bfloat16_rn(v);
-        Fb[i] = h;
-        Fb[n + i] = __float2bfloat16_rn(v - __bfloat162float(h));
+        hi[i] = h;
+        hi[lo_off + i] = __float2bfloat16_rn(v - __bfloat162float(h));
     }
 }
 
-cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st) {
-    k_split_field<<<1024, 256, 0, st>>>(w, Fb, n);
+cudaError_t launch_split_field(const float *w, __nv_bfloat16 *hi, size_t lo_off, size_t n, cudaStream_t st) {
+    k_split_field<<<1024, 256, 0, st>>>(w, hi, lo_off, n);
     return cudaGetLastError();
 }

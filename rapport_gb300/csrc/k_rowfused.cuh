@@ -76,9 +76,9 @@ __device__ __forceinline__ float block_max(float v) {
 template <int NT>
 __device__ __forceinline__ void store_state_row(const float2 *s, int r, const RowFusedArgs &a, float *F32,
                                                 __nv_bfloat16 *Fb, int g_out) {
-    const size_t rows = 2 * (size_t)a.Nr;
-    float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nr + r) * NT;
-    __nv_bfloat16 *hre = Fb + (size_t)r * NT, *him = Fb + ((size_t)a.Nr + r) * NT;
+    const size_t rows = 2 * (size_t)a.Nrp;
+    float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nrp + r) * NT;
+    __nv_bfloat16 *hre = Fb + (size_t)r * NT, *him = Fb + ((size_t)a.Nrp + r) * NT;
     __nv_bfloat16 *lre = hre + rows * NT, *lim = him + rows * NT;
     if (!a.f16) {
         for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
@@ -131,8 +131,8 @@ __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs
     const float ds = a.f16 ? ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) +
                                             __ldcg(&a.scale[NLSE_SC_SB + g_in % 2])))
                            : 1.0f;
-    const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nr + r) * NT;
-    const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nr + r) * NT;
+    const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nrp + r) * NT;
+    const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nrp + r) * NT;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
         const float2 xr = *reinterpret_cast<const float2 *>(fr + t), xi = *reinterpret_cast<const float2 *>(fi + t);
         const float2 yr = *reinterpret_cast<const float2 *>(dr + t), yi = *reinterpret_cast<const float2 *>(di + t);
@@ -213,8 +213,8 @@ __device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / row_threads<NT>()]
     const float ds = a.f16 ? ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) +
                                             __ldcg(&a.scale[NLSE_SC_SB + g_in % 2])))
                            : 1.0f;
-    const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nr + r) * NT;
-    const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nr + r) * NT;
+    const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nrp + r) * NT;
+    const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nrp + r) * NT;
 #pragma unroll
     for (int m = 0; m < NT / row_threads<NT>(); ++m) {
         const int t = (int)threadIdx.x + m * row_threads<NT>();
@@ -231,9 +231,9 @@ __device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / row_threads<NT>()]
 template <int NT>
 __device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / row_threads<NT>()], int r,
                                                  const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, int g_out) {
-    const size_t rows = 2 * (size_t)a.Nr;
-    float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nr + r) * NT;
-    __nv_bfloat16 *hre = Fb + (size_t)r * NT, *him = Fb + ((size_t)a.Nr + r) * NT;
+    const size_t rows = 2 * (size_t)a.Nrp;
+    float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nrp + r) * NT;
+    __nv_bfloat16 *hre = Fb + (size_t)r * NT, *him = Fb + ((size_t)a.Nrp + r) * NT;
     __nv_bfloat16 *lre = hre + rows * NT, *lim = him + rows * NT;
     if (!a.f16) {
 #pragma unroll

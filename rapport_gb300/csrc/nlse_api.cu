@@ -336,12 +336,17 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     NLSE_TRY(dev_upload<float2>(err, &c->d_work, nullptr, (size_t)Nr * Nt));
     NLSE_TRY(dev_upload<int>(err, &c->d_flag, nullptr, 4));
     NLSE_TRY(dev_upload<int>(err, &c->d_scale, nullptr, NLSE_SC_N));
-    // split-BF16 path: operator terms, Omega-domain state, tensor maps
+    // split (tensor-core) path: operator terms, Omega-domain state, tensor maps.
+    // Each plane of the state and each block of E' has Nrp = Nr rounded up to
+    // 64 rows (the product tiles 2 Nrp by 128); the padding rows and columns
+    // are zero and no kernel writes them.  N_t < 256 is one partial tile
+    // column: its loads read zeros past N_t and its stores stop at N_t.
     c->a_terms = 3;
     c->cached_dz_op = NAN;
-    c->split_ok = (Nr % 64 == 0) && (Nt % 256 == 0);
+    c->Nrp = (Nr + 63) / 64 * 64;
+    c->split_ok = c->Nrp <= 8192;
     if (c->split_ok) {
-        const size_t K2 = 2 * (size_t)Nr;
+        const size_t K2 = 2 * (size_t)c->Nrp;
         NLSE_TRY(dev_upload(err, &c->d_Y64, d->Y, (size_t)Nr * Nr));
         NLSE_TRY(dev_upload<double>(err, &c->d_Er, nullptr, (size_t)Nr * Nr));
         NLSE_TRY(dev_upload<double>(err, &c->d_Ei, nullptr, (size_t)Nr * Nr));
@@ -350,6 +355,16 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
         NLSE_TRY(dev_upload<__nv_bfloat16>(err, &c->d_Fb, nullptr, 2 * K2 * Nt));
         NLSE_TRY(dev_upload<float>(err, &c->d_D, nullptr, K2 * Nt));
         NLSE_TRY(dev_upload<float2>(err, &c->d_Ptf, nullptr, 2 * (size_t)Nt));
+        {
+            cudaError_t ze = cudaMemset(c->d_F32, 0, K2 * Nt * sizeof(float));
+            if (ze == cudaSuccess) ze = cudaMemset(c->d_Fb, 0, 2 * K2 * Nt * sizeof(__nv_bfloat16));
+            if (ze == cudaSuccess) ze = cudaMemset(c->d_D, 0, K2 * Nt * sizeof(float));
+            if (ze != cudaSuccess) {
+                nlse_set_error(err, NLSE_ERR_CUDA, "state init: %s", cudaGetErrorString(ze));
+                free_ctx(c);
+                return NLSE_ERR_CUDA;
+            }
+        }
         alignas(64) CUtensorMap m;
         cuuint32_t estr[2] = {1, 1};
         EncodeTiledFn cuTensorMapEncodeTiled = encode_tiled();
@@ -524,7 +539,7 @@ static int autotune_gemm(nlse_ctx *c, cudaStream_t st);
 static int split_ready(nlse_ctx *c, double dz, int f16, cudaStream_t st) {
     if (!c->split_ok)
         return bad(c, NLSE_ERR_UNSUPPORTED,
-                   "split-BF16 mode needs Nr % 64 == 0 and Nt % 256 == 0 (this grid: use the plain mode)");
+                   "the split (tensor-core) forms take Nr <= 8192 (this grid: use the plain mode)");
     if (c->d_P2)
         return bad(c, NLSE_ERR_UNSUPPORTED,
                    "space-time focusing makes the diffraction phase depend on Omega, so the half step has no "
@@ -534,8 +549,8 @@ static int split_ready(nlse_ctx *c, double dz, int f16, cudaStream_t st) {
     if (dz == c->cached_dz_op && f16 == c->op_f16) return NLSE_OK;
     {
         PROF(K_BUILD_OP);
-        s = launched(c, launch_build_operator(c->d_Y64, c->d_rho_modes, c->Nr, dz, c->komega, c->d_Er, c->d_Ei, 3,
-                                              c->d_A, f16, c->d_scale, st),
+        s = launched(c, launch_build_operator(c->d_Y64, c->d_rho_modes, c->Nr, c->Nrp, dz, c->komega, c->d_Er,
+                                              c->d_Ei, 3, c->d_A, f16, c->d_scale, st),
                      "operator build");
     }
     if (s == NLSE_OK) {
@@ -551,6 +566,7 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
     a.Nr = c->Nr;
     a.Nt = c->Nt;
     a.logNt = c->logNt;
+    a.Nrp = c->Nrp;
     a.tw = c->d_tw;
     a.Pt = c->d_Ptf;
     a.mask_r = c->d_mask_r;
@@ -568,7 +584,7 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
 }
 
 static cudaError_t tc_gemm_raw(nlse_ctx *c, int variant, cudaStream_t st) {
-    const int K2 = 2 * c->Nr;
+    const int K2 = 2 * c->Nrp;
     const CUtensorMap *a = variant ? &c->tmA32 : &c->tmA, *b = variant ? &c->tmB32 : &c->tmB;
     return launch_gemm_tc(a, b, c->d_D, K2, c->Nt, K2, c->a_terms, variant, c->op_f16, c->d_flag, st);
 }
@@ -844,10 +860,17 @@ extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *o
     if (!field_ok(c, w, "w") || !field_ok(c, out, "out")) return NLSE_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
     NLSE_SEQ(split_ready(c, dz, 0, st));
-    const size_t n = 2 * (size_t)c->Nr * c->Nt;
-    NLSE_SEQ(launched(c, launch_split_field(w, c->d_Fb, n, st), "split field"));
+    // w's Re / Im planes (Nr rows each) into the state's planes of Nrp rows
+    const size_t plane = (size_t)c->Nr * c->Nt, pplane = (size_t)c->Nrp * c->Nt;
+    for (int h = 0; h < 2; ++h)
+        NLSE_SEQ(launched(c, launch_split_field(w + h * plane, c->d_Fb + h * pplane, 2 * pplane, plane, st),
+                          "split field"));
     NLSE_SEQ(tc_gemm(c, st));
-    return launched(c, cudaMemcpyAsync(out, c->d_D, n * sizeof(float), cudaMemcpyDeviceToDevice, st), "copy");
+    for (int h = 0; h < 2; ++h)
+        NLSE_SEQ(launched(c, cudaMemcpyAsync(out + h * plane, c->d_D + h * pplane, plane * sizeof(float),
+                                             cudaMemcpyDeviceToDevice, st),
+                          "copy"));
+    return NLSE_OK;
 }
 
 extern "C" int nlse_debug_wait_timeout(nlse_ctx *c, int limit_us, void *stream) {
@@ -1156,9 +1179,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
             BATCH_FAIL(st, "pulse %d: %s", i, msg);
         }
         if (!b->ctx[i]->split_ok)
-            BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: batches run the split-BF16 form, which needs Nr %% 64 == 0 "
-                                             "and Nt %% 256 == 0",
-                       i);
+            BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: batches run the split forms, which take Nr <= 8192", i);
         if (b->ctx[i]->d_P2)
             BATCH_FAIL(NLSE_ERR_UNSUPPORTED,
                        "pulse %d: space-time focusing makes the diffraction phase depend on Omega (no single radial "
@@ -1185,7 +1206,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         memcpy(&maps[4 * i + 1], &c->tmB, sizeof(CUtensorMap));
         memcpy(&maps[4 * i + 2], &oc->tmA32, sizeof(CUtensorMap));
         memcpy(&maps[4 * i + 3], &c->tmB32, sizeof(CUtensorMap));
-        const int M = 2 * c->Nr;
+        const int M = 2 * c->Nrp;
         for (int m0 = 0; m0 < M; m0 += 128)
             for (int n0 = 0; n0 < c->Nt; n0 += 256) tiles.push_back(GemmTile{i, m0, n0, 0});
         // row classes: one per (N_t, full-physics terms)
@@ -1211,7 +1232,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
     if (n >= 2) {
         int acc = 0, p = 0;
         while (p < n - 1 && 2 * acc < b->ntiles) {
-            acc += (2 * b->ctx[p]->Nr / 128) * (b->ctx[p]->Nt / 256);
+            acc += (2 * b->ctx[p]->Nrp / 128) * ((b->ctx[p]->Nt + 255) / 256);
             ++p;
         }
         b->lane_pulse = p;
@@ -1339,9 +1360,9 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
             P.u = (float2 *)u[i];
             P.a.rho_s = q->sc.ste ? rho_s[i] : nullptr;
             P.ste_work = q->sc.ste ? q->d_work : nullptr;
-            P.M = 2 * q->Nr;
+            P.M = 2 * q->Nrp;
             P.N = q->Nt;
-            P.K = 2 * q->Nr;
+            P.K = 2 * q->Nrp;
         }
         NLSE_CUDA_TRY(&b->err, cudaMemcpyAsync(b->d_pulses, b->h_pulses, b->n * sizeof(BatchPulse),
                                                cudaMemcpyHostToDevice, st));

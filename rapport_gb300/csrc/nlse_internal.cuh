@@ -73,6 +73,7 @@ struct ScanParams {
 // Arguments of the fused row kernels (k_rowfused.cu).
 struct RowFusedArgs {
     int Nr, Nt, logNt;
+    int Nrp;              // rows of one plane (Re, Im) of the Omega-domain state: Nr rounded up to 64
     const float2 *tw;     // forward twiddles
     const float2 *Pt;     // e^{i dk dz/2} spec_mask (no 1/Nt); Pt[Nt + k]: its rounding remainder
     const float *mask_r;  // Nr
@@ -112,7 +113,7 @@ struct BatchPulse {
     float2 *u;
     float2 *ste_work;     // exciton channel: row_next writes the physical field here and
                           // the two-population march runs as its own kernel (else NULL)
-    int M, N, K;  // GEMM sizes: 2Nr, Nt, 2Nr
+    int M, N, K;  // GEMM sizes: 2Nrp, Nt, 2Nrp
 };
 
 // One 128 x 256 tile of the grouped tensor-core product.
@@ -155,6 +156,8 @@ struct nlse_ctx {
     int *d_flag;           // device status word
     // split-BF16 path (allocated when Nr % 64 == 0 and Nt % 256 == 0)
     int split_ok, a_terms;
+    int Nrp;               // Nr rounded up to a multiple of 64: rows of one plane of the split-form state
+                           // and of one block of E' (the padding rows / columns are zero)
     int op_f16;            // format of the operator in d_A (0: 3 BF16 terms, 1: 2 scaled FP16 terms)
     int *d_scale;          // NLSE_SC_N scale cells of the split-FP16 form
     double cached_dz_op;   // dz of the operator currently in d_A
@@ -216,7 +219,8 @@ cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float
                            int a_terms, int variant, int f16, int *err, cudaStream_t stream);
 // Builds E in FP64 and splits it: 3 (or a_terms) BF16 terms, or with f16 two
 // FP16 terms of E 2^sa (sa from max |E|, stored in scale[NLSE_SC_SA]).
-cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, double dz, double komega,
+// E' is laid out for Nrp >= Nr rows per block, zero beyond Nr.
+cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, int Nrp, double dz, double komega,
                                   double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, int f16, int *scale,
                                   cudaStream_t stream);
 // Failure-path probe: a bounded mbarrier wait that runs out after limit_ns and
@@ -231,7 +235,8 @@ cudaError_t launch_fft_phase_ifft_tables(float2 *u, int Nr, int Nt, int logNt, c
 void nlse_set_thread_error(int status, const char *msg);
 cudaError_t launch_record(nlse_ctx *c, const float2 *u, const float *rho, const float *rho_s, const int *bin_of_t,
                           int nbins, double *out, cudaStream_t st);
-cudaError_t launch_split_field(const float *w, __nv_bfloat16 *Fb, size_t n, cudaStream_t st);
+// n values of w -> hi at hi[i], lo at hi[lo_off + i] (BF16)
+cudaError_t launch_split_field(const float *w, __nv_bfloat16 *hi, size_t lo_off, size_t n, cudaStream_t st);
 // kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call),
 // 3 = nonlinear with the full-physics block (N_t <= 4096);
 // g = index of the GEMM input the kernel consumes (the split-FP16 scales; -1 for the entry)
@@ -358,11 +363,14 @@ __host__ __device__ constexpr int fft_radix(int N, int NS) {
     return (N / NS) % 8 == 0 ? 8 : ((N / NS) % 4 == 0 ? 4 : 2);
 }
 
-// Twiddle table layout: the pass at NS > 1 owns NS rows of fft_tw_row(R)
-// float2, row k = exp(-2 pi i r k (N / (NS R)) / N) for r = 1 .. R-1, padded
-// to an even count so a butterfly reads its twiddles with R/2 16-byte loads
-// from one contiguous row (the values are those of a plain exp(-2 pi i m / N)
-// table; only the order differs).
+// Twiddle table layout: the pass at NS > 1 (radix R) owns a block of
+// NS * fft_tw_row(R) float2: for butterfly row k = 0 .. NS-1 the factors
+// exp(-2 pi i r k (N / (NS R)) / N), r = 1 .. R-1 (padded to an even count),
+// in pairs (r = 2q + 1, 2q + 2) of one float4 each, stored column-major --
+// float4 q of row k at q NS + k.  The 32 lanes of a warp hold consecutive
+// butterflies, i.e. consecutive k, so each 16-byte twiddle load of a warp is
+// one contiguous 512-byte run (4 cache lines) instead of 32 rows spread over
+// up to 2 KB; the values are those of a plain exp(-2 pi i m / N) table.
 __host__ __device__ constexpr int fft_tw_row(int R) { return R == 2 ? 2 : R; }
 
 __host__ __device__ constexpr int fft_tw_offset(int N, int NS) {
@@ -389,11 +397,11 @@ __host__ __device__ constexpr int fft_tw_size(int N) { return fft_tw_offset(N, N
 // row k of the pass (and its rounding remainders).
 template <int R, bool INV, int N, int NS>
 __device__ __forceinline__ void apply_twiddles(float2 *v, int k, const float2 *__restrict__ tw) {
-    const float4 *w4 = reinterpret_cast<const float4 *>(tw + fft_tw_offset(N, NS) + k * fft_tw_row(R));
+    const float4 *w4 = reinterpret_cast<const float4 *>(tw + fft_tw_offset(N, NS)) + k;
     float2 w[fft_tw_row(R)];
 #pragma unroll
     for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
-        const float4 p = __ldg(&w4[q]);
+        const float4 p = __ldg(&w4[q * NS]);
         w[2 * q] = make_float2(p.x, p.y);
         w[2 * q + 1] = make_float2(p.z, p.w);
     }
@@ -403,7 +411,7 @@ __device__ __forceinline__ void apply_twiddles(float2 *v, int k, const float2 *_
     float2 wl[fft_tw_row(R)];
 #pragma unroll
     for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
-        const float4 p = __ldg(&l4[q]);
+        const float4 p = __ldg(&l4[q * NS]);
         wl[2 * q] = make_float2(p.x, p.y);
         wl[2 * q + 1] = make_float2(p.z, p.w);
     }
@@ -538,15 +546,16 @@ __device__ __forceinline__ float2 *fft_regs(float2 (&v)[N / T], float2 *A, float
     return fft_regs_pass<N, 1, INV, T>(v, B, A, tw);
 }
 
-// Entry e of the twiddle table of an N-point row (host or device, FP64 then
-// rounded): the pass, row k and r it stands for give m = r k N / (NS R).
+// Entry e (a float2 index) of the twiddle table of an N-point row (host or
+// device, FP64 then rounded): the pass, row k and r it stands for give
+// m = r k N / (NS R) (layout above: float4 q of row k at q NS + k).
 __host__ __device__ inline void fft_tw_entry(int N, int e, int *m_out) {
     int off = 0, m = -1;
     for (int NS = 1; NS < N; NS *= fft_radix(N, NS)) {
         if (NS == 1) continue;
         const int R = fft_radix(N, NS), row = fft_tw_row(R), n = NS * row;
         if (e < off + n) {
-            const int k = (e - off) / row, r = (e - off) % row + 1;
+            const int el = e - off, f = el >> 1, q = f / NS, k = f % NS, r = 2 * q + (el & 1) + 1;
             m = r < R ? r * k * (N / (NS * R)) : -1;  // -1: padding
             break;
         }

@@ -70,12 +70,35 @@ def test_batch_two_calls_equal_one():
         assert rel_l2(host(c[i]), host(a[i])) < 1e-6
 
 
-def test_batch_rejects_untileable_grid():
+def test_batch_takes_padded_grids():
+    """N_r not a multiple of 64 (padded inside each context) and N_t = 128 (one
+    partial tile column) in one grouped product: every pulse bit-identical to
+    its single-context run and within the parity tolerance of the oracle."""
     import rapport_gb300 as R
     from rapport_gb300 import _lib
-    cfg = R.workload_config(64, 128, 1e-4, 1e-5, 3e-13, DZ, 1)
-    with pytest.raises(_lib.NLSEError, match="split-BF16"):
-        _lib.Batch([cfg], [R.build_grids(cfg)])
+    shapes = [(100, 128, 1.5e-4), (64, 256, 1e-4), (70, 128, 1.1e-4)]
+    cfgs, grids, u0s = [], [], []
+    for i, (Nr, Nt, Rm) in enumerate(shapes):
+        cfg = R.workload_config(Nr, Nt, Rm, 1e-5, 3e-13 * Nt / 256, DZ, STEPS)
+        g = R.build_grids(cfg)
+        cfgs.append(cfg)
+        grids.append(g)
+        u0s.append(R.envelope_lens(1e-5, 100e-15, 1.5 + 0.3 * i, 1e-2, 40 + i)(g["rr"], g["tt"], cfg, g))
+    b = _lib.Batch(cfgs, grids)
+    us = [dev(u) for u in u0s]
+    rhos = [dev(np.zeros(u.shape)) for u in u0s]
+    b.propagate(us, rhos, None, DZ, STEPS)
+    assert b.device_status() == 0
+    for i, ((Nr, Nt, Rm), cfg, g, u0) in enumerate(zip(shapes, cfgs, grids, u0s)):
+        ctx = _lib.Context(cfg, g)
+        u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+        ctx.propagate(u, rho, rs, DZ, STEPS, _lib.MODE_SPLIT_BF16)
+        assert np.array_equal(host(us[i]), host(u)), i
+        assert np.array_equal(host(rhos[i]), host(rho)), i
+        og = O.OracleGrid(O.workload_config(Nr, Nt, Rm, 1e-5, 3e-13 * Nt / 256))
+        uo, rho_o, _ = og.propagate(u0.copy(), STEPS, DZ)
+        assert rel_l2(host(us[i]), uo) < 5e-5, i
+        assert np.abs(host(rhos[i]) - rho_o).max() <= 1e-3 * max(rho_o.max(), 1e-30), i
 
 
 def test_batch_shared_operator_pulses_match_single_contexts():

@@ -138,11 +138,62 @@ def test_step_split_equals_plain_within_fp32(small, mode):
     assert rel_l2(host(u2), ref) < 2e-5
 
 
-def test_split_rejects_unsupported_grid(tiny):
-    from rapport_gb300._lib import NLSEError
-    c = Case.from_fixture(tiny)  # Nt = 128: not a multiple of the 256-column tile
-    with pytest.raises(NLSEError, match="split-BF16"):
-        c.ctx.half_linear(dev(c.u0), c.dz, MODE_SPLIT_BF16)
+@pytest.mark.parametrize("mode", SPLIT_MODES)
+def test_split_small_nt_matches_reference_fixture(tiny, mode):
+    """N_t = 128 (below the 256-column tile: one partial tile column) in the
+    tensor-core forms, against the reference's own z-steps (tiny.npz) at the
+    plain form's tolerance."""
+    c = Case.from_fixture(tiny)
+    u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+    done = 0
+    for j, s in enumerate(tiny["steps_kept"]):
+        c.ctx.propagate(u, rho, rs, c.dz, int(s) - done, mode)
+        done = int(s)
+        assert rel_l2(host(u)[tiny["rows"]], tiny["u_steps"][j]) < 1e-4, s
+        ro = tiny["rho_steps"][j]
+        assert np.abs(host(rho)[tiny["rows"]] - ro).max() <= 1e-3 * max(ro.max(), 1e-30), s
+    assert c.ctx.device_status() == 0
+
+
+# radial sizes that are not multiples of 64: the context pads them (zero rows
+# and columns of E', zero padding rows of the state).  1023 and 2999 are the
+# grids run(Nr=1024) and run(Nr=3000) build (Config.N - 1 points).
+PADDED = [dict(Nr=100, Nt=256, R_max=1.5e-4, w0=1e-5, T_half=3e-13, fwhm=100e-15, E=2.0, f=1e-2, dz=5e-6),
+          dict(Nr=1023, Nt=2048, R_max=2e-3, w0=150e-6, T_half=800e-15, fwhm=100e-15, E=5.0, f=0.1, dz=2.5e-6),
+          dict(Nr=2999, Nt=1024, R_max=3e-3, w0=150e-6, T_half=600e-15, fwhm=100e-15, E=5.0, f=0.1, dz=2.5e-6)]
+
+
+@pytest.mark.parametrize("k", range(len(PADDED)))
+def test_padded_radial_grid_vs_fp64(k):
+    import fp64_gpu
+    p = PADDED[k]
+    c = Case(**p)
+    ur, rr = fp64_gpu.FP64GPU(c.og).propagate(c.u0, 2, c.dz)
+    ur, rr = ur.cpu().numpy(), rr.cpu().numpy()
+    for mode in SPLIT_MODES:
+        u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+        c.ctx.propagate(u, rho, rs, c.dz, 2, mode)
+        assert rel_l2(host(u), ur) < 2e-5, (p["Nr"], mode)
+        assert np.abs(host(rho) - rr).max() <= 1e-3 * max(rr.max(), 1e-30), (p["Nr"], mode)
+        hl = dev(c.u0)
+        c.ctx.half_linear(hl, c.dz, mode)
+        assert rel_l2(host(hl), c.og.half_linear(c.u0, c.dz)) < 2e-5, (p["Nr"], mode)
+    assert c.ctx.device_status() == 0
+
+
+def test_padded_operator_product():
+    """The diagnostic product on a padded grid equals E'w on the unpadded E'."""
+    import torch
+    c = Case(**PADDED[0])
+    rng = np.random.default_rng(13)
+    w = rng.standard_normal((2 * c.og.Nr, c.og.Nt))
+    wd = torch.from_numpy(w.astype(np.float32)).cuda()
+    out = torch.empty_like(wd)
+    c.ctx.debug_operator_product(wd, out, c.dz)
+    A = _operator(c)
+    ref = A @ w.astype(np.float32).astype(np.float64)
+    o = out.cpu().numpy().astype(np.float64)
+    assert np.all(np.abs(o - ref) <= 2e-5 * (np.abs(A) @ np.abs(w)) + 1e-30)
 
 
 def test_config2_z_steps_split_vs_oracle():

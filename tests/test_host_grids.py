@@ -114,6 +114,9 @@ def test_linear_mode_resolution():
     assert mk().linear_mode == "auto"
     assert resolved_linear_mode(mk(N=1025, Nt=2048, enable_space_time_focusing=False)) == "split_bf16"
     assert resolved_linear_mode(mk(N=1025, Nt=2048, enable_space_time_focusing=True)) == "plain"
-    assert resolved_linear_mode(mk(N=1000, Nt=2048, enable_space_time_focusing=False)) == "plain"
+    # N_r = 999 (the context pads it to 1024) and N_t = 128 (one partial tile) run split too
+    assert resolved_linear_mode(mk(N=1000, Nt=2048, enable_space_time_focusing=False)) == "split_bf16"
+    assert resolved_linear_mode(mk(N=65, Nt=128, enable_space_time_focusing=False)) == "split_bf16"
+    assert resolved_linear_mode(mk(N=9000, Nt=128, enable_space_time_focusing=False)) == "plain"
     assert resolved_linear_mode(mk(linear_mode="split_f16")) == "split_f16"
     assert split_supported(mk(N=257, Nt=512, enable_space_time_focusing=False))
