@@ -12,9 +12,13 @@
  * Carrier densities: row-major float32 (Nr x Nt), cm^-3.
  *
  * Every function returns an nlse_status.  On failure the context keeps a
- * message, readable with nlse_get_last_error.  Launches are asynchronous on
- * the given stream (a cudaStream_t passed as void*; NULL = legacy default).
- * A context is not thread-safe; use one context per host thread.
+ * message, readable with nlse_get_last_error (errors of calls without a
+ * context are kept per host thread).  Launches are asynchronous on the given
+ * stream (a cudaStream_t passed as void*; NULL = legacy default).  A context
+ * is not thread-safe; use one context per host thread.  Calls on one context
+ * share its workspace: issue them on one stream, or order them with events
+ * when they use different streams (a batch does this itself: a call on a new
+ * stream waits for the previous call's work).
  *
  * Reference interfaces replaced (paths in omatousou/Rapport, relative to
  * ".github/deliverable (3)/sim"):

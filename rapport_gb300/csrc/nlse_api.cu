@@ -1029,6 +1029,9 @@ struct nlse_batch {
     int ncls;
     int *d_flag;
     cudaEvent_t staged;      // the last upload of h_pulses has been consumed
+    cudaEvent_t done;        // end of the last nlse_batch_propagate's work, on last_stream
+    cudaStream_t last_stream;
+    int has_done;
     double last_dz;
     void *last_ptrs[3];      // u[0], rho[0] of the last upload (cheap change check)
     int uploaded;
@@ -1047,6 +1050,7 @@ static void batch_free(nlse_batch *b) {
     for (int c = 0; c < b->ncls; ++c)
         if (b->cls[c].d_work) cudaFree(b->cls[c].d_work);
     if (b->staged) cudaEventDestroy(b->staged);
+    if (b->done) cudaEventDestroy(b->done);
     if (b->graph) cudaGraphExecDestroy(b->graph);
     if (b->cap_stream) cudaStreamDestroy(b->cap_stream);
     if (b->cap_stream2) cudaStreamDestroy(b->cap_stream2);
@@ -1249,6 +1253,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_flag, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->d_flag, 0, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
+    if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     b->ncls = nlog;
     for (int k = 0; k < nlog && e == cudaSuccess; ++k) {
         b->cls[k].logNt = logs[k];
@@ -1329,6 +1334,10 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
     if (nsteps == 0) return NLSE_OK;
     cudaStream_t st = (cudaStream_t)stream;
     nlse_ctx *c = b->ctx[0];  // profiling records go to the first pulse's context
+    // A call on another stream than the last one first waits for the last
+    // call's kernels: they read the pulse table and the shared per-pulse state
+    // that this call is about to rewrite.
+    if (b->has_done && st != b->last_stream) NLSE_CUDA_TRY(&b->err, cudaStreamWaitEvent(st, b->done, 0));
     bool changed = !(dz == b->last_dz) || !b->uploaded || b->last_f16 != b->f16;
     for (int i = 0; i < b->n; ++i) {
         if (!field_ok(b->ctx[i], u[i], "u") || !field_ok(b->ctx[i], rho[i], "rho") ||
@@ -1430,5 +1439,8 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
         if (!last && b->nste) BSEQ(K_RATE_SCAN, batch_ste_marches(b, -1, st), "batch exciton march");
     }
 #undef BSEQ
+    NLSE_CUDA_TRY(&b->err, cudaEventRecord(b->done, st));
+    b->last_stream = st;
+    b->has_done = 1;
     return NLSE_OK;
 }
