@@ -384,6 +384,8 @@ def run_ours(args, rank, world, local_rank):
                        kernel_times="second identical pass of K steps with per-launch events"),
         "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "autotuned": {"gemm_variant": ctx.gemm_variant(),
+                      "row_plans": dict(zip(("row_nl", "row_next"), _lib.row_plans(Nt)))},
         "clocks": clocks,
         "forms": dict({k + "_single_pulse": (round(v["zsteps_per_s"], 1) if "zsteps_per_s" in v else v)
                        for k, v in results.items()},
@@ -483,6 +485,10 @@ def run_config4(args, rank, world, local_rank):
                                                                      if k == "k_gemm_tc") * 1e-3) / 1e12,
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
         "finite": ok,
+        "row_plans": {str(nt): dict(zip(("row_nl", "row_next"), _lib.row_plans(nt)))
+                      for nt in sorted({pulses[i]["Nt"] for i in mine})},
+        "gemm_variant": bt.context(0).gemm_variant(),
+        "launches_per_z_step": "2 grouped products + 2 row launches per N_t class (one per half step)",
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

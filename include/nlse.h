@@ -70,8 +70,12 @@ enum {
     NLSE_F_PLASMA_ABSORB  = 1 << 3,  /* enable_plasma_absorption    */
     NLSE_F_KERR_RAMAN     = 1 << 4,  /* enable_kerr_raman  (N_t <= 4096) */
     NLSE_F_SELF_STEEP     = 1 << 5,  /* enable_self_steepening (N_t <= 4096) */
-    NLSE_F_SPACE_TIME     = 1 << 6,  /* enable_space_time_focusing (N_t <= 4096,
-                                        plain mode only)          */
+    NLSE_F_SPACE_TIME     = 1 << 6,  /* enable_space_time_focusing (N_t <= 4096;
+                                        in the split modes and in batches the
+                                        half step's correction runs as
+                                        Y (P(rho, Omega) - 1) Y in scaled FP16
+                                        terms, whichever split mode is asked
+                                        for)                       */
     NLSE_F_STE            = 1 << 7   /* enable_ste (N_t <= 4096)    */
 };
 
@@ -204,14 +208,15 @@ int nlse_debug_operator_product(nlse_ctx *ctx, const float *w, float *out, doubl
                                 void *stream);
 
 /*
- * Batches: many pulses, each with its own grid (Nr % 64 == 0, Nt % 256 == 0)
+ * Batches: many pulses, each with its own grid (Nr <= 8192, padded inside)
  * and tables, advanced together in the split-BF16 form: per z-step ONE
  * grouped tensor-core launch per half step over every pulse's tiles, and one
  * row-kernel launch per distinct (Nt, full-physics terms).  The batch owns one
  * context per pulse.  Pulses may carry the Raman / self-steepening terms
  * (Nt <= 4096) and the exciton channel (its two-population march runs as one
- * launch per such pulse); space-time focusing is refused (NLSE_ERR_UNSUPPORTED:
- * its half step has no single radial operator).
+ * launch per such pulse); pulses with space-time focusing run their half
+ * step's correction as Y (P(rho, Omega) - 1) Y: two grouped launches of their
+ * own and one phase pass per such pulse.
  */
 typedef struct nlse_batch nlse_batch;
 int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch **out);
@@ -237,6 +242,19 @@ void nlse_batch_destroy(nlse_batch *b);
  * make it before any stream capture).  A batch uses its first pulse's. */
 int nlse_set_gemm_variant(nlse_ctx *ctx, int variant);
 int nlse_get_gemm_variant(const nlse_ctx *ctx);
+
+/* Row-kernel plans of the split forms for N_t on the current device: for
+ * the nonlinear row kernel 0 = shared-memory body, 1 = register-resident body
+ * (N_t >= 512), 2 = the shared-memory body with a compact FFT (one run-time
+ * pass body for both transforms); for the next-state row kernel 0 = the default body
+ * (register-resident from N_t = 2048), 1 = the shared-memory body (N_t >= 2048).
+ * Both plans of a kernel compute identical results.  The first context with a
+ * given N_t times both on synthetic rows and keeps the faster (get returns
+ * -1 before that); set pins a pick (-1: time again at the next nlse_create)
+ * and applies to the next launches of every context and batch on the device.
+ * No counterpart in the reference (its transforms are library FFTs). */
+int nlse_get_row_plan(int Nt, int *nl_plan, int *next_plan);
+int nlse_set_row_plan(int Nt, int nl_plan, int next_plan);
 
 /* Number of BF16 terms carrying E in the split mode: 3 (default; 4 MMAs per
  * k-slice) or 2 (the plain hi/lo scheme, 3 MMAs). */

@@ -9,9 +9,10 @@ oracle by tests/test_gpu_accuracy.py before it is used as the long-run FP64
 reference.  Only tests may use it; it never runs on the product path.
 
 Follows (paths under ``deliverable (3)/sim``): half_linear operators.py:47-53,
-split operators.py:89-146 with the measured toggles (Raman, self-steepening,
-space-time focusing and the exciton channel off: split is pointwise and its
-transforms are identities), update_plasma operators.py:165-183 +
+split operators.py:89-146 with the measured toggles (Raman, self-steepening and
+the exciton channel off) and optionally space-time focusing (the Omega-
+dependent diffraction phase of half_linear, operators.py:50, and the U^-1
+filter of split, operators.py:141-144), update_plasma operators.py:165-183 +
 kernels.py:36-106, step integrator.py:138-149.
 """
 import ctypes
@@ -44,7 +45,7 @@ class FP64GPU:
     def __init__(self, og, device="cuda"):
         import torch
         p = og.p
-        for k in ("enable_kerr_raman", "enable_self_steepening", "enable_space_time_focusing", "enable_ste"):
+        for k in ("enable_kerr_raman", "enable_self_steepening", "enable_ste"):
             if p[k]:
                 raise NotImplementedError(f"{k} is not restated here")
         self.t = torch
@@ -70,12 +71,16 @@ class FP64GPU:
         self.on_abs = bool(p["enable_plasma_absorption"])
         self.on_def = bool(p["enable_plasma_defocusing"])
         self.rho_max = p["rho_max"]
+        self.stf = bool(p["enable_space_time_focusing"])
+        self.inv_U_op = torch.tensor(og.inv_U_op, **f64)
+        self.inv_U_nl = torch.tensor(og.inv_U_nl, **f64)
         self._phase_dz = None
 
     def _phase(self, dz):
         if self._phase_dz != dz:
             t = self.t
-            ph = (self.delta_k[None, :] - self.rho2[:, None] / (2 * self.og.komega)) * dz / 2
+            # operators.py:50: the radial phase carries U^-1(Omega) with space-time focusing
+            ph = (self.delta_k[None, :] - self.rho2[:, None] / (2 * self.og.komega) * self.inv_U_op[None, :]) * dz / 2
             self._P = t.exp(1j * ph) * self.spec_mask[None, :]
             self._phase_dz = dz
         return self._P
@@ -107,7 +112,11 @@ class FP64GPU:
         araw = photo + (self.pp * rho if self.on_abs else 0.0)
         alpha = t.clamp(t.nan_to_num(araw, nan=0.0, posinf=0.0, neginf=0.0), min=0.0)
         coeff = complex((1.0 if self.on_abs else 0.0), (self.w0tc if self.on_def else 0.0))
-        rhs = 1j * self.kp * a2 * u - photo * u - self.pp * coeff * rho * u + alpha * u
+        X = 1j * self.kp * a2 * u - photo * u - self.pp * coeff * rho * u
+        if self.stf:
+            # operators.py:141-144: the nonlinear polarisation through U^-1 (T-hat = 1)
+            X = t.fft.ifft(t.fft.fft(X, dim=1) * self.inv_U_nl[None, :], dim=1)
+        rhs = X + alpha * u
         rhs = t.where(a2 < 1e-30, t.zeros_like(rhs), rhs)
         return t.nan_to_num(rhs, nan=0.0, posinf=0.0, neginf=0.0), alpha
 

@@ -21,7 +21,7 @@ MODE_PLAIN_F32, MODE_SPLIT_BF16, MODE_SPLIT_F16 = 0, 1, 2
 EXPORTS = ("nlse_create", "nlse_half_linear", "nlse_half_linear_ex", "nlse_split", "nlse_nonlinear_step",
            "nlse_update_plasma", "nlse_rate_equation", "nlse_step", "nlse_step_batched", "nlse_propagate", "nlse_set_split_terms",
            "nlse_device_status", "nlse_debug_operator_product", "nlse_debug_wait_timeout", "nlse_scan_fallback_rows",
-           "nlse_half_linear_noalloc", "nlse_record", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
+           "nlse_half_linear_noalloc", "nlse_record", "nlse_set_gemm_variant", "nlse_get_gemm_variant", "nlse_get_row_plan", "nlse_set_row_plan", "nlse_batch_create", "nlse_batch_propagate", "nlse_batch_get_context",
            "nlse_batch_set_split_terms", "nlse_batch_set_mode", "nlse_batch_device_status", "nlse_batch_get_last_error",
            "nlse_batch_destroy",
            "nlse_profile_start", "nlse_profile_read", "nlse_kernel_name",
@@ -91,6 +91,8 @@ def load():
     lib.nlse_set_gemm_variant.argtypes = [_P, _I]
     lib.nlse_record.argtypes = [_P, _P, _P, _P, _P, _I, _P, _P]
     lib.nlse_get_gemm_variant.argtypes = [_P]
+    lib.nlse_get_row_plan.argtypes = [_I, ctypes.POINTER(_I), ctypes.POINTER(_I)]
+    lib.nlse_set_row_plan.argtypes = [_I, _I, _I]
     lib.nlse_batch_create.argtypes = [ctypes.POINTER(GridDesc), _I, ctypes.POINTER(_P)]
     lib.nlse_batch_propagate.argtypes = [_P, ctypes.POINTER(_P), ctypes.POINTER(_P), ctypes.POINTER(_P), _D, _I, _P]
     lib.nlse_batch_get_context.argtypes = [_P, _I, ctypes.POINTER(_P)]
@@ -105,6 +107,21 @@ def load():
             getattr(lib, name).restype = _I
     _lib = lib
     return lib
+
+
+def row_plans(Nt):
+    """(row_nl plan, row_next plan) picked for N_t on the current device (-1: not tuned yet)."""
+    lib = load()
+    a, b = _I(-1), _I(-1)
+    if lib.nlse_get_row_plan(int(Nt), ctypes.byref(a), ctypes.byref(b)) != NLSE_OK:
+        raise ValueError(f"Nt={Nt} is not a power of two in [16, 8192]")
+    return a.value, b.value
+
+
+def set_row_plans(Nt, nl_plan, next_plan):
+    """Pin the row plans for N_t on the current device (-1: tune again at the next context)."""
+    if load().nlse_set_row_plan(int(Nt), int(nl_plan), int(next_plan)) != NLSE_OK:
+        raise ValueError((Nt, nl_plan, next_plan))
 
 
 class NLSEError(RuntimeError):

@@ -44,17 +44,27 @@ LINEAR_MODES = ("auto", "plain", "split_bf16", "split_f16")
 
 def split_supported(cfg) -> bool:
     """Whether the tensor-core (split) forms run this Config: any N_t and up to
-    8192 radial points (the library pads N_r to a multiple of 64 inside the
-    context), but not space-time focusing, whose diffraction phase depends on
-    Omega (no single radial operator for the product)."""
-    return (cfg.N - 1) <= 8192 and not cfg.enable_space_time_focusing
+    8192 radial points (the library pads N_r inside the context).  With
+    space-time focusing the diffraction phase depends on Omega, so the half
+    step runs as the sandwich Y P(rho, Omega) Y in scaled FP16 terms."""
+    return (cfg.N - 1) <= 8192
+
+
+def batch_supported(cfg) -> bool:
+    """Whether a batch (grouped products over many pulses) takes this Config:
+    wherever the split forms run (pulses with space-time focusing get their
+    own grouped products of the sandwich Y P Y)."""
+    return split_supported(cfg)
 
 
 def resolved_linear_mode(cfg) -> str:
-    """linear_mode with "auto" resolved: split_bf16 where supported, else plain."""
+    """linear_mode with "auto" resolved: split_bf16 where supported (split_f16,
+    the arithmetic the library runs then, with space-time focusing), else plain."""
     if cfg.linear_mode != "auto":
         return cfg.linear_mode
-    return "split_bf16" if split_supported(cfg) else "plain"
+    if not split_supported(cfg):
+        return "plain"
+    return "split_f16" if cfg.enable_space_time_focusing else "split_bf16"
 
 
 @dataclass

@@ -151,6 +151,7 @@ struct TileSource {
     const CUtensorMap *tmA, *tmB;  // single product
     float *D;
     int M, N, K;
+    int kdiag;                     // single product: block-diagonal operator
     const GemmTile *tiles;         // grouped: tile table, maps, pulses
     const CUtensorMap *maps;
     const BatchPulse *P;
@@ -161,6 +162,8 @@ struct TileJob {
     const CUtensorMap *tmA, *tmB;
     float *D;
     int M, N, K, m0, n0;
+    int k0, kn;  // the K range the tile contracts: all of K, or with a block-diagonal
+                 // operator (M = K = two blocks) the range of the tile's row block
 };
 
 __device__ __forceinline__ TileJob tile_job(const TileSource &src, int t) {
@@ -176,6 +179,7 @@ __device__ __forceinline__ TileJob tile_job(const TileSource &src, int t) {
         j.K = q.K;
         j.m0 = g.m0;
         j.n0 = g.n0;
+        j.k0 = q.kdiag;  // flag, resolved below
     } else {
         const int nt = (src.N + TC_BN - 1) / TC_BN;
         j.tmA = src.tmA;
@@ -186,6 +190,13 @@ __device__ __forceinline__ TileJob tile_job(const TileSource &src, int t) {
         j.K = src.K;
         j.m0 = (t / nt) * TC_BM;
         j.n0 = (t % nt) * TC_BN;
+        j.k0 = src.kdiag;
+    }
+    if (j.k0) {
+        j.kn = j.K / 2;
+        j.k0 = j.m0 >= j.M / 2 ? j.kn : 0;
+    } else {
+        j.kn = j.K;
     }
     return j;
 }
@@ -251,7 +262,7 @@ __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntile
         int g = 0;  // stage sequence number across tiles
         for (int t = blockIdx.x; t < ntiles && !*(volatile int *)&abort_flag; t += gridDim.x) {
             const TileJob j = tile_job(src, t);
-            const int KB = j.K / TC_BK;
+            const int KB = j.kn / TC_BK;
             for (int kb = 0; kb < KB; ++kb, ++g) {
                 const int s = g % TC_STAGES;
                 const uint32_t ph = (uint32_t)(g / TC_STAGES) & 1u;
@@ -264,13 +275,13 @@ __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntile
                 mbar_expect_tx(&full_bar[s], STAGE);
 #pragma unroll
                 for (int a = 0; a < A_TERMS; ++a)
-                    tma_load_2d(st + a * A_BYTES, j.tmA, &full_bar[s], kb * TC_BK, a * j.M + j.m0);
+                    tma_load_2d(st + a * A_BYTES, j.tmA, &full_bar[s], j.k0 + kb * TC_BK, a * j.M + j.m0);
 #pragma unroll
                 for (int b = 0; b < 2; ++b)
 #pragma unroll
                     for (int c = 0; c < TC_BN / 64; ++c)
                         tma_load_2d(st + A_TERMS * A_BYTES + b * B_BYTES + c * B_BOX, j.tmB, &full_bar[s],
-                                    j.n0 + 64 * c, b * j.K + kb * TC_BK);
+                                    j.n0 + 64 * c, b * j.K + j.k0 + kb * TC_BK);
                 issued = g + 1;
             }
         }
@@ -290,7 +301,7 @@ __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntile
                 break;
             }
             tc_fence_after();
-            const int KB = src.tiles ? src.P[src.tiles[t].pulse].K / TC_BK : src.K / TC_BK;
+            const int KB = tile_job(src, t).kn / TC_BK;
             bool ok = true;
             for (int kb = 0; kb < KB; ++kb, ++g) {
                 const int s = g % TC_STAGES;
@@ -373,8 +384,8 @@ __device__ __forceinline__ void gemm_persistent(const TileSource &src, int ntile
 template <int A_TERMS, int BK, int ST, bool F16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-          float *__restrict__ D, int M, int N, int K, int *__restrict__ err) {
-    TileSource src{&tmA, &tmB, D, M, N, K, nullptr, nullptr, nullptr, 0};
+          float *__restrict__ D, int M, int N, int K, int kdiag, int *__restrict__ err) {
+    TileSource src{&tmA, &tmB, D, M, N, K, kdiag, nullptr, nullptr, nullptr, 0};
     gemm_persistent<A_TERMS, BK, ST, F16>(src, (M / TC_BM) * ((N + TC_BN - 1) / TC_BN), err);
 }
 
@@ -386,7 +397,7 @@ template <int A_TERMS, int BK, int ST, bool F16>
 __global__ void __launch_bounds__(TC_THREADS, 1)
 k_gemm_tc_grouped(const CUtensorMap *__restrict__ maps, const BatchPulse *__restrict__ P,
                   const GemmTile *__restrict__ tiles, int ntiles, int *__restrict__ err) {
-    TileSource src{nullptr, nullptr, nullptr, 0, 0, 0, tiles, maps, P, BK == 32 ? 2 : 0};
+    TileSource src{nullptr, nullptr, nullptr, 0, 0, 0, 0, tiles, maps, P, BK == 32 ? 2 : 0};
     gemm_persistent<A_TERMS, BK, ST, F16>(src, ntiles, err);
 }
 
@@ -417,9 +428,11 @@ static size_t tc_smem_bytes(int a_terms, int bk, int stages) {
     else if (variant == 1) { constexpr int AT = AT_, BK = 32, ST = 4; constexpr bool F16 = F16_; __VA_ARGS__; } \
     else if (variant == 2) { constexpr int AT = AT_, BK = 32, ST = 3; constexpr bool F16 = F16_; __VA_ARGS__; } \
     else { constexpr int AT = AT_, BK = 32, ST = 2; constexpr bool F16 = F16_; __VA_ARGS__; }
-// BF16: 3 or 2 operator terms; FP16: always 2 operator terms (3 MMAs)
+// BF16: 3 or 2 operator terms; FP16: 2 operator terms (3 MMAs), or 3 (4 MMAs: the
+// space-time-focusing operator Y, whose rounding is applied twice per half step)
 #define TC_DISPATCH(a_terms, f16, variant, ...)                                                  \
-    if (f16) { TC_DISPATCH_AT(2, true, variant, __VA_ARGS__) }                                   \
+    if (f16 && a_terms == 3) { TC_DISPATCH_AT(3, true, variant, __VA_ARGS__) }                   \
+    else if (f16) { TC_DISPATCH_AT(2, true, variant, __VA_ARGS__) }                              \
     else if (a_terms == 3) { TC_DISPATCH_AT(3, false, variant, __VA_ARGS__) }                    \
     else { TC_DISPATCH_AT(2, false, variant, __VA_ARGS__) }
 
@@ -437,15 +450,16 @@ cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P,
 }
 
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
-                           int a_terms, int variant, int f16, int *err, cudaStream_t stream) {
-    if (M % TC_BM || N % 16 || K % 64) return cudaErrorInvalidValue;
+                           int a_terms, int variant, int f16, int kdiag, int *err, cudaStream_t stream) {
+    if (M % TC_BM || N % 16 || K % 64 || (kdiag && (M != K || (K / 2) % 64 || (M / 2) % TC_BM)))
+        return cudaErrorInvalidValue;
     const int grid = tc_grid((M / TC_BM) * ((N + TC_BN - 1) / TC_BN));
     TC_DISPATCH(a_terms, f16, variant, {
         const size_t smem = tc_smem_bytes(AT, BK, ST);
         cudaError_t e = cudaFuncSetAttribute(k_gemm_tc<AT, BK, ST, F16>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                              (int)smem);
         if (e != cudaSuccess) return e;
-        k_gemm_tc<AT, BK, ST, F16><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, err);
+        k_gemm_tc<AT, BK, ST, F16><<<grid, TC_THREADS, smem, stream>>>(*tmA, *tmB, D, M, N, K, kdiag, err);
     })
     return cudaGetLastError();
 }

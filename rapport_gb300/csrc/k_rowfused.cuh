@@ -68,6 +68,16 @@ __device__ __forceinline__ float block_max(float v) {
     return v;
 }
 
+// Factor that removes the product's scaling: 1 in the split-BF16 form, else
+// 2^-(sa + sb_g) (merged operator: field exponent of input g) or 2^-(sa + sv_g)
+// (space-time focusing: exponent of the second product's input).  Either way
+// the product is E w and the row kernel adds the identity part w exactly.
+__device__ __forceinline__ float product_scale(const RowFusedArgs &a, int g_in) {
+    if (!a.f16) return 1.0f;
+    const int e = __ldcg(&a.scale[(a.stf ? NLSE_SC_VB : NLSE_SC_SB) + g_in % 2]);
+    return ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) + e));
+}
+
 // FP32 planar rows + the 16-bit hi/lo terms (the GEMM's B operand) of one
 // complex row held in smem (padded indexing); two points per thread per
 // iteration.  BF16 form: hi = bf16(w), lo = bf16(w - hi).  Split-FP16 form:
@@ -128,9 +138,7 @@ __device__ __forceinline__ void store_state_row(const float2 *s, int r, const Ro
 template <int NT>
 __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs &a, const float *F32,
                                             const float *D, float scale, int g_in) {
-    const float ds = a.f16 ? ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) +
-                                            __ldcg(&a.scale[NLSE_SC_SB + g_in % 2])))
-                           : 1.0f;
+    const float ds = product_scale(a, g_in);
     const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nrp + r) * NT;
     const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nrp + r) * NT;
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
@@ -207,17 +215,15 @@ __host__ __device__ constexpr bool row_regs() {
     return fft_regs_ok<NT, row_threads<NT>()>() && NT / row_threads<NT>() == 8;
 }
 
-template <int NT>
-__device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / row_threads<NT>()], int r, const RowFusedArgs &a,
+template <int NT, int T>
+__device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / T], int r, const RowFusedArgs &a,
                                              const float *F32, const float *D, float scale, int g_in) {
-    const float ds = a.f16 ? ldexpf(1.0f, -(__ldcg(&a.scale[NLSE_SC_SA]) +
-                                            __ldcg(&a.scale[NLSE_SC_SB + g_in % 2])))
-                           : 1.0f;
+    const float ds = product_scale(a, g_in);
     const float *fr = F32 + (size_t)r * NT, *fi = F32 + ((size_t)a.Nrp + r) * NT;
     const float *dr = D + (size_t)r * NT, *di = D + ((size_t)a.Nrp + r) * NT;
 #pragma unroll
-    for (int m = 0; m < NT / row_threads<NT>(); ++m) {
-        const int t = (int)threadIdx.x + m * row_threads<NT>();
+    for (int m = 0; m < NT / T; ++m) {
+        const int t = (int)threadIdx.x + m * T;
         const float2 x = make_float2(fmaf(dr[t], ds, fr[t]), fmaf(di[t], ds, fi[t]));
         const float2 pt = __ldg(a.Pt + t);
 #if NLSE_COMP_TWIDDLE
@@ -228,8 +234,8 @@ __device__ __forceinline__ void load_mw_regs(float2 (&v)[NT / row_threads<NT>()]
     }
 }
 
-template <int NT>
-__device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / row_threads<NT>()], int r,
+template <int NT, int T>
+__device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / T], int r,
                                                  const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, int g_out) {
     const size_t rows = 2 * (size_t)a.Nrp;
     float *re = F32 + (size_t)r * NT, *im = F32 + ((size_t)a.Nrp + r) * NT;
@@ -237,8 +243,8 @@ __device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / row_thre
     __nv_bfloat16 *lre = hre + rows * NT, *lim = him + rows * NT;
     if (!a.f16) {
 #pragma unroll
-        for (int m = 0; m < NT / row_threads<NT>(); ++m) {
-            const int t = (int)threadIdx.x + m * row_threads<NT>();
+        for (int m = 0; m < NT / T; ++m) {
+            const int t = (int)threadIdx.x + m * T;
             re[t] = v[m].x;
             im[t] = v[m].y;
             const __nv_bfloat16 hx = __float2bfloat16_rn(v[m].x), hy = __float2bfloat16_rn(v[m].y);
@@ -255,8 +261,8 @@ __device__ __forceinline__ void store_state_regs(const float2 (&v)[NT / row_thre
     const float sc = ldexpf(1.0f, sb);
     float mx = 0.0f;
 #pragma unroll
-    for (int m = 0; m < NT / row_threads<NT>(); ++m) {
-        const int t = (int)threadIdx.x + m * row_threads<NT>();
+    for (int m = 0; m < NT / T; ++m) {
+        const int t = (int)threadIdx.x + m * T;
         re[t] = v[m].x;
         im[t] = v[m].y;
         mx = fmaxf(mx, fmaxf(fabsf(v[m].x), fabsf(v[m].y)));
@@ -285,11 +291,12 @@ __device__ __forceinline__ void row_next_regs(const RowFusedArgs &a, int r, floa
                                               __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
                                               float *__restrict__ rho, float2 *__restrict__ u_out, int write_state,
                                               int do_scan, int apply_mask, int g) {
+    constexpr int T = row_threads<NT>();
     extern __shared__ float2 sm2[];
     float2 *A = sm2, *B = sm2 + fft_slots(NT);
-    float2 v[NT / row_threads<NT>()];
-    load_mw_regs<NT>(v, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f, g);
-    if (write_state) store_state_regs<NT>(v, r, a, F32, Fb, g + 1);
+    float2 v[NT / T];
+    load_mw_regs<NT, T>(v, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f, g);
+    if (write_state) store_state_regs<NT, T>(v, r, a, F32, Fb, g + 1);
     if (!do_scan && !u_out) return;
     float2 *F = fft_regs<NT, true, row_threads<NT>()>(v, A, B, a.tw);
     const float inv = 1.0f / (float)NT;
@@ -321,6 +328,57 @@ __host__ __device__ constexpr int row_min_blocks(bool with_march) {
     return by_smem < cap ? by_smem : cap;
 }
 
+// ------------------------------------------------ row plans (autotuned per N_t)
+// Each of row_nl / row_next has two or three plans of the same transforms and
+// point arithmetic (results agree bit for bit; the choice is pure speed):
+//   row_nl   plan 0: shared-memory body, row_threads_nl threads (two points per
+//                    thread per access), compile-time FFT passes;
+//            plan 1: register-resident body, N_t / 8 threads (from N_t = 512);
+//            plan 2: plan 0 with the compact FFT (one run-time pass body for
+//                    both transforms: a fraction of the instruction footprint).
+//   row_next plan 0: register-resident from N_t = 2048, else shared memory;
+//            plan 1: the shared-memory body at the same thread count (N_t >= 2048).
+// The thread count of row_next (its carrier march is chunked per thread) is
+// the same in both plans.
+template <int NT>
+__host__ __device__ constexpr bool nl_plan1_ok() {
+    return NT >= 512 && fft_regs_ok<NT, NT / 8>();
+}
+
+template <int NT>
+__host__ __device__ constexpr bool next_plan1_ok() {
+    return row_regs<NT>();
+}
+
+template <int NT, int PLAN>
+__host__ __device__ constexpr bool nl_plan_ok() {
+    return PLAN == 0 || PLAN == 2 || (PLAN == 1 && nl_plan1_ok<NT>());
+}
+
+template <int NT, int PLAN>
+__host__ __device__ constexpr int nl_threads() {
+    return (PLAN == 1 && nl_plan1_ok<NT>()) ? NT / 8 : row_threads_nl<NT>();
+}
+
+// CTAs per SM a kernel of T threads and the given dynamic shared memory is
+// compiled for: what the shared memory and the 2048 threads per SM admit, at
+// no fewer than 48 registers a thread (64 from 512 threads on).
+template <int T>
+__host__ __device__ constexpr int row_min_blocks_t(size_t smem) {
+    const int by_smem = (228 * 1024) / (int)(smem + 1024);
+    const int by_regs = 65536 / (T * (T >= 512 ? 64 : 48));
+    const int by_thr = 2048 / T;
+    const int m = by_smem < by_regs ? by_smem : by_regs;
+    const int n = m < by_thr ? m : by_thr;
+    return n > 1 ? n : 1;
+}
+
+template <int NT, int PLAN>
+__host__ __device__ constexpr int nl_min_blocks() {
+    return PLAN == 1 && nl_plan1_ok<NT>() ? row_min_blocks_t<nl_threads<NT, PLAN>()>(row_smem_bytes<NT>(false))
+                                          : row_min_blocks<NT>(false);
+}
+
 // Entry: physical u (interleaved) -> w = F[u] (state); optionally rho = march(|u|^2).
 template <int NT>
 __device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, const float2 *__restrict__ u,
@@ -346,18 +404,53 @@ __device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, con
     march_row<NT>(O, R, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), 1.0f, r, a, rho);
 }
 
-// First half step's spectral end + the nonlinear block + forward FFT.
+// row_nl plan 1: the row held in registers, 8 points per thread (N_t / 8
+// threads): the inverse FFT ends and the forward FFT starts in registers, so
+// the nonlinear block acts on the thread's own points and the row crosses
+// shared memory only between FFT passes.
 template <int NT>
+__device__ __forceinline__ void row_nl_regs_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
+                                                 __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
+                                                 const float *__restrict__ rho, int g) {
+    constexpr int T = NT / 8, P = 8;
+    extern __shared__ float2 sm2[];
+    float2 *A = sm2, *B = sm2 + fft_slots(NT);
+    float2 v[P];
+    load_mw_regs<NT, T>(v, r, a, F32, D, 1.0f / (float)NT, g);
+    float2 *F = fft_regs<NT, true, T>(v, A, B, a.tw);
+    const float *gr = rho + (size_t)r * NT;
+    const float *gs = a.rho_s ? a.rho_s + (size_t)r * NT : nullptr;
+#pragma unroll 1
+    for (int m = 0; m < P; ++m) {
+        const int t = (int)threadIdx.x + m * T;
+        v[m] = nl_point(v[m], gr[t], gs ? gs[t] : 0.0f, a.dz, a.nl, a.pchip);
+    }
+    // F was last read before the inverse transform's final barrier: the
+    // forward transform's first pass may write it at once
+    fft_regs<NT, false, T>(v, F, F == A ? B : A, a.tw);
+    store_state_regs<NT, T>(v, r, a, F32, Fb, g + 1);
+}
+
+// First half step's spectral end + the nonlinear block + forward FFT.
+template <int NT, int PLAN = 0>
 __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
                                             __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
                                             const float *__restrict__ rho, int g) {
+    if constexpr (PLAN == 1 && nl_plan1_ok<NT>()) {
+        row_nl_regs_body<NT>(a, r, F32, Fb, D, rho, g);
+        return;
+    }
     extern __shared__ float2 sm2[];
     float2 *b0 = sm2, *b1 = sm2 + fft_slots(NT);
     load_mw_row<NT>(b0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
-    float2 *R = fft_row<NT, true, row_threads_nl<NT>()>(b0, b1, a.tw);
+    float2 *R = PLAN == 2 ? fft_row_s<NT, row_threads_nl<NT>()>(b0, b1, a.tw, true)
+                          : fft_row<NT, true, row_threads_nl<NT>()>(b0, b1, a.tw);
     const float *gr = rho + (size_t)r * NT;
     const float *gs = a.rho_s ? a.rho_s + (size_t)r * NT : nullptr;
+    // kept rolled: the RK4 block is long, and unrolled copies of it (with the
+    // two transforms around it) overflow the instruction cache
+#pragma unroll 1
     for (int t = 2 * threadIdx.x; t < NT; t += 2 * blockDim.x) {
         const float2 rr = *reinterpret_cast<const float2 *>(gr + t);
         const float2 rs = gs ? *reinterpret_cast<const float2 *>(gs + t) : make_float2(0.0f, 0.0f);
@@ -365,18 +458,19 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
         R[pidx(t + 1)] = nl_point(R[pidx(t + 1)], rr.y, rs.y, a.dz, a.nl, a.pchip);
     }
     __syncthreads();
-    float2 *Y = fft_row<NT, false, row_threads_nl<NT>()>(R, R == b0 ? b1 : b0, a.tw);
+    float2 *Y = PLAN == 2 ? fft_row_s<NT, row_threads_nl<NT>()>(R, R == b0 ? b1 : b0, a.tw, false)
+                          : fft_row<NT, false, row_threads_nl<NT>()>(R, R == b0 ? b1 : b0, a.tw);
     store_state_row<NT>(Y, r, a, F32, Fb, g + 1);
 }
 
 // Second half step's spectral end + mask_r: the next state w', and optionally
 // the physical field (u_out) and the next carrier march (rho).
-template <int NT>
+template <int NT, int PLAN = 0>
 __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
                                               __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
                                               float *__restrict__ rho, float2 *__restrict__ u_out, int write_state,
                                               int do_scan, int apply_mask, int g) {
-    if constexpr (row_regs<NT>()) {
+    if constexpr (PLAN == 0 && row_regs<NT>()) {
         row_next_regs<NT>(a, r, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
         return;
     }
@@ -434,18 +528,18 @@ k_row_entry(RowFusedArgs a, const float2 *__restrict__ u, float *__restrict__ F3
     row_entry_body<NT>(a, blockIdx.x, u, F32, Fb, rho, do_scan);
 }
 
-template <int NT>
-__global__ void __launch_bounds__(row_threads_nl<NT>(), row_min_blocks<NT>(false))
+template <int NT, int PLAN>
+__global__ void __launch_bounds__(nl_threads<NT, PLAN>(), nl_min_blocks<NT, PLAN>())
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
          const float *__restrict__ rho, int g) {
-    row_nl_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
+    row_nl_body<NT, PLAN>(a, blockIdx.x, F32, Fb, D, rho, g);
 }
 
-template <int NT>
+template <int NT, int PLAN>
 __global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(true))
 k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
            float *__restrict__ rho, float2 *__restrict__ u_out, int write_state, int do_scan, int apply_mask, int g) {
-    row_next_body<NT>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
+    row_next_body<NT, PLAN>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
 }
 
 // The pulse's table entry staged in shared memory by the whole CTA: the body
@@ -472,23 +566,23 @@ k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, i
     row_entry_body<NT>(q.a, w.y, q.u, q.F32, q.Fb, q.rho, do_scan && !q.ste_work);
 }
 
-template <int NT>
-__global__ void __launch_bounds__(row_threads_nl<NT>(), row_min_blocks<NT>(false))
+template <int NT, int PLAN>
+__global__ void __launch_bounds__(nl_threads<NT, PLAN>(), nl_min_blocks<NT, PLAN>())
 k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = stage_pulse(P, w.x);
-    row_nl_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, g);
+    row_nl_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, g);
 }
 
-template <int NT>
+template <int NT, int PLAN>
 __global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(true))
 k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = stage_pulse(P, w.x);
     if (q.ste_work)  // exciton channel: hand the physical field to the two-population march
-        row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : q.ste_work, !last, 0, 1, g);
+        row_next_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : q.ste_work, !last, 0, 1, g);
     else
-        row_next_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1, g);
+        row_next_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1, g);
 }
 
 // Pulses with the full-physics terms (Raman / self-steepening; one time-grid class).
@@ -514,14 +608,37 @@ struct RowKernels {
     static cudaError_t entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
                              int do_scan, cudaStream_t st);
     static cudaError_t nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,
-                          int g, cudaStream_t st);
+                          int g, int plan, cudaStream_t st);
     static cudaError_t next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, float *rho,
-                            float2 *u_out, int write_state, int do_scan, int apply_mask, int g, cudaStream_t st);
+                            float2 *u_out, int write_state, int do_scan, int apply_mask, int g, int plan,
+                            cudaStream_t st);
     static cudaError_t nl_full(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
                                const float *rho, int g, cudaStream_t st);
     static cudaError_t batch(int kind, const BatchPulse *P, const int2 *work, int nblocks, int flag, int g,
-                             cudaStream_t st);
+                             int plan, cudaStream_t st);
 };
+
+template <int NT, int PLAN>
+static cudaError_t launch_nl_plan(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
+                                  const float *rho, int g, cudaStream_t st) {
+    const size_t smem = row_smem_bytes<NT>(false);
+    cudaError_t e = set_smem(k_row_nl<NT, PLAN>, smem);
+    if (e != cudaSuccess) return e;
+    k_row_nl<NT, PLAN><<<a.Nr, nl_threads<NT, PLAN>(), smem, st>>>(a, F32, Fb, D, rho, g);
+    return cudaGetLastError();
+}
+
+template <int NT, int PLAN>
+static cudaError_t launch_next_plan(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
+                                    float *rho, float2 *u_out, int write_state, int do_scan, int apply_mask, int g,
+                                    cudaStream_t st) {
+    const size_t smem = row_smem_bytes<NT>(true);
+    cudaError_t e = set_smem(k_row_next<NT, PLAN>, smem);
+    if (e != cudaSuccess) return e;
+    k_row_next<NT, PLAN><<<a.Nr, row_threads<NT>(), smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan,
+                                                                apply_mask, g);
+    return cudaGetLastError();
+}
 
 template <int NT>
 cudaError_t RowKernels<NT>::entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
@@ -535,24 +652,19 @@ cudaError_t RowKernels<NT>::entry(const RowFusedArgs &a, const float2 *u, float 
 
 template <int NT>
 cudaError_t RowKernels<NT>::nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
-                               const float *rho, int g, cudaStream_t st) {
-    const size_t smem = row_smem_bytes<NT>(false);
-    cudaError_t e = set_smem(k_row_nl<NT>, smem);
-    if (e != cudaSuccess) return e;
-    k_row_nl<NT><<<a.Nr, row_threads_nl<NT>(), smem, st>>>(a, F32, Fb, D, rho, g);
-    return cudaGetLastError();
+                               const float *rho, int g, int plan, cudaStream_t st) {
+    if (plan == 1 && nl_plan1_ok<NT>()) return launch_nl_plan<NT, 1>(a, F32, Fb, D, rho, g, st);
+    if (plan == 2) return launch_nl_plan<NT, 2>(a, F32, Fb, D, rho, g, st);
+    return launch_nl_plan<NT, 0>(a, F32, Fb, D, rho, g, st);
 }
 
 template <int NT>
 cudaError_t RowKernels<NT>::next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, float *rho,
-                                 float2 *u_out, int write_state, int do_scan, int apply_mask, int g,
+                                 float2 *u_out, int write_state, int do_scan, int apply_mask, int g, int plan,
                                  cudaStream_t st) {
-    const size_t smem = row_smem_bytes<NT>(true);
-    cudaError_t e = set_smem(k_row_next<NT>, smem);
-    if (e != cudaSuccess) return e;
-    k_row_next<NT><<<a.Nr, row_threads<NT>(), smem, st>>>(a, F32, Fb, D, rho, u_out, write_state, do_scan,
-                                                          apply_mask, g);
-    return cudaGetLastError();
+    if (plan == 1 && next_plan1_ok<NT>())
+        return launch_next_plan<NT, 1>(a, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g, st);
+    return launch_next_plan<NT, 0>(a, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g, st);
 }
 
 // The full-physics row kernel exists for N_t <= 4096 (three row buffers).
@@ -572,7 +684,7 @@ cudaError_t RowKernels<NT>::nl_full(const RowFusedArgs &a, float *F32, __nv_bflo
 
 template <int NT>
 cudaError_t RowKernels<NT>::batch(int kind, const BatchPulse *P, const int2 *work, int nblocks, int flag, int g,
-                                  cudaStream_t st) {
+                                  int plan, cudaStream_t st) {
     cudaError_t e;
     if (kind == 3) {
         if constexpr (NT > 4096) {
@@ -591,13 +703,29 @@ cudaError_t RowKernels<NT>::batch(int kind, const BatchPulse *P, const int2 *wor
         if (e != cudaSuccess) return e;
         k_row_entry_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag);
     } else if (kind == 1) {
-        e = set_smem(k_row_nl_b<NT>, smem);
-        if (e != cudaSuccess) return e;
-        k_row_nl_b<NT><<<nblocks, row_threads_nl<NT>(), smem, st>>>(P, work, g);
+        if (plan == 1 && nl_plan1_ok<NT>()) {
+            e = set_smem(k_row_nl_b<NT, 1>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_nl_b<NT, 1><<<nblocks, nl_threads<NT, 1>(), smem, st>>>(P, work, g);
+        } else if (plan == 2) {
+            e = set_smem(k_row_nl_b<NT, 2>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_nl_b<NT, 2><<<nblocks, nl_threads<NT, 2>(), smem, st>>>(P, work, g);
+        } else {
+            e = set_smem(k_row_nl_b<NT, 0>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_nl_b<NT, 0><<<nblocks, nl_threads<NT, 0>(), smem, st>>>(P, work, g);
+        }
     } else {
-        e = set_smem(k_row_next_b<NT>, smem);
-        if (e != cudaSuccess) return e;
-        k_row_next_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag, g);
+        if (plan == 1 && next_plan1_ok<NT>()) {
+            e = set_smem(k_row_next_b<NT, 1>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_next_b<NT, 1><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag, g);
+        } else {
+            e = set_smem(k_row_next_b<NT, 0>, smem);
+            if (e != cudaSuccess) return e;
+            k_row_next_b<NT, 0><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag, g);
+        }
     }
     return cudaGetLastError();
 }

@@ -60,7 +60,8 @@ static void free_ctx(nlse_ctx *c) {
     prof_free(c);
     void *ptrs[] = {c->d_tw,    c->d_Y,   c->d_Y64, c->d_rho_modes, c->d_delta_k, c->d_spec_mask,
                     c->d_mask_r, c->d_pchip, c->d_lut_dt, c->d_lut_s_dt, c->d_Rf, c->d_Tss, c->d_invUnl, c->d_invUop, c->d_P2, c->d_Pt,   c->d_Pr,     c->d_work,
-                    c->d_flag,  c->d_scale, c->d_Er,  c->d_Ei,  c->d_A,  c->d_F32, c->d_Fb,  c->d_D,   c->d_Ptf};
+                    c->d_flag,  c->d_scale, c->d_Er,  c->d_Ei,  c->d_A,  c->d_F32, c->d_Fb,  c->d_D,   c->d_Ptf,
+                    c->d_P2s};
     for (void *p : ptrs)
         if (p) cudaFree(p);
     free(c);
@@ -343,8 +344,11 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     // column: its loads read zeros past N_t and its stores stop at N_t.
     c->a_terms = 3;
     c->cached_dz_op = NAN;
-    c->Nrp = (Nr + 63) / 64 * 64;
+    c->stf = (d->flags & NLSE_F_SPACE_TIME) != 0;
+    // the space-time-focusing product is block-diagonal: each block must be whole 128-row tiles
+    c->Nrp = c->stf ? (Nr + 127) / 128 * 128 : (Nr + 63) / 64 * 64;
     c->split_ok = c->Nrp <= 8192;
+    c->stf = c->stf && c->split_ok;
     if (c->split_ok) {
         const size_t K2 = 2 * (size_t)c->Nrp;
         NLSE_TRY(dev_upload(err, &c->d_Y64, d->Y, (size_t)Nr * Nr));
@@ -355,6 +359,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
         NLSE_TRY(dev_upload<__nv_bfloat16>(err, &c->d_Fb, nullptr, 2 * K2 * Nt));
         NLSE_TRY(dev_upload<float>(err, &c->d_D, nullptr, K2 * Nt));
         NLSE_TRY(dev_upload<float2>(err, &c->d_Ptf, nullptr, 2 * (size_t)Nt));
+        if (c->stf) NLSE_TRY(dev_upload<float4>(err, &c->d_P2s, nullptr, (size_t)Nr * Nt));
         {
             cudaError_t ze = cudaMemset(c->d_F32, 0, K2 * Nt * sizeof(float));
             if (ze == cudaSuccess) ze = cudaMemset(c->d_Fb, 0, 2 * K2 * Nt * sizeof(__nv_bfloat16));
@@ -432,6 +437,29 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     }
     ce = cudaMemset(c->d_flag, 0, 4 * sizeof(int));
     if (ce == cudaSuccess) ce = cudaMemset(c->d_scale, 0, NLSE_SC_N * sizeof(int));
+    // space-time focusing in the split forms: diag(Y, Y) in 3 scaled FP16 terms
+    // (dz-independent, built once) and the bound cY of |Y w| / max |w|
+    if (ce == cudaSuccess && c->stf) {
+        double ymax = 0.0, rmax = 0.0;
+        for (int i = 0; i < Nr; ++i) {
+            double rs = 0.0;
+            for (int k = 0; k < Nr; ++k) {
+                const double y = fabs(d->Y[(size_t)i * Nr + k]);
+                rs += y;
+                ymax = y > ymax ? y : ymax;
+            }
+            rmax = rs > rmax ? rs : rmax;
+        }
+        int e = 0;
+        if (ymax > 0) frexp(ymax, &e);
+        c->cY = (float)rmax;
+        ce = launch_split_Yb16(c->d_Y64, Nr, c->Nrp, 14 - e, reinterpret_cast<__half *>(c->d_A), c->d_scale, 0);
+        c->op_f16 = 1;
+    }
+    // the row kernels' plans for this N_t: timed once per device (synthetic rows)
+    if (ce == cudaSuccess && c->split_ok)
+        ce = row_plan_tune(c->logNt, Nr, c->d_tw, c->d_lut_dt, c->d_pchip, c->d_mask_r, c->nl, c->sc, c->d_Ptf,
+                           c->d_scale);
     if (ce == cudaSuccess) ce = cudaDeviceSynchronize();
     if (ce != cudaSuccess) {
         nlse_set_error(err, NLSE_ERR_CUDA, "context init: %s", cudaGetErrorString(ce));
@@ -509,6 +537,9 @@ static int ensure_tables(nlse_ctx *c, double dz, cudaStream_t st) {
     PROF(K_PHASE_TABLES);
     int s = launched(c, launch_phase_tables(c, dz, st), "phase tables");
     if (s == NLSE_OK && c->d_P2) s = launched(c, launch_phase_table_2d(c, dz, st), "2-d phase table");
+    if (s == NLSE_OK && c->d_P2s)
+        s = launched(c, launch_stf_table(c->d_rho_modes, c->d_invUop, c->Nr, c->Nt, dz, c->komega, c->d_P2s, st),
+                     "space-time phase table");
     if (s == NLSE_OK) c->cached_dz = dz;
     return s;
 }
@@ -540,12 +571,14 @@ static int split_ready(nlse_ctx *c, double dz, int f16, cudaStream_t st) {
     if (!c->split_ok)
         return bad(c, NLSE_ERR_UNSUPPORTED,
                    "the split (tensor-core) forms take Nr <= 8192 (this grid: use the plain mode)");
-    if (c->d_P2)
-        return bad(c, NLSE_ERR_UNSUPPORTED,
-                   "space-time focusing makes the diffraction phase depend on Omega, so the half step has no "
-                   "single radial operator for the split-BF16 product: use the plain mode");
     int s = ensure_tables(c, dz, st);
     if (s) return s;
+    if (c->stf) {
+        // space-time focusing: the sandwich Y P(rho, Omega) Y, in FP16 terms whatever the split mode
+        // (the operator diag(Y, Y) was built at creation; P(rho, Omega) per dz in ensure_tables)
+        (void)f16;
+        return autotune_gemm(c, st);
+    }
     if (dz == c->cached_dz_op && f16 == c->op_f16) return NLSE_OK;
     {
         PROF(K_BUILD_OP);
@@ -580,18 +613,41 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
     a.ft = FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf};
     a.f16 = c->op_f16;
     a.scale = c->d_scale;
+    a.stf = c->stf;
     return a;
 }
+
+#define NLSE_SEQ_(x)             \
+    do {                         \
+        int s_ = (x);            \
+        if (s_) return s_;       \
+    } while (0)
 
 static cudaError_t tc_gemm_raw(nlse_ctx *c, int variant, cudaStream_t st) {
     const int K2 = 2 * c->Nrp;
     const CUtensorMap *a = variant ? &c->tmA32 : &c->tmA, *b = variant ? &c->tmB32 : &c->tmB;
-    return launch_gemm_tc(a, b, c->d_D, K2, c->Nt, K2, c->a_terms, variant, c->op_f16, c->d_flag, st);
+    // operator terms: 3 FP16 (space-time focusing: Y), 2 FP16 (merged E, split-FP16), or a_terms BF16
+    const int terms = c->stf ? 3 : (c->op_f16 ? 2 : c->a_terms);
+    return launch_gemm_tc(a, b, c->d_D, K2, c->Nt, K2, terms, variant, c->op_f16, c->stf, c->d_flag, st);
 }
 
 static int tc_gemm(nlse_ctx *c, cudaStream_t st) {
     PROF(K_GEMM_TC);
     return launched(c, tc_gemm_raw(c, c->gemm_variant, st), "tcgen05 gemm");
+}
+
+// The linear half step's product on GEMM input g: E'w (merged operator), or with
+// space-time focusing Y P Y w -- product, phase pass, product.
+static int linear_product(nlse_ctx *c, int g, cudaStream_t st) {
+    NLSE_SEQ_(tc_gemm(c, st));
+    if (!c->stf) return NLSE_OK;
+    {
+        PROF(K_STF_PHASE);
+        NLSE_SEQ_(launched(c, launch_stf_phase(c->d_D, c->d_P2s, c->d_Fb, c->Nr, c->Nrp, c->Nt, c->cY, g, c->d_scale,
+                                               st),
+                           "space-time phase"));
+    }
+    return tc_gemm(c, st);
 }
 
 // Pipeline autotuner: time each (k depth, stages) variant of the tensor-core
@@ -651,13 +707,15 @@ static int row_nl(nlse_ctx *c, const RowFusedArgs &a, const float *rho, int g, c
     PROF(K_ROW_NL);
     if (c->full_nl)
         return launched(c, launch_row_nl_full(a, c->d_F32, c->d_Fb, c->d_D, rho, g, st), "row nonlinear");
-    return launched(c, launch_row_nl(a, c->d_F32, c->d_Fb, c->d_D, rho, g, st), "row nonlinear");
+    return launched(c, launch_row_nl(a, c->d_F32, c->d_Fb, c->d_D, rho, g, row_plan(c->logNt, 0), st),
+                    "row nonlinear");
 }
 
 static int row_next(nlse_ctx *c, const RowFusedArgs &a, float *rho, float2 *u_out, int write_state, int scan,
                     int mask, int g, cudaStream_t st) {
     PROF(K_ROW_NEXT);
-    return launched(c, launch_row_next(a, c->d_F32, c->d_Fb, c->d_D, rho, u_out, write_state, scan, mask, g, st),
+    return launched(c, launch_row_next(a, c->d_F32, c->d_Fb, c->d_D, rho, u_out, write_state, scan, mask, g,
+                                       row_plan(c->logNt, 1), st),
                     "row next");
 }
 
@@ -669,7 +727,7 @@ static int half_linear_split(nlse_ctx *c, float2 *u, double dz, int f16, cudaStr
     NLSE_SEQ(split_ready(c, dz, f16, st));
     RowFusedArgs a = row_args(c, dz);
     NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
-    NLSE_SEQ(tc_gemm(c, st));
+    NLSE_SEQ(linear_product(c, 0, st));
     return row_next(c, a, nullptr, u, 0, 0, 0, 0, st);
 }
 
@@ -679,9 +737,9 @@ static int step_split(nlse_ctx *c, float2 *u, const float *rho, const float *rho
     RowFusedArgs a = row_args(c, dz);
     a.rho_s = c->sc.ste ? rho_s : nullptr;
     NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
-    NLSE_SEQ(tc_gemm(c, st));
+    NLSE_SEQ(linear_product(c, 0, st));
     NLSE_SEQ(row_nl(c, a, rho, 0, st));
-    NLSE_SEQ(tc_gemm(c, st));
+    NLSE_SEQ(linear_product(c, 1, st));
     return row_next(c, a, nullptr, u, 0, 0, 1, 1, st);
 }
 
@@ -701,9 +759,9 @@ static int propagate_split_ste(nlse_ctx *c, float2 *u, float *rho, float *rho_s,
     NLSE_SEQ(row_entry(c, a, u, nullptr, 0, st));
     for (int i = 0; i < n; ++i) {
         const bool last = i == n - 1;
-        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(linear_product(c, 2 * i, st));
         NLSE_SEQ(row_nl(c, a, rho, 2 * i, st));
-        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(linear_product(c, 2 * i + 1, st));
         NLSE_SEQ(row_next(c, a, nullptr, last ? u : c->d_work, last ? 0 : 1, 0, 1, 2 * i + 1, st));
         if (!last) NLSE_SEQ(rate_scan(c, c->d_work, rho, rho_s, st));
     }
@@ -721,9 +779,9 @@ static int propagate_split(nlse_ctx *c, float2 *u, float *rho, float *rho_s, dou
     NLSE_SEQ(row_entry(c, a, u, rho, 1, st));
     for (int i = 0; i < n; ++i) {
         const bool last = i == n - 1;
-        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(linear_product(c, 2 * i, st));
         NLSE_SEQ(row_nl(c, a, rho, 2 * i, st));
-        NLSE_SEQ(tc_gemm(c, st));
+        NLSE_SEQ(linear_product(c, 2 * i + 1, st));
         NLSE_SEQ(row_next(c, a, rho, last ? u : nullptr, last ? 0 : 1, last ? 0 : 1, 1, 2 * i + 1, st));
     }
     return NLSE_OK;
@@ -859,6 +917,10 @@ extern "C" int nlse_debug_operator_product(nlse_ctx *c, const float *w, float *o
     if (!c) return NLSE_ERR_INVALID_ARG;
     if (!field_ok(c, w, "w") || !field_ok(c, out, "out")) return NLSE_ERR_INVALID_ARG;
     cudaStream_t st = (cudaStream_t)stream;
+    if (c->stf)
+        return bad(c, NLSE_ERR_UNSUPPORTED,
+                   "the operator-product diagnostic shows the merged operator E'; with space-time focusing the "
+                   "half step is the sandwich Y P Y");
     NLSE_SEQ(split_ready(c, dz, 0, st));
     // w's Re / Im planes (Nr rows each) into the state's planes of Nrp rows
     const size_t plane = (size_t)c->Nr * c->Nt, pplane = (size_t)c->Nrp * c->Nt;
@@ -899,6 +961,28 @@ extern "C" int nlse_set_gemm_variant(nlse_ctx *c, int variant) {
 }
 
 extern "C" int nlse_get_gemm_variant(const nlse_ctx *c) { return c ? c->gemm_variant : -1; }
+
+static int log2_nt(int Nt) {
+    if (Nt < 16 || Nt > NLSE_MAX_NT || (Nt & (Nt - 1))) return -1;
+    int l = 0;
+    while ((1 << l) < Nt) ++l;
+    return l;
+}
+
+extern "C" int nlse_get_row_plan(int Nt, int *nl_plan, int *next_plan) {
+    const int l = log2_nt(Nt);
+    if (l < 0 || !nl_plan || !next_plan) return NLSE_ERR_INVALID_ARG;
+    *nl_plan = row_plan_get(l, 0);
+    *next_plan = row_plan_get(l, 1);
+    return NLSE_OK;
+}
+
+extern "C" int nlse_set_row_plan(int Nt, int nl_plan, int next_plan) {
+    const int l = log2_nt(Nt);
+    if (l < 0 || nl_plan < -1 || nl_plan > 2 || next_plan < -1 || next_plan > 1) return NLSE_ERR_INVALID_ARG;
+    if (row_plan_set(l, 0, nl_plan) || row_plan_set(l, 1, next_plan)) return NLSE_ERR_CUDA;
+    return NLSE_OK;
+}
 
 extern "C" int nlse_set_split_terms(nlse_ctx *c, int a_terms) {
     if (!c) return NLSE_ERR_INVALID_ARG;
@@ -989,6 +1073,7 @@ extern "C" const char *nlse_kernel_name(int kid) {
         case K_ROW_NEXT: return "k_row_next";
         case K_BUILD_OP: return "k_build_operator";
         case K_RECORD: return "k_record";
+        case K_STF_PHASE: return "k_stf_phase";
         default: return "";
     }
 }
@@ -1004,14 +1089,17 @@ struct nlse_batch {
     cudaStream_t cap_stream, cap_stream2;
     cudaEvent_t cap_fork, cap_join;
     cudaGraphExec_t graph;
-    int graph_key[4];        // (variant, a_terms, f16, buffer generation) it was captured for
+    int graph_key[5];        // (variant, a_terms, f16, buffer generation, row-plan generation) it was captured for
     int graph_off;           // capture failed once: launch directly
     nlse_ctx **ctx;          // one context per pulse (tables, operator, state buffers)
     BatchPulse *h_pulses;    // pinned staging of the per-pulse table
     BatchPulse *d_pulses;
     CUtensorMap *d_maps;     // 4 per pulse: A, B (k depth 64), A, B (k depth 32)
-    GemmTile *d_tiles;
-    int ntiles;
+    GemmTile *d_tiles;       // the tiles of the pulses without space-time focusing, then those with it
+    int ntiles;              // all tiles
+    int nmain;               // tiles of the pulses without space-time focusing (the batch's form)
+    int main_lane, stf_lane; // of those / of the rest: the tiles of lane 0's pulses
+    int *stf_idx, nstf;      // pulses with space-time focusing (products Y P Y in 3 FP16 terms)
     struct Class {
         int logNt, nblocks;
         int full;            // its pulses have the full-physics terms (row_nl kind 3)
@@ -1043,6 +1131,7 @@ static void batch_free(nlse_batch *b) {
         for (int i = 0; i < b->n; ++i) nlse_destroy(b->ctx[i]);
     free(b->ctx);
     free(b->ste_idx);
+    free(b->stf_idx);
     if (b->h_pulses) cudaFreeHost(b->h_pulses);
     void *ptrs[] = {b->d_pulses, b->d_maps, b->d_tiles, b->d_flag};
     for (void *p : ptrs)
@@ -1084,18 +1173,47 @@ static cudaError_t batch_ste_marches_on(nlse_batch *b, void *const *u, cudaStrea
     return e;
 }
 
+// The row plan of a batched row-kernel kind (1: row_nl, 2: row_next; others have one plan).
+static int batch_plan(int logNt, int kind) {
+    return kind == 1 ? row_plan(logNt, 0) : (kind == 2 ? row_plan(logNt, 1) : 0);
+}
+
+// The products of one half step for the pulses of a lane (0 or 1; -1: all) on
+// GEMM input g: one grouped launch over the pulses in the batch's form, and
+// for the pulses with space-time focusing Y P Y -- a grouped launch of their
+// block-diagonal products, the phase pass of each, a second grouped launch.
+static cudaError_t batch_products(nlse_batch *b, int g, int lane, cudaStream_t st) {
+    nlse_ctx *c = b->ctx[0];
+    const int m0 = lane == 1 ? b->main_lane : 0;
+    const int mn = lane < 0 ? b->nmain : (lane == 0 ? b->main_lane : b->nmain - b->main_lane);
+    cudaError_t e = cudaSuccess;
+    if (mn > 0)
+        e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + m0, mn, b->f16 ? 2 : b->a_terms,
+                                   c->gemm_variant, b->f16, b->d_flag, st);
+    const int nst = b->ntiles - b->nmain;
+    const int s0 = b->nmain + (lane == 1 ? b->stf_lane : 0);
+    const int sn = lane < 0 ? nst : (lane == 0 ? b->stf_lane : nst - b->stf_lane);
+    if (sn <= 0 || e != cudaSuccess) return e;
+    e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + s0, sn, 3, c->gemm_variant, 1, b->d_flag, st);
+    for (int j = 0; j < b->nstf && e == cudaSuccess; ++j) {
+        const int i = b->stf_idx[j];
+        if (lane >= 0 && (i < b->lane_pulse) != (lane == 0)) continue;
+        nlse_ctx *q = b->ctx[i];
+        e = launch_stf_phase(q->d_D, q->d_P2s, q->d_Fb, q->Nr, q->Nrp, q->Nt, q->cY, g, q->d_scale, st);
+    }
+    if (e == cudaSuccess)
+        e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + s0, sn, 3, c->gemm_variant, 1, b->d_flag,
+                                   st);
+    return e;
+}
+
 // One z-step of one lane (0 or 1; -1: all pulses) on stream st: GEMM, row_nl
 // (consumes input g), GEMM, row_next (consumes g + 1; writes input g + 2 and
 // marches the carriers unless last).
 static cudaError_t batch_zstep(nlse_batch *b, int g, int last, int lane, cudaStream_t st) {
-    nlse_ctx *c = b->ctx[0];
-    const int t0 = lane == 1 ? b->lane_tiles : 0;
-    const int nt = lane < 0 ? b->ntiles : (lane == 0 ? b->lane_tiles : b->ntiles - b->lane_tiles);
     cudaError_t e = cudaSuccess;
     for (int half = 0; half < 2 && e == cudaSuccess; ++half) {
-        if (nt > 0)
-            e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + t0, nt, b->a_terms, c->gemm_variant,
-                                       b->f16, b->d_flag, st);
+        e = batch_products(b, g + half, lane, st);
         for (int k = 0; k < b->ncls && e == cudaSuccess; ++k) {
             const int w0 = lane == 1 ? b->cls[k].split : 0;
             const int nw = lane < 0 ? b->cls[k].nblocks
@@ -1103,7 +1221,7 @@ static cudaError_t batch_zstep(nlse_batch *b, int g, int last, int lane, cudaStr
             const int kind = half == 1 ? 2 : (b->cls[k].full ? 3 : 1);
             if (nw > 0)
                 e = launch_row_batch(kind, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work + w0, nw,
-                                     half == 0 ? 0 : last, g + half, st);
+                                     half == 0 ? 0 : last, g + half, batch_plan(b->cls[k].logNt, kind), st);
         }
     }
     if (e == cudaSuccess && !last) e = batch_ste_marches(b, lane, st);
@@ -1113,7 +1231,8 @@ static cudaError_t batch_zstep(nlse_batch *b, int g, int last, int lane, cudaStr
 // The graph of three non-final z-steps for the batch's current launch
 // configuration; NULL (and direct launches from then on) if capture fails.
 static cudaGraphExec_t batch_graph(nlse_batch *b) {
-    const int key[4] = {b->ctx[0]->gemm_variant, b->a_terms, b->f16, b->nste ? b->ptr_gen : 0};
+    const int key[5] = {b->ctx[0]->gemm_variant, b->a_terms, b->f16, b->nste ? b->ptr_gen : 0,
+                        row_plan_generation()};
     if (b->graph && !memcmp(key, b->graph_key, sizeof(key))) return b->graph;
     if (b->graph_off) return nullptr;
     if (b->graph) {
@@ -1184,13 +1303,9 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         }
         if (!b->ctx[i]->split_ok)
             BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "pulse %d: batches run the split forms, which take Nr <= 8192", i);
-        if (b->ctx[i]->d_P2)
-            BATCH_FAIL(NLSE_ERR_UNSUPPORTED,
-                       "pulse %d: space-time focusing makes the diffraction phase depend on Omega (no single radial "
-                       "operator for the tensor-core product): run it on its own context in the plain mode",
-                       i);
     }
-    std::vector<GemmTile> tiles;
+    std::vector<GemmTile> tiles, stf_tiles;
+    std::vector<int> stf;
     std::vector<CUtensorMap> maps(4 * (size_t)n);
     int logs[32], fulls[32], nlog = 0;
     std::vector<std::vector<int2>> work(32);
@@ -1200,10 +1315,11 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         // pulses built from the same QDHT tables and k0 have the same operator
         // (dz is common to the batch): they read the first such pulse's copy,
         // so the grouped product streams one operator from L2 instead of many
+        // (the operator's kind too: E' of the batch's form, or diag(Y, Y) with space-time focusing)
         int owner = i;
         for (int j = 0; j < i && owner == i; ++j)
             if (descs[j].Y == descs[i].Y && descs[j].rho_modes == descs[i].rho_modes && descs[j].Nr == descs[i].Nr &&
-                descs[j].komega == descs[i].komega)
+                descs[j].komega == descs[i].komega && b->ctx[j]->stf == c->stf)
                 owner = j;
         nlse_ctx *oc = b->ctx[owner];
         memcpy(&maps[4 * i], &oc->tmA, sizeof(CUtensorMap));
@@ -1212,7 +1328,8 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         memcpy(&maps[4 * i + 3], &c->tmB32, sizeof(CUtensorMap));
         const int M = 2 * c->Nrp;
         for (int m0 = 0; m0 < M; m0 += 128)
-            for (int n0 = 0; n0 < c->Nt; n0 += 256) tiles.push_back(GemmTile{i, m0, n0, 0});
+            for (int n0 = 0; n0 < c->Nt; n0 += 256) (c->stf ? stf_tiles : tiles).push_back(GemmTile{i, m0, n0, 0});
+        if (c->stf) stf.push_back(i);
         // row classes: one per (N_t, full-physics terms)
         int k = 0;
         while (k < nlog && (logs[k] != c->logNt || fulls[k] != c->full_nl)) ++k;
@@ -1229,6 +1346,14 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         if (!b->ste_idx) BATCH_FAIL(NLSE_ERR_INVALID_ARG, "out of host memory");
         memcpy(b->ste_idx, ste.data(), ste.size() * sizeof(int));
     }
+    b->nstf = (int)stf.size();
+    if (b->nstf) {
+        b->stf_idx = (int *)malloc(stf.size() * sizeof(int));
+        if (!b->stf_idx) BATCH_FAIL(NLSE_ERR_INVALID_ARG, "out of host memory");
+        memcpy(b->stf_idx, stf.data(), stf.size() * sizeof(int));
+    }
+    b->nmain = (int)tiles.size();
+    tiles.insert(tiles.end(), stf_tiles.begin(), stf_tiles.end());
     b->ntiles = (int)tiles.size();
     // lane 0 = the first pulses up to about half of the tiles
     b->lane_pulse = 0;
@@ -1242,6 +1367,9 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         b->lane_pulse = p;
         b->lane_tiles = acc;
     }
+    b->main_lane = b->stf_lane = 0;
+    for (int t = 0; t < b->ntiles; ++t)
+        if (tiles[t].pulse < b->lane_pulse) ++(t < b->nmain ? b->main_lane : b->stf_lane);
     cudaError_t e = cudaMalloc((void **)&b->d_tiles, tiles.size() * sizeof(GemmTile));
     if (e == cudaSuccess)
         e = cudaMemcpy(b->d_tiles, tiles.data(), tiles.size() * sizeof(GemmTile), cudaMemcpyHostToDevice);
@@ -1372,6 +1500,7 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
             P.M = 2 * q->Nrp;
             P.N = q->Nt;
             P.K = 2 * q->Nrp;
+            P.kdiag = q->stf;
         }
         NLSE_CUDA_TRY(&b->err, cudaMemcpyAsync(b->d_pulses, b->h_pulses, b->n * sizeof(BatchPulse),
                                                cudaMemcpyHostToDevice, st));
@@ -1396,8 +1525,8 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
             return NLSE_ERR_CUDA;                                                      \
         }                                                                              \
     } while (0)
-    if (b->f16)
-        for (int i = 0; i < b->n; ++i)
+    for (int i = 0; i < b->n; ++i)
+        if (b->f16 || b->ctx[i]->stf)
             BSEQ(K_ROW_ENTRY,
                  launch_field_bound((const float2 *)u[i], (size_t)b->ctx[i]->Nr * b->ctx[i]->Nt, b->ctx[i]->Nt,
                                     b->ctx[i]->d_scale, st),
@@ -1406,7 +1535,7 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
     if (b->nste) BSEQ(K_RATE_SCAN, batch_ste_marches_on(b, u, st), "batch exciton march");
     for (int k = 0; k < b->ncls; ++k)
         BSEQ(K_ROW_ENTRY,
-             launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, -1, st),
+             launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, -1, 0, st),
              "batch row entry");
     int it = 0;
     // the bulk of the non-final steps as graph launches of three steps each
@@ -1418,23 +1547,18 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
     }
     for (; it < nsteps; ++it) {
         const int last = it == nsteps - 1;
-        BSEQ(K_GEMM_TC,
-             launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
-                                    b->f16, b->d_flag, st),
-             "batch gemm");
+        BSEQ(K_GEMM_TC, batch_products(b, 2 * it, -1, st), "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NL,
                  launch_row_batch(b->cls[k].full ? 3 : 1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work,
-                                  b->cls[k].nblocks, 0, 2 * it, st),
+                                  b->cls[k].nblocks, 0, 2 * it, batch_plan(b->cls[k].logNt, b->cls[k].full ? 3 : 1),
+                                  st),
                  "batch row nonlinear");
-        BSEQ(K_GEMM_TC,
-             launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->ntiles, b->a_terms, c->gemm_variant,
-                                    b->f16, b->d_flag, st),
-             "batch gemm");
+        BSEQ(K_GEMM_TC, batch_products(b, 2 * it + 1, -1, st), "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NEXT,
                  launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last,
-                                  2 * it + 1, st),
+                                  2 * it + 1, batch_plan(b->cls[k].logNt, 2), st),
                  "batch row next");
         if (!last && b->nste) BSEQ(K_RATE_SCAN, batch_ste_marches(b, -1, st), "batch exciton march");
     }

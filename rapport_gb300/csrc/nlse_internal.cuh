@@ -4,6 +4,7 @@
 #include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
+#include <cuda_fp16.h>
 #include <stdint.h>
 #include <stdio.h>
 
@@ -87,6 +88,8 @@ struct RowFusedArgs {
     FullTabs ft;          // full-physics split tables (all NULL: the measured toggles)
     int f16;              // split-FP16 form: scaled FP16 field terms (see NLSE_SC_*)
     int *scale;           // the pulse's scale cells (split-FP16 form)
+    int stf;              // space-time focusing in the split form: D holds E(Omega) w = Y (P - 1) Y w,
+                          // scaled by 2^(sa + sv) with sv in scale[NLSE_SC_VB + g % 2]
 };
 
 // Scale cells of the split-FP16 form (int each, per pulse):
@@ -101,7 +104,14 @@ struct RowFusedArgs {
 #define NLSE_SC_SA 5
 #define NLSE_SC_OVF 6
 #define NLSE_SC_EMAX 7
-#define NLSE_SC_N 8
+//   [8..9]  space-time focusing: exponent sv of the FP16 terms of P Y w (the
+//           second product's input) of GEMM input g (slot 8 + g % 2)
+#define NLSE_SC_VB 8
+//   [10..12] space-time focusing: ring of the maxima of |P Y w| (float bits) of the GEMM inputs
+//           (input g's goes to slot 10 + g % 3; input g + 1 takes its scale from it; input 0's
+//           "previous" maximum comes from a reduction over its first product, slot 12)
+#define NLSE_SC_VMAX 10
+#define NLSE_SC_N 16
 
 // One pulse of a batch, as the batched kernels see it (device memory).
 struct BatchPulse {
@@ -114,6 +124,8 @@ struct BatchPulse {
     float2 *ste_work;     // exciton channel: row_next writes the physical field here and
                           // the two-population march runs as its own kernel (else NULL)
     int M, N, K;  // GEMM sizes: 2Nrp, Nt, 2Nrp
+    int kdiag;    // block-diagonal operator (space-time focusing: Y on each plane): a tile of rows in
+                  // block b takes only the K range of block b
 };
 
 // One 128 x 256 tile of the grouped tensor-core product.
@@ -156,6 +168,10 @@ struct nlse_ctx {
     int *d_flag;           // device status word
     // split-BF16 path (allocated when Nr % 64 == 0 and Nt % 256 == 0)
     int split_ok, a_terms;
+    int stf;               // space-time focusing in the split forms: d_A holds diag(Y, Y) in 3 scaled FP16
+                           // terms (built once); E(Omega) w = Y (P(rho, Omega) - 1) Y w (stf_phase between)
+    float cY;              // max_m sum_k |Y_mk| (bounds |Y w| by cY max |w|)
+    float4 *d_P2s;         // Nr x Nt: exp(-i rho_m^2 dz U^-1(Omega_t) / (4 k0)) - 1 and its rounding remainder
     int Nrp;               // Nr rounded up to a multiple of 64: rows of one plane of the split-form state
                            // and of one block of E' (the padding rows / columns are zero)
     int op_f16;            // format of the operator in d_A (0: 3 BF16 terms, 1: 2 scaled FP16 terms)
@@ -193,6 +209,7 @@ enum {
     K_ROW_NEXT = 9,
     K_BUILD_OP = 10,
     K_RECORD = 11,
+    K_STF_PHASE = 12,
     K_NUM_KINDS = 16
 };
 
@@ -215,14 +232,31 @@ cudaError_t launch_row_nl_full(const RowFusedArgs &a, float *F32, __nv_bfloat16 
 cudaError_t launch_phase_table_2d(nlse_ctx *c, double dz, cudaStream_t stream);
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s,
                              int zero_first, cudaStream_t stream);
+// kdiag: block-diagonal operator (rows of block b use only K range b; M = K = 2 blocks);
+// a_terms = 3 with f16: the operator in 3 scaled FP16 terms (space-time focusing)
 cudaError_t launch_gemm_tc(const CUtensorMap *tmA, const CUtensorMap *tmB, float *D, int M, int N, int K,
-                           int a_terms, int variant, int f16, int *err, cudaStream_t stream);
+                           int a_terms, int variant, int f16, int kdiag, int *err, cudaStream_t stream);
 // Builds E in FP64 and splits it: 3 (or a_terms) BF16 terms, or with f16 two
 // FP16 terms of E 2^sa (sa from max |E|, stored in scale[NLSE_SC_SA]).
 // E' is laid out for Nrp >= Nr rows per block, zero beyond Nr.
 cudaError_t launch_build_operator(const double *Y64, const double *rho, int Nr, int Nrp, double dz, double komega,
                                   double *Er, double *Ei, int a_terms, __nv_bfloat16 *A, int f16, int *scale,
                                   cudaStream_t stream);
+// Space-time focusing in the split forms (k_stf.cu).
+// diag(Y, Y) (2 Nrp x 2 Nrp, zero outside the Nr x Nr blocks) as 3 FP16 terms of Y 2^sa;
+// sa is written to scale[NLSE_SC_SA].
+cudaError_t launch_split_Yb16(const double *Y64, int Nr, int Nrp, int sa, __half *A, int *scale,
+                              cudaStream_t stream);
+// P2s[m][t] = exp(-i rho_m^2 dz invU[t] / (4 k0)) - 1 (FP64, rounded) and its remainder.
+cudaError_t launch_stf_table(const double *rho, const double *invU, int Nr, int Nt, double dz, double komega,
+                             float4 *P2s, cudaStream_t stream);
+// Between the two products of a half step: v = D 2^-(sa + sb_g) (planes of Nrp rows), v' = P2s v,
+// written as FP16 terms of v' 2^sv into Fb (the second product's input) with sv from the
+// largest component of the previous input's v' (every sixth input, g % 6 == 0: of its own,
+// from a reduction pass first); sv goes to scale[NLSE_SC_VB + g % 2].
+cudaError_t launch_stf_phase(const float *D, const float4 *P2s, __nv_bfloat16 *Fb, int Nr, int Nrp, int Nt, float cY,
+                             int g, int *scale, cudaStream_t stream);
+
 // Failure-path probe: a bounded mbarrier wait that runs out after limit_ns and
 // raises bit 3 of the status word err.
 cudaError_t launch_wait_probe(int *err, unsigned long long limit_ns, cudaStream_t stream);
@@ -239,18 +273,34 @@ cudaError_t launch_record(nlse_ctx *c, const float2 *u, const float *rho, const 
 cudaError_t launch_split_field(const float *w, __nv_bfloat16 *hi, size_t lo_off, size_t n, cudaStream_t st);
 // kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call),
 // 3 = nonlinear with the full-physics block (N_t <= 4096);
-// g = index of the GEMM input the kernel consumes (the split-FP16 scales; -1 for the entry)
+// g = index of the GEMM input the kernel consumes (the split-FP16 scales; -1 for the entry);
+// plan = the row plan of kinds 1 and 2 (0 or 1, see row_plan)
 cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
-                             int g, cudaStream_t st);
+                             int g, int plan, cudaStream_t st);
 cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
                                    int a_terms, int variant, int f16, int *err, cudaStream_t stream);
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,
                              int do_scan, cudaStream_t st);
-// g: index of the GEMM input whose product D the kernel consumes; it writes input g + 1
+// g: index of the GEMM input whose product D the kernel consumes; it writes input g + 1;
+// plan: the row plan (0 or 1; both give identical results, see row_plan)
 cudaError_t launch_row_nl(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, const float *rho,
-                          int g, cudaStream_t st);
+                          int g, int plan, cudaStream_t st);
 cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D, float *rho,
-                            float2 *u_out, int write_state, int do_scan, int apply_mask, int g, cudaStream_t st);
+                            float2 *u_out, int write_state, int do_scan, int apply_mask, int g, int plan,
+                            cudaStream_t st);
+// Row plans of this device for N_t = 2^logNt: the pick of row_nl (kind 0) and
+// row_next (kind 1), timed once per device and N_t on synthetic rows the first
+// time a context of that N_t needs them (row_plan_tune, in nlse_create).
+int row_plan(int logNt, int kind);
+// Times both plans of each kind on R <= Nr synthetic rows (scratch allocated
+// and freed here; Pt_scratch: 2 N_t float2 it may overwrite) unless already
+// tuned for this device and N_t; synchronous.
+cudaError_t row_plan_tune(int logNt, int Nr, const float2 *tw, const float *lut, const float4 *pchip,
+                          const float *mask_r, const NLParams &nl, const ScanParams &sc, float2 *Pt_scratch,
+                          int *scale);
+int row_plan_get(int logNt, int kind);             // -1: not tuned yet
+int row_plan_set(int logNt, int kind, int plan);   // plan -1: tune again at the next context creation
+int row_plan_generation();                         // bumped by every row_plan_set
 
 // ---------------------------------------------------------------- complex
 __device__ __forceinline__ float2 c_add(float2 a, float2 b) { return make_float2(a.x + b.x, a.y + b.y); }
@@ -481,6 +531,152 @@ __device__ __forceinline__ float2 *fft_passes(float2 *src, float2 *dst, const fl
 template <int N, bool INV, int T = NLSE_ROW_THREADS>
 __device__ __forceinline__ float2 *fft_row(float2 *buf0, float2 *buf1, const float2 *__restrict__ tw) {
     return fft_passes<N, 1, INV, T>(buf0, buf1, tw);
+}
+
+// ------------------------------------------------ compact row FFT (one pass body)
+// The same Stockham plan, butterflies, twiddle products and rounding as
+// fft_row (results agree bit for bit), with the pass stride NS and the
+// direction taken at run time: one radix-8 pass body serves every radix-8 pass
+// of both transforms, so a kernel with two row FFTs carries two pass bodies
+// instead of eight unrolled ones (the unrolled form's code overflows the
+// instruction cache in the fused row kernels).  sg = +1 forward, -1 inverse;
+// multiplying by sg is exact, and every sum and rounding is that of the
+// compile-time form (e.g. the inverse's x - y is formed as x + (-y)).
+
+// v *= exp(-+ i pi / 2) for sg = +1 / -1
+__device__ __forceinline__ float2 c_quarter_s(float2 a, float sg) { return make_float2(sg * a.y, -sg * a.x); }
+
+__device__ __forceinline__ void dft4_s(float2 *v, float sg) {
+    float2 y0 = c_add(v[0], v[2]), y1 = c_sub(v[0], v[2]);
+    float2 y2 = c_add(v[1], v[3]), y3 = c_quarter_s(c_sub(v[1], v[3]), sg);
+    v[0] = c_add(y0, y2);
+    v[2] = c_sub(y0, y2);
+    v[1] = c_add(y1, y3);
+    v[3] = c_sub(y1, y3);
+}
+
+__device__ __forceinline__ void dft8_s(float2 *v, float sg) {
+    float2 a[4], b[4];
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+        a[r] = c_add(v[r], v[r + 4]);
+        b[r] = c_sub(v[r], v[r + 4]);
+    }
+    // b_r *= w8^r, w8 = exp(-+ i pi / 4) (dft8's expressions with y -> sg y)
+    {
+        const float y = sg * b[1].y;
+        b[1] = make_float2(mul_rsqrt2(b[1].x + y), sg * mul_rsqrt2(y - b[1].x));
+    }
+    b[2] = c_quarter_s(b[2], sg);
+    {
+        const float y = sg * b[3].y;
+        b[3] = make_float2(mul_rsqrt2(y - b[3].x), -sg * mul_rsqrt2(b[3].x + y));
+    }
+    dft4_s(a, sg);
+    dft4_s(b, sg);
+#pragma unroll
+    for (int m = 0; m < 4; ++m) {
+        v[2 * m] = a[m];
+        v[2 * m + 1] = b[m];
+    }
+}
+
+template <int R>
+__device__ __forceinline__ void dft_small_s(float2 *v, float sg) {
+    if (R == 2) {
+        dft2<false>(v);
+    } else if (R == 4) {
+        dft4_s(v, sg);
+    } else {
+        dft8_s(v, sg);
+    }
+}
+
+// One radix-R pass over an N-point row at run-time stride NS (> 1: twiddles
+// from the pass's table block at tw_pass; tw_rem = the remainders' offset).
+template <int R, int N, int T>
+__device__ __forceinline__ void stockham_pass_s(const float2 *__restrict__ src, float2 *__restrict__ dst,
+                                                const float2 *__restrict__ tw_pass, int tw_rem, int NS, float sg) {
+    constexpr int nb = N / R;
+#pragma unroll
+    for (int jj = 0; jj < (nb + T - 1) / T; ++jj) {
+        const int j = (int)threadIdx.x + jj * T;
+        if (nb % T == 0 || j < nb) {
+            const int k = j & (NS - 1);
+            float2 v[R];
+#pragma unroll
+            for (int r = 0; r < R; ++r) v[r] = src[pidx(j + r * nb)];
+            if (NS > 1) {
+                const float4 *w4 = reinterpret_cast<const float4 *>(tw_pass) + k;
+                float2 w[fft_tw_row(R)];
+#pragma unroll
+                for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
+                    const float4 p = __ldg(&w4[q * NS]);
+                    w[2 * q] = make_float2(p.x, p.y);
+                    w[2 * q + 1] = make_float2(p.z, p.w);
+                }
+#if NLSE_COMP_TWIDDLE
+                const float4 *l4 = w4 + tw_rem / 2;
+                float2 wl[fft_tw_row(R)];
+#pragma unroll
+                for (int q = 0; q < fft_tw_row(R) / 2; ++q) {
+                    const float4 p = __ldg(&l4[q * NS]);
+                    wl[2 * q] = make_float2(p.x, p.y);
+                    wl[2 * q + 1] = make_float2(p.z, p.w);
+                }
+#pragma unroll
+                for (int r = 1; r < R; ++r) {
+                    const float2 x = make_float2(w[r - 1].x, sg * w[r - 1].y);
+                    const float2 xl = make_float2(wl[r - 1].x, sg * wl[r - 1].y);
+#if NLSE_COMP_TWIDDLE == 2
+                    v[r] = c_mul_exact(v[r], x, xl);
+#else
+                    v[r] = c_mul_comp(v[r], x, xl);
+#endif
+                }
+#else
+#pragma unroll
+                for (int r = 1; r < R; ++r) v[r] = c_mul(v[r], make_float2(w[r - 1].x, sg * w[r - 1].y));
+#endif
+            }
+            dft_small_s<R>(v, sg);
+            const int d0 = (j - k) * R + k;
+#pragma unroll
+            for (int r = 0; r < R; ++r) dst[pidx(d0 + r * NS)] = v[r];
+        }
+    }
+}
+
+// Full FFT of one row (as fft_row: buf0 in, buf1 scratch, returns the buffer
+// holding the unnormalised result); inv selects the direction at run time.
+template <int N, int T = NLSE_ROW_THREADS>
+__device__ __forceinline__ float2 *fft_row_s(float2 *buf0, float2 *buf1, const float2 *__restrict__ tw, bool inv) {
+    const float sg = inv ? -1.0f : 1.0f;
+    float2 *src = buf0, *dst = buf1;
+    int NS = 1, off = 0;
+#pragma unroll 1
+    while (fft_radix(N, NS) == 8 && NS < N) {
+        stockham_pass_s<8, N, T>(src, dst, tw + off, fft_tw_size(N), NS, sg);
+        if (NS > 1) off += NS * fft_tw_row(8);
+        NS *= 8;
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    if (NS < N) {
+        // the one remaining pass (radix N / NS, 4 or 2)
+        if (N / NS == 4) {
+            stockham_pass_s<4, N, T>(src, dst, tw + off, fft_tw_size(N), NS, sg);
+        } else {
+            stockham_pass_s<2, N, T>(src, dst, tw + off, fft_tw_size(N), NS, sg);
+        }
+        __syncthreads();
+        float2 *t = src;
+        src = dst;
+        dst = t;
+    }
+    return src;
 }
 
 // ------------------------------------------------ register-resident row FFT

@@ -6,10 +6,11 @@ A scenario is a name and the keyword overrides of ``run()`` on top of shared
 base parameters.  ``run_scenarios`` runs every scenario whose ``result.npz`` is
 not already cached (with the current code fingerprint) concurrently on one GPU:
 
-* scenarios that the batched tensor-core form accepts (split-BF16 mode, grid a
-  multiple of 64 x 256, no exciton channel or full-physics term) and that share
-  dz, nz and save_stride advance together in one ``nlse_batch`` -- one grouped
-  GEMM and one row launch per time-grid class per half step for all of them;
+* scenarios that the batched tensor-core form accepts (a split linear mode --
+  "auto" resolves to split-BF16 -- up to 8192 radial points, no space-time
+  focusing) and that share dz, nz, save_stride and that form advance together
+  in one ``nlse_batch`` -- one grouped GEMM and one row launch per time-grid
+  class per half step for all of them;
 * every other scenario runs on its own context and CUDA stream;
 
 and all of them are advanced one save interval at a time, round robin, so the
@@ -25,7 +26,7 @@ import numpy as np
 import torch
 
 from ._lib import MODE_SPLIT_F16, Batch
-from .config import resolved_linear_mode, split_supported
+from .config import batch_supported, resolved_linear_mode
 from .filament_sim import FIELD_TOGGLES, run_config
 from .grids import build_grids
 from .integrator import Integrator, code_fingerprint
@@ -83,7 +84,7 @@ def summarize(results):
 def _batchable(cfg):
     # a batch takes the Raman / self-steepening terms and the exciton channel;
     # space-time focusing has no single radial operator (plain mode, own context)
-    return resolved_linear_mode(cfg) in ("split_bf16", "split_f16") and split_supported(cfg)
+    return resolved_linear_mode(cfg) in ("split_bf16", "split_f16") and batch_supported(cfg)
 
 
 class _Group:

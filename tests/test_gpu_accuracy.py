@@ -37,6 +37,18 @@ def test_fp64_gpu_reference_is_pinned():
     assert np.abs(rho.cpu().numpy() - ref_rho).max() <= 1e-11 * ref_rho.max()
 
 
+def test_fp64_gpu_space_time_focusing_is_pinned():
+    """The FP64 GPU restatement with space-time focusing (the Omega-dependent
+    diffraction phase and the U^-1 filter of split) against the numpy oracle."""
+    import fp64_gpu
+    og = O.OracleGrid(O.workload_config(64, 256, 1e-4, 1e-5, 3e-13, enable_space_time_focusing=True))
+    u0 = O.lens_gaussian(og, 1e-5, 100e-15, 2.0, 1e-2, 0)
+    ref_u, ref_rho, _ = og.propagate(u0.copy(), 5, 5e-6)
+    u, rho = fp64_gpu.FP64GPU(og).propagate(u0, 5, 5e-6)
+    assert rel_l2(u.cpu().numpy(), ref_u) < 1e-11
+    assert np.abs(rho.cpu().numpy() - ref_rho).max() <= 1e-11 * ref_rho.max()
+
+
 def _metrics(u, rho, uref, rref, dt, invE2):
     flu = (np.abs(u) ** 2).sum(axis=1) * dt * invE2
     flu_r = (np.abs(uref) ** 2).sum(axis=1) * dt * invE2
@@ -88,3 +100,47 @@ def test_one_cm_accuracy():
         for name in ("split_bf16_3term", "split_f16"):
             m = entry[name]
             assert m["l2"] <= 1e-4 and m["peak_rho"] <= 1e-3, (at, name, m)
+
+
+def test_space_time_focusing_half_cm_accuracy():
+    """The 1024 x 2048 workload with space-time focusing on (the reference's
+    default), 2000 z-steps (0.5 cm): the tensor-core sandwich Y P(rho, Omega) Y
+    (scaled FP16 terms) and the plain FP32 form against the FP64 reference,
+    with the bounds L2 <= 1e-4 and peak-rho <= 1e-3 at every checkpoint for the
+    tensor-core form; written to NLSE_REPORT_DIR like the 1 cm report."""
+    import torch
+    import fp64_gpu
+    from rapport_gb300._lib import MODE_PLAIN_F32, MODE_SPLIT_F16
+
+    c = Case(**CONFIG2, enable_space_time_focusing=True)
+    ref = fp64_gpu.FP64GPU(c.og)
+    forms = {"split_stf_sandwich": MODE_SPLIT_F16, "plain_fp32": MODE_PLAIN_F32}
+    state = {k: (dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))) for k in forms}
+    ur = torch.tensor(c.u0, dtype=torch.complex128, device="cuda")
+    rr = torch.zeros(c.u0.shape, dtype=torch.float64, device="cuda")
+    report = {"workload": "1024x2048, 5 uJ, w0 150 um, f 10 cm, dz 2.5 um, 1% noise seed 0, space-time focusing",
+              "commit": os.environ.get("NLSE_COMMIT", "unknown"),
+              "reference": "FP64 GPU restatement (oracle/fp64_gpu.py), same seeded input", "checkpoints": {}}
+    done = 0
+    for stop in (500, 1000, 2000):
+        for _ in range(stop - done):
+            ref.update_plasma(ur, rr)
+            ur = ref.step(ur, rr, c.dz)
+        for name, mode in forms.items():
+            u, rho, rs = state[name]
+            c.ctx.propagate(u, rho, rs, c.dz, stop - done, mode)
+        done = stop
+        urn, rrn = ur.cpu().numpy(), rr.cpu().numpy()
+        entry = {name: _metrics(host(state[name][0]), host(state[name][1]), urn, rrn, c.og.dt, c.og.invE2)
+                 for name in forms}
+        report["checkpoints"][f"{stop * c.dz * 100:.3f} cm"] = entry
+        print(stop, json.dumps(entry), flush=True)
+    assert c.ctx.device_status() == 0
+    out = os.environ.get("NLSE_REPORT_DIR")
+    if out:
+        os.makedirs(out, exist_ok=True)
+        with open(os.path.join(out, "accuracy_stf_halfcm_1024x2048.json"), "w") as f:
+            json.dump(report, f, indent=1)
+    for at, entry in report["checkpoints"].items():
+        m = entry["split_stf_sandwich"]
+        assert m["l2"] <= 1e-4 and m["peak_rho"] <= 1e-3, (at, m)

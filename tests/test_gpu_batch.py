@@ -231,9 +231,37 @@ def test_batch_exciton_pulse_needs_rho_s():
         b.propagate(us, rhos, None, DZ, STEPS)
 
 
-def test_batch_rejects_space_time_focusing():
+@pytest.mark.parametrize("mode", [1, 2])
+def test_batch_with_space_time_focusing_pulses(mode):
+    """Pulses with space-time focusing (their own grouped products of the
+    sandwich Y P Y and a phase pass each) beside pulses in the batch's form:
+    every pulse bit-identical to its single-context run, within the parity
+    tolerance of the oracle, also over enough steps for the z-step graph."""
     import rapport_gb300 as R
     from rapport_gb300 import _lib
-    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, DZ, 1, enable_space_time_focusing=True)
-    with pytest.raises(_lib.NLSEError, match="space-time focusing"):
-        _lib.Batch([cfg], [R.build_grids(cfg)])
+    spec = [(64, 256, dict(enable_space_time_focusing=True)), (64, 256, {}),
+            (100, 512, dict(enable_space_time_focusing=True, f_R=0.18, enable_kerr_raman=True)),
+            (128, 512, {})]
+    cfgs, grids, u0s = [], [], []
+    for i, (Nr, Nt, over) in enumerate(spec):
+        cfg = R.workload_config(Nr, Nt, 1e-4 * Nr / 64, 1.5e-5, 3e-13 * Nt / 256, DZ, 8, **over)
+        g = R.build_grids(cfg)
+        cfgs.append(cfg)
+        grids.append(g)
+        u0s.append(R.envelope_lens(1.5e-5, 100e-15, 1.0 + 0.2 * i, 1e-2, 30 + i)(g["rr"], g["tt"], cfg, g))
+    b = _lib.Batch(cfgs, grids)
+    b.set_mode(mode)
+    us = [dev(u) for u in u0s]
+    rhos = [dev(np.zeros(u.shape)) for u in u0s]
+    b.propagate(us, rhos, None, DZ, 8)
+    assert b.device_status() == 0
+    for i, ((Nr, Nt, over), cfg, g, u0) in enumerate(zip(spec, cfgs, grids, u0s)):
+        ctx = _lib.Context(cfg, g)
+        u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+        ctx.propagate(u, rho, rs, DZ, 8, mode)
+        assert np.array_equal(host(us[i]), host(u)), i
+        assert np.array_equal(host(rhos[i]), host(rho)), i
+        og = O.OracleGrid(O.workload_config(Nr, Nt, 1e-4 * Nr / 64, 1.5e-5, 3e-13 * Nt / 256, **over))
+        uo, rho_o, _ = og.propagate(O.lens_gaussian(og, 1.5e-5, 100e-15, 1.0 + 0.2 * i, 1e-2, 30 + i), 8, DZ)
+        assert rel_l2(host(us[i]), uo) < 5e-5, i
+        assert np.abs(host(rhos[i]) - rho_o).max() <= 1e-3 * max(rho_o.max(), 1e-30), i

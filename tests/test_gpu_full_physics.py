@@ -114,12 +114,11 @@ def test_row_with_a_nan_gets_no_nonlinear_term(fc):
     assert rel_l2(got[keep], ref[keep]) < 2e-5
 
 
-def test_split_bf16_without_space_time_focusing(full):
-    """Raman + self-steepening + excitons in the tensor-core form (row_nl runs
-    the full block); space-time focusing is rejected there."""
+def test_split_forms_without_space_time_focusing(full):
+    """Raman + self-steepening + excitons in the tensor-core forms (row_nl runs
+    the full block; the merged operator I + E)."""
     from rapport_gb300 import _lib
     m = meta_case(full)
-    # the split form tiles Nr by 64 and Nt by 256
     c = Case(64, 256, m["R_max"], m["w0"], m["T_half"], m["fwhm"], m["E"], m["f"], m["dz"], 4, 0, **NO_STF)
     uo, ro, so = c.og.propagate(c.u0.copy(), 4, c.dz)
     for mode in (_lib.MODE_SPLIT_BF16, _lib.MODE_SPLIT_F16):
@@ -129,10 +128,49 @@ def test_split_bf16_without_space_time_focusing(full):
         assert np.abs(host(rho) - ro).max() <= 1e-3 * ro.max(), mode
         assert np.abs(host(rs) - so).max() <= 1e-3 * so.max(), mode
         assert c.ctx.device_status() == 0
-    s = Case(64, 256, m["R_max"], m["w0"], m["T_half"], m["fwhm"], m["E"], m["f"], m["dz"], 1, 0, **FULL_PHYSICS)
-    with pytest.raises(_lib.NLSEError, match="space-time focusing"):
-        s.ctx.propagate(dev(s.u0), dev(np.zeros(s.u0.shape)), dev(np.zeros(s.u0.shape)), s.dz, 1,
-                        _lib.MODE_SPLIT_BF16)
+
+
+@pytest.mark.parametrize("mode", [1, 2])
+def test_split_forms_every_term_match_reference_fixture(fc, full, mode):
+    """The reference's default physics -- space-time focusing with Raman,
+    self-steepening and excitons -- in the tensor-core forms: the half step is
+    the sandwich Y P(rho, Omega) Y in scaled FP16 terms, against the
+    reference's own z-steps (tiny_full.npz) at the plain form's tolerance."""
+    u, rho, rs = dev(fc.u0), dev(np.zeros(fc.u0.shape)), dev(np.zeros(fc.u0.shape))
+    done = 0
+    for j, s in enumerate(full["steps_kept"]):
+        fc.ctx.propagate(u, rho, rs, fc.dz, int(s) - done, mode)
+        done = int(s)
+        assert rel_l2(host(u), full["u_steps"][j]) < 1e-4, s
+        ro, so = full["rho_steps"][j], full["rho_s_steps"][j]
+        assert np.abs(host(rho) - ro).max() <= 1e-3 * ro.max(), s
+        assert np.abs(host(rs) - so).max() <= 1e-3 * so.max(), s
+    assert fc.ctx.device_status() == 0
+
+
+@pytest.mark.parametrize("over,shape", [(FULL_PHYSICS, (64, 256)), (SINGLE["stf"], (256, 512)),
+                                        (SINGLE["stf"], (100, 1024))])
+def test_split_space_time_focusing_vs_oracle(full, over, shape):
+    """Space-time focusing in the tensor-core forms against the FP64 oracle:
+    with every term and alone, on a radial size that is padded (100 -> 128)."""
+    from rapport_gb300 import _lib
+    m = meta_case(full)
+    Nr, Nt = shape
+    c = Case(Nr, Nt, m["R_max"] * Nr / 64, m["w0"], m["T_half"] * Nt / 128, m["fwhm"], m["E"], m["f"], m["dz"],
+             4, 0, **over)
+    uo, ro, so = c.og.propagate(c.u0.copy(), 4, c.dz)
+    hl_o = c.og.half_linear(c.u0, c.dz)
+    for mode in (_lib.MODE_SPLIT_BF16, _lib.MODE_SPLIT_F16):
+        hl = dev(c.u0)
+        c.ctx.half_linear(hl, c.dz, mode)
+        assert rel_l2(host(hl), hl_o) < 2e-5, (shape, mode)
+        u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+        c.ctx.propagate(u, rho, rs, c.dz, 4, mode)
+        assert rel_l2(host(u), uo) < 5e-5, (shape, mode)
+        assert np.abs(host(rho) - ro).max() <= 1e-3 * max(ro.max(), 1e-30), (shape, mode)
+        if so.max() > 0:
+            assert np.abs(host(rs) - so).max() <= 1e-3 * so.max(), (shape, mode)
+        assert c.ctx.device_status() == 0
 
 
 def test_full_physics_limits():
@@ -141,7 +179,3 @@ def test_full_physics_limits():
     cfg = R.workload_config(16, 8192, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_self_steepening=True)
     with pytest.raises(_lib.NLSEError, match="4096"):
         _lib.Context(cfg, R.build_grids(cfg))
-    # a batch takes Raman / self-steepening pulses but not space-time focusing
-    cfg = R.workload_config(64, 256, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_space_time_focusing=True)
-    with pytest.raises(_lib.NLSEError, match="space-time focusing"):
-        _lib.Batch([cfg], [R.build_grids(cfg)])

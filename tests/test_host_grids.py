@@ -107,13 +107,14 @@ def test_keldysh_tables_match_reference(tiny_keldysh):
 
 
 def test_linear_mode_resolution():
-    """auto = the split-BF16 tensor-core form where the grid tiles and the
-    physics has a single radial operator, else the plain FP32 form."""
+    """auto = a tensor-core form wherever the library runs one (split-BF16, or
+    split-FP16 with space-time focusing), else the plain FP32 form."""
     from rapport_gb300.config import resolved_linear_mode, split_supported
     mk = lambda **kw: R.Config(verbose=False, out_dir="", **kw)  # noqa: E731
     assert mk().linear_mode == "auto"
     assert resolved_linear_mode(mk(N=1025, Nt=2048, enable_space_time_focusing=False)) == "split_bf16"
-    assert resolved_linear_mode(mk(N=1025, Nt=2048, enable_space_time_focusing=True)) == "plain"
+    # space-time focusing: the sandwich Y P Y, whose arithmetic is the split-FP16 form's
+    assert resolved_linear_mode(mk(N=1025, Nt=2048, enable_space_time_focusing=True)) == "split_f16"
     # N_r = 999 (the context pads it to 1024) and N_t = 128 (one partial tile) run split too
     assert resolved_linear_mode(mk(N=1000, Nt=2048, enable_space_time_focusing=False)) == "split_bf16"
     assert resolved_linear_mode(mk(N=65, Nt=128, enable_space_time_focusing=False)) == "split_bf16"
