@@ -139,7 +139,8 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl", device_id=dev)
     w = WORKLOAD
     Z = args.zsteps
-    cfg = R.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], w["dz"], Z)
+    stf = dict(enable_space_time_focusing=True) if args.space_time_focusing else {}
+    cfg = R.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], w["dz"], Z, **stf)
     g = R.build_grids(cfg)
     ctx = _lib.Context(cfg, g)
     u0 = R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"])(g["rr"], g["tt"], cfg, g)
@@ -380,6 +381,7 @@ def run_ours(args, rank, world, local_rank):
         "dtype": {"split_bf16": "bf16x3-split + f32", "split_f16": "f16x2-split + f32"}.get(bmode, "f32"),
         "data": "synthetic (seeded lens-focused Gaussian pulses with 1% noise)",
         "config": dict(CONFIG, form=form, pulses=max(B, 1), z_steps_per_step=Z, parallelism=f"replicas{world}",
+                       space_time_focusing=bool(args.space_time_focusing),
                        l2="256 MB flush before each timed step (outside its events); per pulse 24 MB",
                        kernel_times="second identical pass of K steps with per-launch events"),
         "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
@@ -762,6 +764,9 @@ def main():
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=8, help="pulses of the batched (headline) form; 0 = single pulse")
+    ap.add_argument("--space-time-focusing", action="store_true",
+                    help="the single / batched workload with space-time focusing on (the reference's default): "
+                         "the tensor-core forms run the correction Y (P - 1) Y")
     ap.add_argument("--workload", default="single", choices=["single", "config4", "config5", "tour"],
                     help="tour: every kernel once at 1024 x 2048 (for ncu launch lists)")
     ap.add_argument("--record-traffic", metavar="CSV",
