@@ -24,16 +24,17 @@
 #pragma once
 #include "nl_impl.cuh"
 
-// Shared memory of the full block: three padded complex row buffers (FFTs)
-// and the rows U, KS, S.  202,752 bytes at N_t = 4096.
+// Shared memory of the full block: three padded complex row buffers (FFTs),
+// the rows U, KS, S and the float row PH.  219,136 bytes at N_t = 4096.
 template <int NT>
 __host__ __device__ constexpr size_t full_smem_bytes() {
-    return 3 * (size_t)fft_slots(NT) * sizeof(float2) + 3 * (size_t)NT * sizeof(float2);
+    return 3 * (size_t)fft_slots(NT) * sizeof(float2) + 3 * (size_t)NT * sizeof(float2) + (size_t)NT * sizeof(float);
 }
 
 struct FullRows {
     float2 *B0, *B1, *B2;  // padded FFT buffers
     float2 *U, *KS, *S;    // post-alpha field, RK accumulator, stage field (index t)
+    float *PH;             // the stage's photo-ionisation term per point (index t)
 };
 
 template <int NT>
@@ -45,6 +46,7 @@ __device__ __forceinline__ FullRows full_rows(float2 *smem) {
     r.U = smem + 3 * fft_slots(NT);
     r.KS = r.U + NT;
     r.S = r.KS + NT;
+    r.PH = reinterpret_cast<float *>(r.S + NT);
     return r;
 }
 
@@ -70,16 +72,27 @@ __device__ __forceinline__ float alpha_from(float photo, float rho, const NLPara
 
 __device__ __forceinline__ bool c_finite(float2 v) { return isfinite(v.x) && isfinite(v.y); }
 
-// k = split(S) for the thread's points of the stage field S (shared, index
-// t); sink(t, k_t) consumes each value and may overwrite S[t], which is not
-// read again for that point.  All threads of the CTA call it; the three FFT
-// buffers are free again on return (synced).
-template <int NT, typename Sink>
-__device__ __forceinline__ void rhs_full(const FullRows &m, const float *__restrict__ rho,
+// CTAs per SM the full-physics kernels are compiled for: what their shared
+// memory admits, at most 2 (<= 128 registers a thread at 256 threads; with
+// the whole block inlined ptxas otherwise spends ~180 and fits one CTA).
+template <int NT>
+__host__ __device__ constexpr int full_min_blocks() {
+    return (228 * 1024) / (int)(full_smem_bytes<NT>() + 1024) >= 2 ? 2 : 1;
+}
+
+// k = split(S) for every point of the stage field S (shared, index t), left in
+// a free FFT buffer (padded index) whose pointer is returned; synced, and the
+// other buffers are free again.  All threads of the CTA call it.  Each thread
+// evaluates photo-ionisation once per point (kept in m.PH for the second
+// pass).  Out of line: the RK block calls it four times, and four inlined
+// copies overflow the registers (one CTA per SM).
+template <int NT>
+__device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restrict__ rho,
                                          const float *__restrict__ rhos, const NLParams &p,
                                          const float4 *__restrict__ tab, const FullTabs &ft,
-                                         const float2 *__restrict__ tw, Sink sink) {
+                                         const float2 *__restrict__ tw) {
     constexpr int TT = NLSE_ROW_THREADS;
+    constexpr int PP = (NT + TT - 1) / TT;  // points per thread
     constexpr float inv_n = 1.0f / (float)NT;
     const bool fft_path = ft.T != nullptr || ft.invU != nullptr;
     float2 *B0 = m.B0, *B1 = m.B1, *B2 = m.B2;
@@ -100,26 +113,31 @@ __device__ __forceinline__ void rhs_full(const FullRows &m, const float *__restr
     // the pointwise terms; X1 (and X2) into the transform buffers on the FFT
     // path (a point's Q value is read before the same thread overwrites it)
     int bad = 0;
-    for (int t = threadIdx.x; t < NT; t += TT) {
-        const float2 s = S[t];
-        const float a2 = fmaf(s.x, s.x, s.y * s.y);
-        const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
-        const float ph = photo_term(a2, r, p, tab);
-        const float kr = Q ? Q[pidx(t)].x * inv_n : 0.0f;
-        const float K = fmaf(p.kp, a2, p.kp_raman * kr);  // kerr_pref * kerr_I
-        const float2 x1 = make_float2(-K * s.y, K * s.x);   // i K S
-        const float2 x2 = c_scale(s, ph);
-        const float2 x3 = c_mul(s, make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r)));
-        bad |= !(c_finite(x1) && c_finite(x2) && c_finite(x3));
-        if (ft.T) {
-            B0[pidx(t)] = x1;
-            B2[pidx(t)] = x2;
-        } else if (ft.invU) {
-            B0[pidx(t)] = c_add(c_sub(x1, x2), x3);
+#pragma unroll
+    for (int q = 0; q < PP; ++q) {
+        const int t = (int)threadIdx.x + q * TT;
+        if (NT % TT == 0 || t < NT) {
+            const float2 s = S[t];
+            const float a2 = fmaf(s.x, s.x, s.y * s.y);
+            const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
+            const float ph = photo_term(a2, r, p, tab);
+            m.PH[t] = ph;
+            const float kr = Q ? Q[pidx(t)].x * inv_n : 0.0f;
+            const float K = fmaf(p.kp, a2, p.kp_raman * kr);  // kerr_pref * kerr_I
+            const float2 x1 = make_float2(-K * s.y, K * s.x);   // i K S
+            const float2 x2 = c_scale(s, ph);
+            const float2 x3 = c_mul(s, make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r)));
+            bad |= !(c_finite(x1) && c_finite(x2) && c_finite(x3));
+            if (ft.T) {
+                B0[pidx(t)] = x1;
+                B2[pidx(t)] = x2;
+            } else if (ft.invU) {
+                B0[pidx(t)] = c_add(c_sub(x1, x2), x3);
+            }
         }
     }
     bad = __syncthreads_or(bad);  // also orders the buffer writes before the transforms
-    const float2 *Y = nullptr;    // the spectral part of k (inverse-transformed, unnormalised)
+    float2 *Y = nullptr;          // the spectral part of k (inverse-transformed, unnormalised)
     if (fft_path && !bad) {
         float2 *C;
         if (ft.T) {
@@ -136,9 +154,13 @@ __device__ __forceinline__ void rhs_full(const FullRows &m, const float *__restr
             C = P1;
             if (ft.invU) {
                 // F[X3] through the two free buffers, then the U^-1 factor
-                for (int t = threadIdx.x; t < NT; t += TT) {
-                    const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
-                    P2[pidx(t)] = c_mul(S[t], make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r)));
+#pragma unroll
+                for (int q = 0; q < PP; ++q) {
+                    const int t = (int)threadIdx.x + q * TT;
+                    if (NT % TT == 0 || t < NT) {
+                        const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
+                        P2[pidx(t)] = c_mul(S[t], make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r)));
+                    }
                 }
                 __syncthreads();
                 float2 *P3 = fft_row<NT, false>(P2, fr2, tw);
@@ -157,30 +179,36 @@ __device__ __forceinline__ void rhs_full(const FullRows &m, const float *__restr
             Y = fft_row<NT, true>(C, C == B0 ? B1 : B0, tw);
         }
     }
-    // k per point
-    for (int t = threadIdx.x; t < NT; t += TT) {
-        const float2 s = S[t];
-        const float a2 = fmaf(s.x, s.x, s.y * s.y);
-        const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
-        const float ph = photo_term(a2, r, p, tab);
-        const float al = alpha_from(ph, r, p);
-        float2 k;
-        if (fft_path) {
-            k = bad ? make_float2(0.0f, 0.0f) : c_scale(Y[pidx(t)], inv_n);
-            if (!ft.invU)  // X3 pointwise
-                k = c_add(k, c_mul(s, make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r))));
-            k = make_float2(fmaf(al, s.x, k.x), fmaf(al, s.y, k.y));
-        } else {
-            // X1 - X2 + X3 + alpha S = i w S + (alpha - photo - pp_abs rho) S
-            const float kr = Q ? Q[pidx(t)].x * inv_n : 0.0f;
-            const float w = fmaf(p.kp, a2, p.kp_raman * kr) + fmaf(p.ste_pref, rs, -p.pp_def * r);
-            const float corr = al - fmaf(p.pp_abs, r, ph);
-            k = make_float2(fmaf(corr, s.x, -w * s.y), fmaf(corr, s.y, w * s.x));
+    // k per point, written where the thread read its Y (or Q) value: the same
+    // point of a buffer nothing else reads any more
+    float2 *K = Y ? Y : B0;
+#pragma unroll
+    for (int q = 0; q < PP; ++q) {
+        const int t = (int)threadIdx.x + q * TT;
+        if (NT % TT == 0 || t < NT) {
+            const float2 s = S[t];
+            const float a2 = fmaf(s.x, s.x, s.y * s.y);
+            const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f, ph = m.PH[t];
+            const float al = alpha_from(ph, r, p);
+            float2 k;
+            if (fft_path) {
+                k = bad ? make_float2(0.0f, 0.0f) : c_scale(Y[pidx(t)], inv_n);
+                if (!ft.invU)  // X3 pointwise
+                    k = c_add(k, c_mul(s, make_float2(-p.pp_abs * r, fmaf(p.ste_pref, rs, -p.pp_def * r))));
+                k = make_float2(fmaf(al, s.x, k.x), fmaf(al, s.y, k.y));
+            } else {
+                // X1 - X2 + X3 + alpha S = i w S + (alpha - photo - pp_abs rho) S
+                const float kr = Q ? Q[pidx(t)].x * inv_n : 0.0f;
+                const float w = fmaf(p.kp, a2, p.kp_raman * kr) + fmaf(p.ste_pref, rs, -p.pp_def * r);
+                const float corr = al - fmaf(p.pp_abs, r, ph);
+                k = make_float2(fmaf(corr, s.x, -w * s.y), fmaf(corr, s.y, w * s.x));
+            }
+            if (bad || !(a2 >= 1e-30f) || !c_finite(k)) k = make_float2(0.0f, 0.0f);
+            K[pidx(t)] = k;
         }
-        if (bad || !(a2 >= 1e-30f) || !c_finite(k)) k = make_float2(0.0f, 0.0f);
-        sink(t, k);
     }
-    __syncthreads();  // the FFT buffers are free for the next call
+    __syncthreads();
+    return K;
 }
 
 // alpha/2, RK4 on split(), alpha/2 (Integrator.step, integrator.py:140-147)
@@ -201,19 +229,29 @@ __device__ __forceinline__ void nl_block_full(const FullRows &m, const float *__
         U[t] = S[t] = c_damp(u, -hdz * al);
     }
     // k1..k4; KS = k1 + 2 k2 + 2 k3 + k4 (each thread touches only its points)
-    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) {
+    const float2 *K = rhs_full<NT>(m, rho, rhos, p, tab, ft, tw);
+    for (int t = threadIdx.x; t < NT; t += TT) {
+        const float2 k = K[pidx(t)];
         KS[t] = k;
         S[t] = make_float2(fmaf(hdz, k.x, U[t].x), fmaf(hdz, k.y, U[t].y));
-    });
-    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) {
+    }
+    __syncthreads();
+    K = rhs_full<NT>(m, rho, rhos, p, tab, ft, tw);
+    for (int t = threadIdx.x; t < NT; t += TT) {
+        const float2 k = K[pidx(t)];
         KS[t] = make_float2(fmaf(2.0f, k.x, KS[t].x), fmaf(2.0f, k.y, KS[t].y));
         S[t] = make_float2(fmaf(hdz, k.x, U[t].x), fmaf(hdz, k.y, U[t].y));
-    });
-    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) {
+    }
+    __syncthreads();
+    K = rhs_full<NT>(m, rho, rhos, p, tab, ft, tw);
+    for (int t = threadIdx.x; t < NT; t += TT) {
+        const float2 k = K[pidx(t)];
         KS[t] = make_float2(fmaf(2.0f, k.x, KS[t].x), fmaf(2.0f, k.y, KS[t].y));
         S[t] = make_float2(fmaf(dz, k.x, U[t].x), fmaf(dz, k.y, U[t].y));
-    });
-    rhs_full<NT>(m, rho, rhos, p, tab, ft, tw, [&](int t, float2 k) { KS[t] = c_add(KS[t], k); });
+    }
+    __syncthreads();
+    K = rhs_full<NT>(m, rho, rhos, p, tab, ft, tw);
+    for (int t = threadIdx.x; t < NT; t += TT) KS[t] = c_add(KS[t], K[pidx(t)]);
     const float s6 = dz * (1.0f / 6.0f);
     for (int t = threadIdx.x; t < NT; t += TT) {
         float2 u = make_float2(fmaf(s6, KS[t].x, U[t].x), fmaf(s6, KS[t].y, U[t].y));

@@ -5,7 +5,7 @@
 #include "fullnl_impl.cuh"
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
 k_nl_full(float2 *__restrict__ u, const float *__restrict__ rho, const float *__restrict__ rhos, float dz, NLParams p,
           const float4 *__restrict__ tab, FullTabs ft, const float2 *__restrict__ tw) {
     extern __shared__ float2 smf[];
@@ -17,7 +17,7 @@ k_nl_full(float2 *__restrict__ u, const float *__restrict__ rho, const float *__
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
 k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const float *__restrict__ rhos,
              float2 *__restrict__ rhs, float *__restrict__ alpha, NLParams p, const float4 *__restrict__ tab,
              FullTabs ft, const float2 *__restrict__ tw) {
@@ -32,8 +32,9 @@ k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const 
             alpha[base + t] = alpha_from(photo_term(fmaf(v.x, v.x, v.y * v.y), r, p, tab), r, p);
         }
     }
-    rhs_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, p, tab, ft, tw,
-                 [&](int t, float2 k) { rhs[base + t] = k; });
+    __syncthreads();
+    const float2 *K = rhs_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, p, tab, ft, tw);
+    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) rhs[base + t] = K[pidx(t)];
 }
 
 static FullTabs ctx_tabs(const nlse_ctx *c) { return FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf}; }

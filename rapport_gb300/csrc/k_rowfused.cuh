@@ -515,7 +515,7 @@ __device__ __forceinline__ void row_nl_full_body(const RowFusedArgs &a, int r, f
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
 k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
               const float *__restrict__ rho, int g) {
     row_nl_full_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
@@ -587,7 +587,7 @@ k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, in
 
 // Pulses with the full-physics terms (Raman / self-steepening; one time-grid class).
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
 k_row_nl_full_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
     const BatchPulse &q = P[w.x];
