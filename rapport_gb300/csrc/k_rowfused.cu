@@ -35,12 +35,12 @@ cudaError_t launch_row_next(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb
     return cudaErrorInvalidValue;
 }
 
-cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
-                             int g, int plan, cudaStream_t st) {
+cudaError_t launch_row_batch(int kind, int logNt, const PulseTable &T, const BatchCall *calls, const int2 *work,
+                             int nblocks, int flag, int g, int plan, cudaStream_t st) {
     if (kind == 3) {
-        NLSE_DISPATCH_NT_FULL(logNt, return RowKernels<NT>::batch(kind, P, work, nblocks, flag, g, plan, st));
+        NLSE_DISPATCH_NT_FULL(logNt, return RowKernels<NT>::batch(kind, T, calls, work, nblocks, flag, g, plan, st));
     } else {
-        NLSE_DISPATCH_NT(logNt, return RowKernels<NT>::batch(kind, P, work, nblocks, flag, g, plan, st));
+        NLSE_DISPATCH_NT(logNt, return RowKernels<NT>::batch(kind, T, calls, work, nblocks, flag, g, plan, st));
     }
     return cudaErrorInvalidValue;
 }

@@ -169,13 +169,13 @@ template <int NT>
 __device__ __forceinline__ void march_scan(float *sI, float2 *Rb, float *X, int r, const RowFusedArgs &a,
                                            float *rho) {
     constexpr int S = scan_span(NT, row_threads<NT>());
-    const ScanLayout L = scan_layout(NT);
+    using Sh = ScanShape<NT, row_threads<NT>()>;
     float *sW = sI + S;
     __syncthreads();
-    float *sx = reinterpret_cast<float *>(Rb), *sJ = sx + S;
-    scan_row(sI, sW, sx, sJ, X, NT, a.sc, a.lut, 0.0f, a.stats);
+    float *sx = reinterpret_cast<float *>(Rb);
+    scan_row_ct<NT, row_threads<NT>()>(sI, sW, sx, a.sc, a.lut, 0.0f, a.stats);
     float *gr = rho + (size_t)r * NT;
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) gr[t] = sx[scan_slot(t, L)];
+    for (int t = threadIdx.x; t < NT; t += row_threads<NT>()) gr[t] = sx[Sh::slot(t)];
 }
 
 // Carrier march of the physical row held (unnormalised by inv) in R; scratch
@@ -183,11 +183,11 @@ __device__ __forceinline__ void march_scan(float *sI, float2 *Rb, float *X, int 
 template <int NT>
 __device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float inv, int r, const RowFusedArgs &a,
                                           float *rho) {
-    const ScanLayout L = scan_layout(NT);
+    using Sh = ScanShape<NT, row_threads<NT>()>;
     float *sI = reinterpret_cast<float *>(O);
-    for (int t = threadIdx.x; t < NT; t += blockDim.x) {
+    for (int t = threadIdx.x; t < NT; t += row_threads<NT>()) {
         const float2 v = c_scale(R[pidx(t)], inv);
-        sI[scan_slot(t, L)] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
+        sI[Sh::slot(t)] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
     }
     march_scan<NT>(sI, R, X, r, a, rho);
 }
@@ -306,12 +306,12 @@ __device__ __forceinline__ void row_next_regs(const RowFusedArgs &a, int r, floa
         for (int m = 0; m < NT / row_threads<NT>(); ++m) gu[threadIdx.x + m * row_threads<NT>()] = c_scale(v[m], inv);
     }
     if (!do_scan) return;
-    const ScanLayout L = scan_layout(NT);
+    using Sh = ScanShape<NT, row_threads<NT>()>;
     float *sI = reinterpret_cast<float *>(F);
 #pragma unroll
     for (int m = 0; m < NT / row_threads<NT>(); ++m) {
         const float2 w = c_scale(v[m], inv);
-        sI[scan_slot((int)threadIdx.x + m * row_threads<NT>(), L)] = fmaf(w.x, w.x, w.y * w.y) * a.sc.invE2;
+        sI[Sh::slot((int)threadIdx.x + m * row_threads<NT>())] = fmaf(w.x, w.x, w.y * w.y) * a.sc.invE2;
     }
     march_scan<NT>(sI, F == A ? B : A, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), r, a, rho);
 }
@@ -411,7 +411,8 @@ __device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, con
 template <int NT>
 __device__ __forceinline__ void row_nl_regs_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
                                                  __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-                                                 const float *__restrict__ rho, int g) {
+                                                 const float *__restrict__ rho, const float *__restrict__ rho_s,
+                                                 int g) {
     constexpr int T = NT / 8, P = 8;
     extern __shared__ float2 sm2[];
     float2 *A = sm2, *B = sm2 + fft_slots(NT);
@@ -419,14 +420,24 @@ __device__ __forceinline__ void row_nl_regs_body(const RowFusedArgs &a, int r, f
     load_mw_regs<NT, T>(v, r, a, F32, D, 1.0f / (float)NT, g);
     float2 *F = fft_regs<NT, true, T>(v, A, B, a.tw);
     const float *gr = rho + (size_t)r * NT;
-    const float *gs = a.rho_s ? a.rho_s + (size_t)r * NT : nullptr;
+    const float *gs = rho_s ? rho_s + (size_t)r * NT : nullptr;
+    // The nonlinear block runs rolled (its unrolled copies overflow the
+    // instruction cache), which would index v at run time and move it to
+    // local memory: the thread's points go through their own slots of F
+    // instead (F was last read before the inverse transform's final barrier,
+    // and each thread reads back only what it wrote).
+#pragma unroll
+    for (int m = 0; m < P; ++m) F[pidx((int)threadIdx.x + m * T)] = v[m];
 #pragma unroll 1
     for (int m = 0; m < P; ++m) {
         const int t = (int)threadIdx.x + m * T;
-        v[m] = nl_point(v[m], gr[t], gs ? gs[t] : 0.0f, a.dz, a.nl, a.pchip);
+        F[pidx(t)] = nl_point(F[pidx(t)], gr[t], gs ? gs[t] : 0.0f, a.dz, a.nl, a.pchip);
     }
-    // F was last read before the inverse transform's final barrier: the
-    // forward transform's first pass may write it at once
+#pragma unroll
+    for (int m = 0; m < P; ++m) v[m] = F[pidx((int)threadIdx.x + m * T)];
+    // the forward transform's first pass writes F without a barrier: every
+    // thread must have read its points back first
+    __syncthreads();
     fft_regs<NT, false, T>(v, F, F == A ? B : A, a.tw);
     store_state_regs<NT, T>(v, r, a, F32, Fb, g + 1);
 }
@@ -435,9 +446,9 @@ __device__ __forceinline__ void row_nl_regs_body(const RowFusedArgs &a, int r, f
 template <int NT, int PLAN = 0>
 __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
                                             __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-                                            const float *__restrict__ rho, int g) {
+                                            const float *__restrict__ rho, const float *__restrict__ rho_s, int g) {
     if constexpr (PLAN == 1 && nl_plan1_ok<NT>()) {
-        row_nl_regs_body<NT>(a, r, F32, Fb, D, rho, g);
+        row_nl_regs_body<NT>(a, r, F32, Fb, D, rho, rho_s, g);
         return;
     }
     extern __shared__ float2 sm2[];
@@ -447,7 +458,7 @@ __device__ __forceinline__ void row_nl_body(const RowFusedArgs &a, int r, float 
     float2 *R = PLAN == 2 ? fft_row_s<NT, row_threads_nl<NT>()>(b0, b1, a.tw, true)
                           : fft_row<NT, true, row_threads_nl<NT>()>(b0, b1, a.tw);
     const float *gr = rho + (size_t)r * NT;
-    const float *gs = a.rho_s ? a.rho_s + (size_t)r * NT : nullptr;
+    const float *gs = rho_s ? rho_s + (size_t)r * NT : nullptr;
     // kept rolled: the RK4 block is long, and unrolled copies of it (with the
     // two transforms around it) overflow the instruction cache
 #pragma unroll 1
@@ -498,7 +509,8 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
 template <int NT>
 __device__ __forceinline__ void row_nl_full_body(const RowFusedArgs &a, int r, float *__restrict__ F32,
                                                  __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
-                                                 const float *__restrict__ rho, int g) {
+                                                 const float *__restrict__ rho, const float *__restrict__ rho_s,
+                                                 int g) {
     extern __shared__ float2 sm2[];
     const FullRows m = full_rows<NT>(sm2);
     load_mw_row<NT>(m.B0, r, a, F32, D, 1.0f / (float)NT, g);
@@ -506,7 +518,7 @@ __device__ __forceinline__ void row_nl_full_body(const RowFusedArgs &a, int r, f
     const float2 *R = fft_row<NT, true>(m.B0, m.B1, a.tw);
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.U[t] = R[pidx(t)];
     __syncthreads();
-    nl_block_full<NT>(m, rho + (size_t)r * NT, a.rho_s ? a.rho_s + (size_t)r * NT : nullptr, a.dz, a.nl, a.pchip,
+    nl_block_full<NT>(m, rho + (size_t)r * NT, rho_s ? rho_s + (size_t)r * NT : nullptr, a.dz, a.nl, a.pchip,
                       a.ft, a.tw);
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.B0[pidx(t)] = m.U[t];
     __syncthreads();
@@ -518,7 +530,7 @@ template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
 k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
               const float *__restrict__ rho, int g) {
-    row_nl_full_body<NT>(a, blockIdx.x, F32, Fb, D, rho, g);
+    row_nl_full_body<NT>(a, blockIdx.x, F32, Fb, D, rho, a.rho_s, g);
 }
 
 template <int NT>
@@ -532,7 +544,7 @@ template <int NT, int PLAN>
 __global__ void __launch_bounds__(nl_threads<NT, PLAN>(), nl_min_blocks<NT, PLAN>())
 k_row_nl(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
          const float *__restrict__ rho, int g) {
-    row_nl_body<NT, PLAN>(a, blockIdx.x, F32, Fb, D, rho, g);
+    row_nl_body<NT, PLAN>(a, blockIdx.x, F32, Fb, D, rho, a.rho_s, g);
 }
 
 template <int NT, int PLAN>
@@ -542,56 +554,51 @@ k_row_next(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ 
     row_next_body<NT, PLAN>(a, blockIdx.x, F32, Fb, D, rho, u_out, write_state, do_scan, apply_mask, g);
 }
 
-// The pulse's table entry staged in shared memory by the whole CTA: the body
-// then reads its arguments from there as it needs them (re-read after each
-// barrier) instead of holding them in registers across the row's passes.
-__device__ __forceinline__ const BatchPulse &stage_pulse(const BatchPulse *__restrict__ P, int i) {
-    __shared__ __align__(16) BatchPulse sq;
-    static_assert(sizeof(BatchPulse) % 4 == 0, "staged as words");
-    const int *src = reinterpret_cast<const int *>(P + i);
-    int *dst = reinterpret_cast<int *>(&sq);
-    for (int k = threadIdx.x; k < (int)(sizeof(BatchPulse) / 4); k += blockDim.x) dst[k] = __ldg(src + k);
-    __syncthreads();
-    return sq;
-}
-
 // ------------------------------------------------------------------ batched (many pulses, one time-grid class)
-// work[b] = (pulse, row) for CTA b; every pulse of the class has the same N_t.
+// work[b] = (pulse, row) for CTA b, the pulse an index into the launch's table
+// T (its arguments, read through the constant cache) and into C (the caller's
+// buffers for this call); every pulse of the class has the same N_t.
 template <int NT>
 __global__ void __launch_bounds__(row_threads<NT>())
-k_row_entry_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int do_scan) {
+k_row_entry_b(const __grid_constant__ PulseTable T, const BatchCall *__restrict__ C, const int2 *__restrict__ work,
+              int do_scan) {
     const int2 w = work[blockIdx.x];
-    const BatchPulse &q = P[w.x];
+    const BatchPulse &q = T.p[w.x];
+    const BatchCall c = C[w.x];
     // exciton channel: its two-population march runs as a kernel of its own
-    row_entry_body<NT>(q.a, w.y, q.u, q.F32, q.Fb, q.rho, do_scan && !q.ste_work);
+    row_entry_body<NT>(q.a, w.y, c.u, q.F32, q.Fb, c.rho, do_scan && !q.ste_work);
 }
 
 template <int NT, int PLAN>
 __global__ void __launch_bounds__(nl_threads<NT, PLAN>(), nl_min_blocks<NT, PLAN>())
-k_row_nl_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
+k_row_nl_b(const __grid_constant__ PulseTable T, const BatchCall *__restrict__ C, const int2 *__restrict__ work,
+           int g) {
     const int2 w = work[blockIdx.x];
-    const BatchPulse &q = stage_pulse(P, w.x);
-    row_nl_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, g);
+    const BatchPulse &q = T.p[w.x];
+    row_nl_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, C[w.x].rho, C[w.x].rho_s, g);
 }
 
 template <int NT, int PLAN>
 __global__ void __launch_bounds__(row_threads<NT>(), row_min_blocks<NT>(true))
-k_row_next_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int last, int g) {
+k_row_next_b(const __grid_constant__ PulseTable T, const BatchCall *__restrict__ C, const int2 *__restrict__ work,
+             int last, int g) {
     const int2 w = work[blockIdx.x];
-    const BatchPulse &q = stage_pulse(P, w.x);
+    const BatchPulse &q = T.p[w.x];
+    const BatchCall c = C[w.x];
     if (q.ste_work)  // exciton channel: hand the physical field to the two-population march
-        row_next_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : q.ste_work, !last, 0, 1, g);
+        row_next_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, c.rho, last ? c.u : q.ste_work, !last, 0, 1, g);
     else
-        row_next_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, last ? q.u : nullptr, !last, !last, 1, g);
+        row_next_body<NT, PLAN>(q.a, w.y, q.F32, q.Fb, q.D, c.rho, last ? c.u : nullptr, !last, !last, 1, g);
 }
 
 // Pulses with the full-physics terms (Raman / self-steepening; one time-grid class).
 template <int NT>
 __global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
-k_row_nl_full_b(const BatchPulse *__restrict__ P, const int2 *__restrict__ work, int g) {
+k_row_nl_full_b(const __grid_constant__ PulseTable T, const BatchCall *__restrict__ C,
+                const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
-    const BatchPulse &q = P[w.x];
-    row_nl_full_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, q.rho, g);
+    const BatchPulse &q = T.p[w.x];
+    row_nl_full_body<NT>(q.a, w.y, q.F32, q.Fb, q.D, C[w.x].rho, C[w.x].rho_s, g);
 }
 
 template <typename K>
@@ -614,8 +621,8 @@ struct RowKernels {
                             cudaStream_t st);
     static cudaError_t nl_full(const RowFusedArgs &a, float *F32, __nv_bfloat16 *Fb, const float *D,
                                const float *rho, int g, cudaStream_t st);
-    static cudaError_t batch(int kind, const BatchPulse *P, const int2 *work, int nblocks, int flag, int g,
-                             int plan, cudaStream_t st);
+    static cudaError_t batch(int kind, const PulseTable &T, const BatchCall *C, const int2 *work, int nblocks,
+                             int flag, int g, int plan, cudaStream_t st);
 };
 
 template <int NT, int PLAN>
@@ -683,8 +690,8 @@ cudaError_t RowKernels<NT>::nl_full(const RowFusedArgs &a, float *F32, __nv_bflo
 }
 
 template <int NT>
-cudaError_t RowKernels<NT>::batch(int kind, const BatchPulse *P, const int2 *work, int nblocks, int flag, int g,
-                                  int plan, cudaStream_t st) {
+cudaError_t RowKernels<NT>::batch(int kind, const PulseTable &T, const BatchCall *C, const int2 *work, int nblocks,
+                                  int flag, int g, int plan, cudaStream_t st) {
     cudaError_t e;
     if (kind == 3) {
         if constexpr (NT > 4096) {
@@ -693,7 +700,7 @@ cudaError_t RowKernels<NT>::batch(int kind, const BatchPulse *P, const int2 *wor
             const size_t smem = full_smem_bytes<NT>();
             e = set_smem(k_row_nl_full_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_full_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(P, work, g);
+            k_row_nl_full_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(T, C, work, g);
             return cudaGetLastError();
         }
     }
@@ -701,30 +708,30 @@ cudaError_t RowKernels<NT>::batch(int kind, const BatchPulse *P, const int2 *wor
     if (kind == 0) {
         e = set_smem(k_row_entry_b<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_entry_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag);
+        k_row_entry_b<NT><<<nblocks, row_threads<NT>(), smem, st>>>(T, C, work, flag);
     } else if (kind == 1) {
         if (plan == 1 && nl_plan1_ok<NT>()) {
             e = set_smem(k_row_nl_b<NT, 1>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_b<NT, 1><<<nblocks, nl_threads<NT, 1>(), smem, st>>>(P, work, g);
+            k_row_nl_b<NT, 1><<<nblocks, nl_threads<NT, 1>(), smem, st>>>(T, C, work, g);
         } else if (plan == 2) {
             e = set_smem(k_row_nl_b<NT, 2>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_b<NT, 2><<<nblocks, nl_threads<NT, 2>(), smem, st>>>(P, work, g);
+            k_row_nl_b<NT, 2><<<nblocks, nl_threads<NT, 2>(), smem, st>>>(T, C, work, g);
         } else {
             e = set_smem(k_row_nl_b<NT, 0>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_b<NT, 0><<<nblocks, nl_threads<NT, 0>(), smem, st>>>(P, work, g);
+            k_row_nl_b<NT, 0><<<nblocks, nl_threads<NT, 0>(), smem, st>>>(T, C, work, g);
         }
     } else {
         if (plan == 1 && next_plan1_ok<NT>()) {
             e = set_smem(k_row_next_b<NT, 1>, smem);
             if (e != cudaSuccess) return e;
-            k_row_next_b<NT, 1><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag, g);
+            k_row_next_b<NT, 1><<<nblocks, row_threads<NT>(), smem, st>>>(T, C, work, flag, g);
         } else {
             e = set_smem(k_row_next_b<NT, 0>, smem);
             if (e != cudaSuccess) return e;
-            k_row_next_b<NT, 0><<<nblocks, row_threads<NT>(), smem, st>>>(P, work, flag, g);
+            k_row_next_b<NT, 0><<<nblocks, row_threads<NT>(), smem, st>>>(T, C, work, flag, g);
         }
     }
     return cudaGetLastError();

@@ -1089,7 +1089,8 @@ struct nlse_batch {
     cudaStream_t cap_stream, cap_stream2;
     cudaEvent_t cap_fork, cap_join;
     cudaGraphExec_t graph;
-    int graph_key[5];        // (variant, a_terms, f16, buffer generation, row-plan generation) it was captured for
+    int graph_key[6];        // (variant, a_terms, f16, buffer generation, row-plan generation, table
+                             // generation) it was captured for
     int graph_off;           // capture failed once: launch directly
     nlse_ctx **ctx;          // one context per pulse (tables, operator, state buffers)
     BatchPulse *h_pulses;    // pinned staging of the per-pulse table
@@ -1103,9 +1104,15 @@ struct nlse_batch {
     struct Class {
         int logNt, nblocks;
         int full;            // its pulses have the full-physics terms (row_nl kind 3)
-        int2 *d_work;
+        int2 *d_work;        // (index into tab / the class's calls, row) per CTA
         int split;           // work entries of lane 0 (pulses [0, lane_pulse))
+        int npulse, call0;   // its pulses; their BatchCall entries start at d_calls + call0
+        int pulse[NLSE_TABLE_PULSES];  // the batch's index of each
+        PulseTable *tab;     // the row launches' parameter table (host; copied into each launch)
     } cls[32];
+    BatchCall *h_calls;      // pinned staging of the caller's buffers per pulse, class by class
+    BatchCall *d_calls;
+    int tab_gen;             // bumped whenever the class tables change (a captured graph holds a copy)
     // pulses with the exciton channel: their two-population march runs as a
     // kernel of its own after row_next (its pointers are launch arguments, so
     // a change of buffers re-captures the graph: ptr_gen)
@@ -1133,11 +1140,14 @@ static void batch_free(nlse_batch *b) {
     free(b->ste_idx);
     free(b->stf_idx);
     if (b->h_pulses) cudaFreeHost(b->h_pulses);
-    void *ptrs[] = {b->d_pulses, b->d_maps, b->d_tiles, b->d_flag};
+    if (b->h_calls) cudaFreeHost(b->h_calls);
+    void *ptrs[] = {b->d_pulses, b->d_calls, b->d_maps, b->d_tiles, b->d_flag};
     for (void *p : ptrs)
         if (p) cudaFree(p);
-    for (int c = 0; c < b->ncls; ++c)
+    for (int c = 0; c < b->ncls; ++c) {
         if (b->cls[c].d_work) cudaFree(b->cls[c].d_work);
+        free(b->cls[c].tab);
+    }
     if (b->staged) cudaEventDestroy(b->staged);
     if (b->done) cudaEventDestroy(b->done);
     if (b->graph) cudaGraphExecDestroy(b->graph);
@@ -1220,8 +1230,9 @@ static cudaError_t batch_zstep(nlse_batch *b, int g, int last, int lane, cudaStr
                                     : (lane == 0 ? b->cls[k].split : b->cls[k].nblocks - b->cls[k].split);
             const int kind = half == 1 ? 2 : (b->cls[k].full ? 3 : 1);
             if (nw > 0)
-                e = launch_row_batch(kind, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work + w0, nw,
-                                     half == 0 ? 0 : last, g + half, batch_plan(b->cls[k].logNt, kind), st);
+                e = launch_row_batch(kind, b->cls[k].logNt, *b->cls[k].tab, b->d_calls + b->cls[k].call0,
+                                     b->cls[k].d_work + w0, nw, half == 0 ? 0 : last, g + half,
+                                     batch_plan(b->cls[k].logNt, kind), st);
         }
     }
     if (e == cudaSuccess && !last) e = batch_ste_marches(b, lane, st);
@@ -1231,8 +1242,8 @@ static cudaError_t batch_zstep(nlse_batch *b, int g, int last, int lane, cudaStr
 // The graph of three non-final z-steps for the batch's current launch
 // configuration; NULL (and direct launches from then on) if capture fails.
 static cudaGraphExec_t batch_graph(nlse_batch *b) {
-    const int key[5] = {b->ctx[0]->gemm_variant, b->a_terms, b->f16, b->nste ? b->ptr_gen : 0,
-                        row_plan_generation()};
+    const int key[6] = {b->ctx[0]->gemm_variant, b->a_terms, b->f16, b->nste ? b->ptr_gen : 0,
+                        row_plan_generation(), b->tab_gen};
     if (b->graph && !memcmp(key, b->graph_key, sizeof(key))) return b->graph;
     if (b->graph_off) return nullptr;
     if (b->graph) {
@@ -1309,6 +1320,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
     std::vector<CUtensorMap> maps(4 * (size_t)n);
     int logs[32], fulls[32], nlog = 0;
     std::vector<std::vector<int2>> work(32);
+    std::vector<std::vector<int>> members(32);
     std::vector<int> ste;
     for (int i = 0; i < n; ++i) {
         nlse_ctx *c = b->ctx[i];
@@ -1330,14 +1342,22 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         for (int m0 = 0; m0 < M; m0 += 128)
             for (int n0 = 0; n0 < c->Nt; n0 += 256) (c->stf ? stf_tiles : tiles).push_back(GemmTile{i, m0, n0, 0});
         if (c->stf) stf.push_back(i);
-        // row classes: one per (N_t, full-physics terms)
+        // row classes: one per (N_t, full-physics terms), of at most
+        // NLSE_TABLE_PULSES pulses (the parameter table of a row launch)
         int k = 0;
-        while (k < nlog && (logs[k] != c->logNt || fulls[k] != c->full_nl)) ++k;
+        while (k < nlog && (logs[k] != c->logNt || fulls[k] != c->full_nl ||
+                            (int)members[k].size() >= NLSE_TABLE_PULSES))
+            ++k;
         if (k == nlog) {
+            if (nlog == 32)
+                BATCH_FAIL(NLSE_ERR_UNSUPPORTED, "batch: more than 32 row classes (time grid x physics terms, %d pulses each)",
+                           NLSE_TABLE_PULSES);
             logs[nlog] = c->logNt;
             fulls[nlog++] = c->full_nl;
         }
-        for (int r = 0; r < c->Nr; ++r) work[k].push_back(make_int2(i, r));
+        const int j = (int)members[k].size();
+        members[k].push_back(i);
+        for (int r = 0; r < c->Nr; ++r) work[k].push_back(make_int2(j, r));
         if (c->sc.ste) ste.push_back(i);
     }
     b->nste = (int)ste.size();
@@ -1378,17 +1398,25 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
         e = cudaMemcpy(b->d_maps, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_pulses, n * sizeof(BatchPulse));
     if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_pulses, n * sizeof(BatchPulse));
+    if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_calls, n * sizeof(BatchCall));
+    if (e == cudaSuccess) e = cudaMallocHost((void **)&b->h_calls, n * sizeof(BatchCall));
     if (e == cudaSuccess) e = cudaMalloc((void **)&b->d_flag, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(b->d_flag, 0, 4 * sizeof(int));
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->staged, cudaEventDisableTiming);
     if (e == cudaSuccess) e = cudaEventCreateWithFlags(&b->done, cudaEventDisableTiming);
     b->ncls = nlog;
-    for (int k = 0; k < nlog && e == cudaSuccess; ++k) {
+    for (int k = 0, call0 = 0; k < nlog && e == cudaSuccess; ++k) {
         b->cls[k].logNt = logs[k];
         b->cls[k].full = fulls[k];
         b->cls[k].nblocks = (int)work[k].size();
+        b->cls[k].npulse = (int)members[k].size();
+        b->cls[k].call0 = call0;
+        call0 += b->cls[k].npulse;
+        for (int j = 0; j < b->cls[k].npulse; ++j) b->cls[k].pulse[j] = members[k][j];
+        b->cls[k].tab = (PulseTable *)calloc(1, sizeof(PulseTable));
+        if (!b->cls[k].tab) e = cudaErrorMemoryAllocation;
         b->cls[k].split = 0;
-        for (const int2 &w : work[k]) b->cls[k].split += w.x < b->lane_pulse;
+        for (const int2 &w : work[k]) b->cls[k].split += members[k][w.x] < b->lane_pulse;
         e = cudaMalloc((void **)&b->cls[k].d_work, work[k].size() * sizeof(int2));
         if (e == cudaSuccess)
             e = cudaMemcpy(b->cls[k].d_work, work[k].data(), work[k].size() * sizeof(int2), cudaMemcpyHostToDevice);
@@ -1483,8 +1511,10 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
                             b->h_pulses[i].a.rho_s != rs_i))
             changed = true;
     }
+    // the row launches' parameter tables hold everything but the caller's buffers
+    const bool tab_changed = !(dz == b->last_dz) || !b->uploaded || b->last_f16 != b->f16;
     if (changed) {
-        // the previous upload must be consumed before the staging buffer is rewritten
+        // the previous upload must be consumed before the staging buffers are rewritten
         NLSE_CUDA_TRY(&b->err, cudaEventSynchronize(b->staged));
         for (int i = 0; i < b->n; ++i) {
             nlse_ctx *q = b->ctx[i];
@@ -1502,7 +1532,22 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
             P.K = 2 * q->Nrp;
             P.kdiag = q->stf;
         }
+        for (int k = 0; k < b->ncls; ++k)
+            for (int j = 0; j < b->cls[k].npulse; ++j) {
+                const BatchPulse &P = b->h_pulses[b->cls[k].pulse[j]];
+                b->h_calls[b->cls[k].call0 + j] = BatchCall{P.u, P.rho, P.a.rho_s, nullptr};
+                if (tab_changed) {
+                    BatchPulse &E = b->cls[k].tab->p[j];
+                    E = P;
+                    E.u = nullptr;
+                    E.rho = nullptr;
+                    E.a.rho_s = nullptr;
+                }
+            }
+        if (tab_changed) ++b->tab_gen;
         NLSE_CUDA_TRY(&b->err, cudaMemcpyAsync(b->d_pulses, b->h_pulses, b->n * sizeof(BatchPulse),
+                                               cudaMemcpyHostToDevice, st));
+        NLSE_CUDA_TRY(&b->err, cudaMemcpyAsync(b->d_calls, b->h_calls, b->n * sizeof(BatchCall),
                                                cudaMemcpyHostToDevice, st));
         NLSE_CUDA_TRY(&b->err, cudaEventRecord(b->staged, st));
         b->last_dz = dz;
@@ -1535,7 +1580,8 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
     if (b->nste) BSEQ(K_RATE_SCAN, batch_ste_marches_on(b, u, st), "batch exciton march");
     for (int k = 0; k < b->ncls; ++k)
         BSEQ(K_ROW_ENTRY,
-             launch_row_batch(0, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, 1, -1, 0, st),
+             launch_row_batch(0, b->cls[k].logNt, *b->cls[k].tab, b->d_calls + b->cls[k].call0, b->cls[k].d_work,
+                              b->cls[k].nblocks, 1, -1, 0, st),
              "batch row entry");
     int it = 0;
     // the bulk of the non-final steps as graph launches of three steps each
@@ -1550,15 +1596,16 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
         BSEQ(K_GEMM_TC, batch_products(b, 2 * it, -1, st), "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NL,
-                 launch_row_batch(b->cls[k].full ? 3 : 1, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work,
-                                  b->cls[k].nblocks, 0, 2 * it, batch_plan(b->cls[k].logNt, b->cls[k].full ? 3 : 1),
-                                  st),
+                 launch_row_batch(b->cls[k].full ? 3 : 1, b->cls[k].logNt, *b->cls[k].tab,
+                                  b->d_calls + b->cls[k].call0, b->cls[k].d_work, b->cls[k].nblocks, 0, 2 * it,
+                                  batch_plan(b->cls[k].logNt, b->cls[k].full ? 3 : 1), st),
                  "batch row nonlinear");
         BSEQ(K_GEMM_TC, batch_products(b, 2 * it + 1, -1, st), "batch gemm");
         for (int k = 0; k < b->ncls; ++k)
             BSEQ(K_ROW_NEXT,
-                 launch_row_batch(2, b->cls[k].logNt, b->d_pulses, b->cls[k].d_work, b->cls[k].nblocks, last,
-                                  2 * it + 1, batch_plan(b->cls[k].logNt, 2), st),
+                 launch_row_batch(2, b->cls[k].logNt, *b->cls[k].tab, b->d_calls + b->cls[k].call0,
+                                  b->cls[k].d_work, b->cls[k].nblocks, last, 2 * it + 1,
+                                  batch_plan(b->cls[k].logNt, 2), st),
                  "batch row next");
         if (!last && b->nste) BSEQ(K_RATE_SCAN, batch_ste_marches(b, -1, st), "batch exciton march");
     }

@@ -128,6 +128,29 @@ struct BatchPulse {
                   // block b takes only the K range of block b
 };
 
+// The pulses of one batched row launch (one time-grid class, at most
+// NLSE_TABLE_PULSES of them), passed by value as a __grid_constant__ kernel
+// parameter: the row kernels read their pulse's arguments (physics constants,
+// table pointers) through the constant cache, as the single-pulse kernels
+// read theirs, instead of re-reading a copy in shared memory at every use
+// (those reloads took a third of k_row_nl's shared-memory wavefronts).  The
+// pointers to the caller's buffers (u, rho, rho_s) change from call to call;
+// they are zero here and come from the class's BatchCall array in device
+// memory, so a captured graph stays valid when only they change.
+#define NLSE_TABLE_PULSES 64
+struct PulseTable {
+    BatchPulse p[NLSE_TABLE_PULSES];
+};
+static_assert(sizeof(PulseTable) + 64 <= 32764, "a kernel's parameters are limited to 32764 bytes");
+
+// The caller's buffers of one pulse for one call (device memory, indexed like PulseTable).
+struct BatchCall {
+    float2 *u;
+    float *rho;
+    const float *rho_s;  // exciton density (channel on) or NULL
+    void *pad;
+};
+
 // One 128 x 256 tile of the grouped tensor-core product.
 struct GemmTile {
     int pulse, m0, n0, pad;
@@ -274,9 +297,9 @@ cudaError_t launch_split_field(const float *w, __nv_bfloat16 *hi, size_t lo_off,
 // kind 0 = entry (flag = do_scan), 1 = nonlinear, 2 = next (flag = last step of the call),
 // 3 = nonlinear with the full-physics block (N_t <= 4096);
 // g = index of the GEMM input the kernel consumes (the split-FP16 scales; -1 for the entry);
-// plan = the row plan of kinds 1 and 2 (0 or 1, see row_plan)
-cudaError_t launch_row_batch(int kind, int logNt, const BatchPulse *P, const int2 *work, int nblocks, int flag,
-                             int g, int plan, cudaStream_t st);
+// plan = the row plan of kinds 1 and 2 (see row_plan); work[b] = (index into T and calls, row)
+cudaError_t launch_row_batch(int kind, int logNt, const PulseTable &T, const BatchCall *calls, const int2 *work,
+                             int nblocks, int flag, int g, int plan, cudaStream_t st);
 cudaError_t launch_gemm_tc_grouped(const CUtensorMap *maps, const BatchPulse *P, const GemmTile *tiles, int ntiles,
                                    int a_terms, int variant, int f16, int *err, cudaStream_t stream);
 cudaError_t launch_row_entry(const RowFusedArgs &a, const float2 *u, float *F32, __nv_bfloat16 *Fb, float *rho,

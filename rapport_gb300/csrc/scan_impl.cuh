@@ -264,6 +264,110 @@ static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ
     __syncthreads();
 }
 
+// The scan layout of an NT-point row marched by T threads, at compile time
+// (the fused row kernels know both): C steps per thread, row stride S.
+template <int NT, int T>
+struct ScanShape {
+    static constexpr int C = (NT - 1 + T - 1) / T;
+    static constexpr int logC = C >= 16 ? 4 : (C >= 8 ? 3 : (C >= 4 ? 2 : (C >= 2 ? 1 : 0)));
+    static constexpr int S = T + scan_pad(C);
+    static_assert((1 << logC) == C, "C is a power of two for power-of-two NT and T");
+    __device__ __forceinline__ static int slot(int n) { return (n & (C - 1)) * S + (n >> logC); }
+};
+
+// scan_row for an NT-point row and T = blockDim.x threads known at compile
+// time: the same iterations, step maps and roundings (results are identical),
+// with the thread's C steps unrolled -- the slots are constant offsets, each
+// step's right-hand intensity, rate and iterate are the next step's left-hand
+// ones, and the affine maps of the sweep stay in registers between the scan
+// and the update instead of passing through shared memory.
+template <int NT, int T>
+static __device__ void scan_row_ct(const float *sI, float *sW, float *sx, const ScanParams &p,
+                                   const float *__restrict__ lut, float x0, int *stats) {
+    using Sh = ScanShape<NT, T>;
+    constexpr int C = Sh::C, S = Sh::S;
+    __shared__ Aff wsum[32];
+    __shared__ float red[100];
+    const int tid = threadIdx.x;
+    for (int t = tid; t < NT; t += T) {
+        const int q = Sh::slot(t);
+        sW[q] = lut_rate_dt(sI[q], lut, p);
+        sx[q] = t == 0 ? x0 : 0.0f;
+    }
+    __syncthreads();
+    // the thread's steps n0 .. n0 + nst - 1 at slots j S + tid; the step after
+    // its last is the next thread's first (slot tid + 1)
+    const int n0 = min(tid * C, NT - 1), nst = min(n0 + C, NT - 1) - n0;
+    int converged = 0, clamp_any = 0;
+    for (int it = 0; it < SCAN_MAX_IT; ++it) {
+        float J[C], B[C];
+        Aff acc{1.0f, 0.0f};
+        bool cl = false;
+        float I0 = 0.0f, W0 = 0.0f, xn = 0.0f;
+        if (nst > 0) {
+            I0 = sI[tid];
+            W0 = sW[tid];
+            xn = sx[tid];
+        }
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+            if (j < nst) {
+                const int q1 = j + 1 < C ? (j + 1) * S + tid : tid + 1;
+                const float I1 = sI[q1], W1 = sW[q1];
+                float Ia = 0.5f * (I0 + I1);
+                float b = 0.5f * (W0 + W1);
+                float Jv = 0.0f, F = 0.0f;
+                if (isfinite(Ia)) F = step_map(xn, p.a_coef * Ia, b, p, &Jv, &cl);
+                const float Bv = fmaf(-Jv, xn, F);
+                J[j] = Jv;
+                B[j] = Bv;
+                acc = aff_then(acc, Aff{Jv, Bv});
+                I0 = I1;
+                W0 = W1;
+                xn = sx[q1];
+            }
+        }
+        Aff pre = block_exclusive_scan(acc, wsum);
+        float xs = fmaf(pre.A, x0, pre.B);
+        float dmax = 0.0f, xmax = 0.0f;
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+            if (j < nst) {
+                const int q1 = j + 1 < C ? (j + 1) * S + tid : tid + 1;
+                xs = fmaf(J[j], xs, B[j]);
+                dmax = fmaxf(dmax, fabsf(xs - sx[q1]));
+                xmax = fmaxf(xmax, fabsf(xs));
+                sx[q1] = xs;
+            }
+        }
+        int f = cl ? 1 : 0;
+        block_reduce(dmax, xmax, f, red);
+        clamp_any |= f;
+        if (clamp_any) break;
+        if (dmax <= SCAN_TOL * xmax || (it == 0 && xmax < p.x_tiny)) {
+            converged = 1;
+            break;
+        }
+    }
+    if (!converged) {
+        // exact sequential march (saturated or non-converging row)
+        if (tid == 0) {
+            float x = x0;
+            bool cl = false;
+            for (int n = 0; n < NT - 1; ++n) {
+                const int q0 = Sh::slot(n), q1 = Sh::slot(n + 1);
+                float Ia = 0.5f * (sI[q0] + sI[q1]);
+                float b = 0.5f * (sW[q0] + sW[q1]);
+                float Jv;
+                x = isfinite(Ia) ? step_map(x, p.a_coef * Ia, b, p, &Jv, &cl) : 0.0f;
+                sx[q1] = x;
+            }
+            if (stats) atomicAdd(&stats[1], 1);
+        }
+    }
+    __syncthreads();
+}
+
 // ------------------------------------------------------------------ two populations (self-trapped excitons)
 // With the exciton channel on, the reference march (kernels.py:72-95) advances
 // (e, s) = (rho_e, rho_s) by
