@@ -298,7 +298,11 @@ __device__ __forceinline__ void row_next_regs(const RowFusedArgs &a, int r, floa
     load_mw_regs<NT, T>(v, r, a, F32, D, apply_mask ? __ldg(&a.mask_r[r]) : 1.0f, g);
     if (write_state) store_state_regs<NT, T>(v, r, a, F32, Fb, g + 1);
     if (!do_scan && !u_out) return;
-    float2 *F = fft_regs<NT, true, row_threads<NT>()>(v, A, B, a.tw);
+    // a physical field that only feeds the march (rebuilt from it every z-step)
+    // takes plain twiddle products (see apply_twiddles); one handed to the
+    // caller (the state of the next call) the compensated ones
+    float2 *F = u_out ? fft_regs<NT, true, row_threads<NT>(), true>(v, A, B, a.tw)
+                      : fft_regs<NT, true, row_threads<NT>(), false>(v, A, B, a.tw);
     const float inv = 1.0f / (float)NT;
     if (u_out) {
         float2 *gu = u_out + (size_t)r * NT;
@@ -491,7 +495,9 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
     __syncthreads();
     if (write_state) store_state_row<NT>(b0, r, a, F32, Fb, g + 1);
     if (!do_scan && !u_out) return;
-    float2 *R = fft_row<NT, true, row_threads<NT>()>(b0, b1, a.tw);
+    // plain twiddle products when the physical field only feeds the march (as in row_next_regs)
+    float2 *R = u_out ? fft_row<NT, true, row_threads<NT>(), true>(b0, b1, a.tw)
+                      : fft_row<NT, true, row_threads<NT>(), false>(b0, b1, a.tw);
     const float inv = 1.0f / (float)NT;
     if (u_out) {
         float2 *g = u_out + (size_t)r * NT;

@@ -44,15 +44,16 @@ __device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p
                                           const float4 *__restrict__ tab, float *raw) {
     float photo = 0.0f;
     if (p.photo_on) {
-        float I = a2 * p.invE2;
-        if (isfinite(I)) {
-            if (!(I < p.I_skip)) {
+        const float I = a2 * p.invE2;
+        // one test on the common path (a finite I below I_skip); NaN fails it too
+        if (!(I < p.I_skip)) {
+            if (isfinite(I)) {
                 float dep = fminf(fmaxf((p.rho_max - rho) * p.inv_rho_max, 0.0f), 1.0f);
                 photo = photo_rate(I, p, tab) * dep;
-            }
-        } else if (isnan(I)) {
-            photo = I;  // NaN: split() turns the sum into alpha = 0 (nan_to_num)
-        }             // +Inf: W(Imax) / Inf = 0 in split()
+            } else if (isnan(I)) {
+                photo = I;  // NaN: split() turns the sum into alpha = 0 (nan_to_num)
+            }             // +Inf: W(Imax) / Inf = 0 in split()
+        }
     }
     float ar = fmaf(p.pp_abs, rho, photo);
     *raw = ar;
@@ -63,7 +64,6 @@ __device__ __forceinline__ float alpha_of(float a2, float rho, const NLParams &p
 __device__ __forceinline__ float2 nl_rhs(float2 u, float rho, float rho_s, const NLParams &p,
                                          const float4 *__restrict__ tab) {
     float a2 = fmaf(u.x, u.x, u.y * u.y);
-    if (!(a2 >= 1e-30f)) return make_float2(0.0f, 0.0f);  // also NaN
     float w = fmaf(p.kp, a2, fmaf(p.ste_pref, rho_s, -p.pp_def * rho));  // i w u
     float corr = 0.0f;
     if (rho < 0.0f) {
@@ -72,8 +72,10 @@ __device__ __forceinline__ float2 nl_rhs(float2 u, float rho, float rho_s, const
         corr = isfinite(raw) ? al - raw : 0.0f;
     }
     float2 r = make_float2(fmaf(corr, u.x, -w * u.y), fmaf(corr, u.y, w * u.x));
-    if (!isfinite(r.x) || !isfinite(r.y)) r = make_float2(0.0f, 0.0f);
-    return r;
+    // zero below |u|^2 = 1e-30 (also NaN) and for a non-finite result, as a
+    // select rather than an early return
+    const bool keep = a2 >= 1e-30f && isfinite(r.x) && isfinite(r.y);
+    return keep ? r : make_float2(0.0f, 0.0f);
 }
 
 __device__ __forceinline__ float2 nl_point(float2 u, float rho, float rho_s, float dz, const NLParams &p,

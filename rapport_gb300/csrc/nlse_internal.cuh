@@ -467,8 +467,10 @@ __host__ __device__ constexpr int fft_tw_size(int N) { return fft_tw_offset(N, N
 
 // Twiddle products of butterfly k of the pass at NS (radix R) of an N-point
 // row: v[r] *= exp(-+ 2 pi i r k (N / (NS R)) / N), r = 1 .. R-1, from table
-// row k of the pass (and its rounding remainders).
-template <int R, bool INV, int N, int NS>
+// row k of the pass (and its rounding remainders).  COMP = false: plain
+// products with the FP32 table, for a transform whose output is not carried
+// from z-step to z-step (its fixed rounding then does not add up).
+template <int R, bool INV, int N, int NS, bool COMP = true>
 __device__ __forceinline__ void apply_twiddles(float2 *v, int k, const float2 *__restrict__ tw) {
     const float4 *w4 = reinterpret_cast<const float4 *>(tw + fft_tw_offset(N, NS)) + k;
     float2 w[fft_tw_row(R)];
@@ -477,6 +479,15 @@ __device__ __forceinline__ void apply_twiddles(float2 *v, int k, const float2 *_
         const float4 p = __ldg(&w4[q * NS]);
         w[2 * q] = make_float2(p.x, p.y);
         w[2 * q + 1] = make_float2(p.z, p.w);
+    }
+    if constexpr (!COMP || !NLSE_COMP_TWIDDLE) {
+#pragma unroll
+        for (int r = 1; r < R; ++r) {
+            float2 x = w[r - 1];
+            if (INV) x.y = -x.y;
+            v[r] = c_mul(v[r], x);
+        }
+        return;
     }
 #if NLSE_COMP_TWIDDLE
     // the table's rounding remainders follow the table
@@ -514,7 +525,7 @@ __device__ __forceinline__ void apply_twiddles(float2 *v, int k, const float2 *_
 // One Stockham autosort pass of radix R over a row of N points (compile-time
 // sizes): reads src, writes dst (padded indexing).  NS = product of the
 // radices already applied; tw = the twiddle table above.
-template <int R, bool INV, int N, int NS, int T>
+template <int R, bool INV, int N, int NS, int T, bool COMP = true>
 __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, float2 *__restrict__ dst,
                                               const float2 *__restrict__ tw) {
     constexpr int nb = N / R;
@@ -526,7 +537,7 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
             float2 v[R];
 #pragma unroll
             for (int r = 0; r < R; ++r) v[r] = src[pidx(j + r * nb)];
-            if (NS > 1) apply_twiddles<R, INV, N, NS>(v, k, tw);
+            if (NS > 1) apply_twiddles<R, INV, N, NS, COMP>(v, k, tw);
             dft_small<R, INV>(v);
             const int d0 = (j - k) * R + k;
 #pragma unroll
@@ -536,24 +547,24 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
 }
 
 // Remaining passes from NS on.
-template <int N, int NS, bool INV, int T>
+template <int N, int NS, bool INV, int T, bool COMP = true>
 __device__ __forceinline__ float2 *fft_passes(float2 *src, float2 *dst, const float2 *__restrict__ tw) {
     if constexpr (NS >= N) {
         return src;
     } else {
         constexpr int R = fft_radix(N, NS);
-        stockham_pass<R, INV, N, NS, T>(src, dst, tw);
+        stockham_pass<R, INV, N, NS, T, COMP>(src, dst, tw);
         __syncthreads();
-        return fft_passes<N, NS * R, INV, T>(dst, src, tw);
+        return fft_passes<N, NS * R, INV, T, COMP>(dst, src, tw);
     }
 }
 
 // Full in-CTA FFT of one row of N points (power of two, 16..8192) held in
 // buf0 (padded indexing), buf1 = scratch of the same size; returns the buffer
 // holding the unnormalised result.  Every thread of the CTA (T of them) calls it.
-template <int N, bool INV, int T = NLSE_ROW_THREADS>
+template <int N, bool INV, int T = NLSE_ROW_THREADS, bool COMP = true>
 __device__ __forceinline__ float2 *fft_row(float2 *buf0, float2 *buf1, const float2 *__restrict__ tw) {
-    return fft_passes<N, 1, INV, T>(buf0, buf1, tw);
+    return fft_passes<N, 1, INV, T, COMP>(buf0, buf1, tw);
 }
 
 // ------------------------------------------------ compact row FFT (one pass body)
@@ -722,7 +733,7 @@ __host__ __device__ constexpr bool fft_regs_ok() {
     return passes >= 3;  // at least two exchanges (see fft_regs)
 }
 
-template <int N, int NS, bool INV, int T>
+template <int N, int NS, bool INV, int T, bool COMP = true>
 __device__ __forceinline__ float2 *fft_regs_pass(float2 (&v)[N / T], float2 *src, float2 *dst,
                                                  const float2 *__restrict__ tw) {
     constexpr int P = N / T, R = fft_radix(N, NS), Q = P / R, nb = N / R;
@@ -735,7 +746,7 @@ __device__ __forceinline__ float2 *fft_regs_pass(float2 (&v)[N / T], float2 *src
         float2 y[R];
 #pragma unroll
         for (int r = 0; r < R; ++r) y[r] = first ? v[q + r * Q] : src[pidx(j + r * nb)];
-        if (NS > 1) apply_twiddles<R, INV, N, NS>(y, k, tw);
+        if (NS > 1) apply_twiddles<R, INV, N, NS, COMP>(y, k, tw);
         dft_small<R, INV>(y);
         if constexpr (last) {
 #pragma unroll
@@ -748,7 +759,7 @@ __device__ __forceinline__ float2 *fft_regs_pass(float2 (&v)[N / T], float2 *src
     }
     if constexpr (!last) {
         __syncthreads();
-        return fft_regs_pass<N, NS * R, INV, T>(v, dst, src, tw);
+        return fft_regs_pass<N, NS * R, INV, T, COMP>(v, dst, src, tw);
     } else {
         return dst;
     }
@@ -758,11 +769,11 @@ __device__ __forceinline__ float2 *fft_regs_pass(float2 (&v)[N / T], float2 *src
 // without a barrier, so no thread may still read A.  Returns a buffer that was
 // last read before the final barrier: free to write at once (the other one
 // only after a barrier).
-template <int N, bool INV, int T = NLSE_ROW_THREADS>
+template <int N, bool INV, int T = NLSE_ROW_THREADS, bool COMP = true>
 __device__ __forceinline__ float2 *fft_regs(float2 (&v)[N / T], float2 *A, float2 *B,
                                             const float2 *__restrict__ tw) {
     static_assert(fft_regs_ok<N, T>(), "row length not supported by the register FFT");
-    return fft_regs_pass<N, 1, INV, T>(v, B, A, tw);
+    return fft_regs_pass<N, 1, INV, T, COMP>(v, B, A, tw);
 }
 
 // Entry e (a float2 index) of the twiddle table of an N-point row (host or
