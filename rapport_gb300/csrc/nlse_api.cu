@@ -162,6 +162,20 @@ static int check_desc(const nlse_grid_desc *d, nlse_error_slot *err) {
     return NLSE_OK;
 }
 
+// Intensity below which lut_rate_dt's interpolation reads two zero entries of
+// the W * dt table l (uniform in log10 I from log_min, inv_dlog entries per
+// decade), so the rate is exactly 0: half a table interval below the point
+// where the first nonzero entry starts to count.  The margin is ~1e3 times the
+// FP32 error of the device's table position.  0 when the table starts nonzero;
+// infinity when it is zero throughout.
+static float lut_zero_below(const std::vector<float> &l, double log_min, double inv_dlog) {
+    size_t k0 = 0;
+    while (k0 < l.size() && l[k0] == 0.0f) ++k0;
+    if (k0 >= l.size()) return INFINITY;
+    if (k0 < 2) return 0.0f;
+    return (float)pow(10.0, log_min + ((double)k0 - 1.5) / inv_dlog);
+}
+
 extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
     nlse_error_slot *gerr = &g_create_err;
     gerr->status = NLSE_OK;
@@ -304,6 +318,8 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
             l[k] = (float)v;
         }
         NLSE_TRY(dev_upload(err, &c->d_lut_dt, l.data(), d->lut_n));
+        c->sc.I_w0 = lut_zero_below(l, d->lut_log_min, d->lut_inv_dlog);
+        c->sc.I_w0s = 0.0f;
         if (d->flags & NLSE_F_STE) {
             for (int k = 0; k < d->lut_n; ++k) {
                 double v = d->lut_s[k] * d->dt;
@@ -312,6 +328,7 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
                 l[k] = (float)v;
             }
             NLSE_TRY(dev_upload(err, &c->d_lut_s_dt, l.data(), d->lut_n));
+            c->sc.I_w0s = lut_zero_below(l, d->lut_log_min, d->lut_inv_dlog);
         }
     }
     c->full_nl = (d->flags & (NLSE_F_KERR_RAMAN | NLSE_F_SELF_STEEP | NLSE_F_SPACE_TIME)) != 0;

@@ -69,6 +69,8 @@ struct ScanParams {
     float cs_ste;       // dt / tau_ste
     float lut_log_min, lut_inv_dlog, Imin, Imax;
     int lut_n;
+    float I_w0, I_w0s;  // below these intensities the W * dt tables (electrons, excitons) interpolate
+                        // between two zero entries: the rate is exactly 0 (0: no such range)
 };
 
 // Arguments of the fused row kernels (k_rowfused.cu).

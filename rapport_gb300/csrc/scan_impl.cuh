@@ -17,8 +17,12 @@ __device__ __forceinline__ Aff aff_then(Aff first, Aff second) {
 }
 
 // W(I) * dt, linear in log10 I on the uniform table (kernels.py:14-26).
-__device__ __forceinline__ float lut_rate_dt(float I, const float *__restrict__ lut, const ScanParams &p) {
+// I_zero: below it the table's entries on both sides are zero and so is the
+// result, without the logarithm and the table reads.
+__device__ __forceinline__ float lut_rate_dt(float I, const float *__restrict__ lut, float I_zero,
+                                             const ScanParams &p) {
     if (!isfinite(I) || I < 0.0f) I = 0.0f;
+    if (I < I_zero) return 0.0f;
     I = fminf(fmaxf(I, p.Imin), p.Imax);
     // log10 from the hardware log2 (~2^-22 relative): it moves the interpolation
     // weight by ~1e-5 of one of the table's 0.004-decade intervals
@@ -190,6 +194,16 @@ __host__ __device__ __forceinline__ constexpr int scan_span(int Nt, int threads)
 // sB are scratch of scan_span(Nt) floats each (may alias any other buffer the
 // caller no longer needs).  On return (synced) sx[slot of t] holds the density
 // at t, sx[slot 0] = x0.  C = chunk of steps per thread = ceil((Nt-1)/blockDim).
+// Whether a point keeps a row's march from being skipped.  With x0 = 0 and
+// W = 0 at every point, every step maps 0 to exactly 0 (y = 0 + e^z 0 + 0),
+// every affine map has B = +0 and the row's densities are +0 -- provided the
+// products of the maps' A = e^z stay finite, which (Nt - 1) a_coef I < 64 at
+// every point guarantees (z <= a_coef I_avg).  Such a row (most rows, away
+// from the beam) skips the sweeps; the result is the same bit for bit.
+__device__ __forceinline__ int march_needed(float W, float I, int Nt, const ScanParams &p) {
+    return W != 0.0f || !((float)(Nt - 1) * (p.a_coef * I) < 64.0f);
+}
+
 static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ, float *sB, int Nt,
                                 const ScanParams &p, const float *__restrict__ lut, float x0, int *stats) {
     __shared__ Aff wsum[32];
@@ -197,12 +211,15 @@ static __device__ void scan_row(const float *sI, float *sW, float *sx, float *sJ
     const int T = Nt - 1;
     const ScanLayout L = scan_layout(Nt);
     const int C = L.C;
+    int need = 0;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
         const int q = scan_slot(t, L);
-        sW[q] = lut_rate_dt(sI[q], lut, p);
+        sW[q] = lut_rate_dt(sI[q], lut, p.I_w0, p);
         sx[q] = t == 0 ? x0 : 0.0f;
+        need |= march_needed(sW[q], sI[q], Nt, p);
     }
-    __syncthreads();
+    // a row without ionisation and carriers stays at exactly zero (see march_needed)
+    if (!__syncthreads_or(need) && x0 == 0.0f) return;
     // the thread's chunk: steps n0 .. n1-1 at slots j S + tid; the step after
     // the chunk's last is the next thread's first (slot tid + 1)
     const int n0 = min((int)threadIdx.x * C, T), n1 = min(n0 + C, T);
@@ -289,12 +306,16 @@ static __device__ void scan_row_ct(const float *sI, float *sW, float *sx, const 
     __shared__ Aff wsum[32];
     __shared__ float red[100];
     const int tid = threadIdx.x;
+    int need = 0;
     for (int t = tid; t < NT; t += T) {
         const int q = Sh::slot(t);
-        sW[q] = lut_rate_dt(sI[q], lut, p);
+        const float w = lut_rate_dt(sI[q], lut, p.I_w0, p);
+        sW[q] = w;
         sx[q] = t == 0 ? x0 : 0.0f;
+        need |= march_needed(w, sI[q], NT, p);
     }
-    __syncthreads();
+    // a row without ionisation and carriers stays at exactly zero (see march_needed)
+    if (!__syncthreads_or(need) && x0 == 0.0f) return;
     // the thread's steps n0 .. n0 + nst - 1 at slots j S + tid; the step after
     // its last is the next thread's first (slot tid + 1)
     const int n0 = min(tid * C, NT - 1), nst = min(n0 + C, NT - 1) - n0;
@@ -560,8 +581,8 @@ static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *
     const int C = L.C;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
         const int q = scan_slot(t, L);
-        sW[q] = lut_rate_dt(sI[q], lut, p);
-        sWs[q] = lut_rate_dt(sI[q], lut_s, p);
+        sW[q] = lut_rate_dt(sI[q], lut, p.I_w0, p);
+        sWs[q] = lut_rate_dt(sI[q], lut_s, p.I_w0s, p);
         se[q] = t == 0 ? x0e : 0.0f;
         ss[q] = t == 0 ? x0s : 0.0f;
     }
