@@ -163,11 +163,10 @@ __device__ __forceinline__ void load_mw_row(float2 *s, int r, const RowFusedArgs
 }
 
 // Carrier march of the intensities already written to sI (scan layout): scan
-// in the scratch Rb (a complex row buffer no thread reads any more) and X;
-// writes rho row r.
+// in the scratch Rb (a complex row buffer no thread reads any more); writes
+// rho row r.
 template <int NT>
-__device__ __forceinline__ void march_scan(float *sI, float2 *Rb, float *X, int r, const RowFusedArgs &a,
-                                           float *rho) {
+__device__ __forceinline__ void march_scan(float *sI, float2 *Rb, int r, const RowFusedArgs &a, float *rho) {
     constexpr int S = scan_span(NT, row_threads<NT>());
     using Sh = ScanShape<NT, row_threads<NT>()>;
     float *sW = sI + S;
@@ -179,9 +178,9 @@ __device__ __forceinline__ void march_scan(float *sI, float2 *Rb, float *X, int 
 }
 
 // Carrier march of the physical row held (unnormalised by inv) in R; scratch
-// in the other FFT buffer O and the extra float area X; writes rho row r.
+// in the other FFT buffer O; writes rho row r.
 template <int NT>
-__device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float inv, int r, const RowFusedArgs &a,
+__device__ __forceinline__ void march_row(float2 *R, float2 *O, float inv, int r, const RowFusedArgs &a,
                                           float *rho) {
     using Sh = ScanShape<NT, row_threads<NT>()>;
     float *sI = reinterpret_cast<float *>(O);
@@ -189,17 +188,19 @@ __device__ __forceinline__ void march_row(float2 *R, float2 *O, float *X, float 
         const float2 v = c_scale(R[pidx(t)], inv);
         sI[Sh::slot(t)] = fmaf(v.x, v.x, v.y * v.y) * a.sc.invE2;
     }
-    march_scan<NT>(sI, R, X, r, a, rho);
+    march_scan<NT>(sI, R, r, a, rho);
 }
 
-// 2 padded complex row buffers (+ one float scan array, scan_span(NT) long, for the march).
-// The march aliases two float arrays into each complex buffer: 2 * span floats
-// must fit in fft_slots(NT) float2, which holds for every NT >= 16 with 256 threads.
+// 2 padded complex row buffers.  The march aliases its arrays into them (the
+// intensities and rates into one, the densities into the other): 2 * span
+// floats must fit in fft_slots(NT) float2, which holds for every NT >= 16 with
+// 256 threads.  (The sweep's affine maps stay in registers, scan_row_ct.)
 template <int NT>
 __host__ __device__ constexpr size_t row_smem_bytes(bool with_march) {
     constexpr int span = scan_span(NT, row_threads<NT>());
     static_assert(2 * span <= 2 * fft_slots(NT), "scan arrays must fit in the FFT buffers");
-    return 2 * (size_t)fft_slots(NT) * sizeof(float2) + (with_march ? (size_t)span * sizeof(float) : 0);
+    (void)with_march;
+    return 2 * (size_t)fft_slots(NT) * sizeof(float2);
 }
 
 // ------------------------------------------------ register-resident row_next
@@ -317,18 +318,18 @@ __device__ __forceinline__ void row_next_regs(const RowFusedArgs &a, int r, floa
         const float2 w = c_scale(v[m], inv);
         sI[Sh::slot((int)threadIdx.x + m * row_threads<NT>())] = fmaf(w.x, w.x, w.y * w.y) * a.sc.invE2;
     }
-    march_scan<NT>(sI, F == A ? B : A, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), r, a, rho);
+    march_scan<NT>(sI, F == A ? B : A, r, a, rho);
 }
 
-// CTAs per SM the row kernels are compiled for: 5 (48 registers at 256
-// threads), fewer when the shared memory admits fewer (228 KB per SM, 1 KB
-// reserved per CTA), and for 512 / 1024 threads no more than leave 64
-// registers a thread.
+// CTAs per SM the row kernels are compiled for: 6 (40 registers at 256
+// threads: more warps to hide the latency of the row's loads and barriers),
+// fewer when the shared memory admits fewer (228 KB per SM, 1 KB reserved per
+// CTA), and for 512 / 1024 threads no more than leave 64 registers a thread.
 template <int NT>
 __host__ __device__ constexpr int row_min_blocks(bool with_march) {
     const int T = with_march ? row_threads<NT>() : row_threads_nl<NT>();
     const int by_smem = (228 * 1024) / (int)(row_smem_bytes<NT>(with_march) + 1024);
-    const int cap = T >= 512 ? 65536 / (T * 64) : 5;
+    const int cap = T >= 512 ? 65536 / (T * 64) : 6;
     return by_smem < cap ? by_smem : cap;
 }
 
@@ -370,7 +371,7 @@ __host__ __device__ constexpr int nl_threads() {
 template <int T>
 __host__ __device__ constexpr int row_min_blocks_t(size_t smem) {
     const int by_smem = (228 * 1024) / (int)(smem + 1024);
-    const int by_regs = 65536 / (T * (T >= 512 ? 64 : 48));
+    const int by_regs = 65536 / (T * (T >= 512 ? 64 : 40));
     const int by_thr = 2048 / T;
     const int m = by_smem < by_regs ? by_smem : by_regs;
     const int n = m < by_thr ? m : by_thr;
@@ -405,7 +406,7 @@ __device__ __forceinline__ void row_entry_body(const RowFusedArgs &a, int r, con
     float2 *O = R == b0 ? b1 : b0;
     for (int t = threadIdx.x; t < NT; t += blockDim.x) O[pidx(t)] = g[t];
     __syncthreads();
-    march_row<NT>(O, R, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), 1.0f, r, a, rho);
+    march_row<NT>(O, R, 1.0f, r, a, rho);
 }
 
 // row_nl plan 1: the row held in registers, 8 points per thread (N_t / 8
@@ -507,7 +508,7 @@ __device__ __forceinline__ void row_next_body(const RowFusedArgs &a, int r, floa
         }
     }
     if (!do_scan) return;
-    march_row<NT>(R, R == b0 ? b1 : b0, reinterpret_cast<float *>(sm2 + 2 * fft_slots(NT)), inv, r, a, rho);
+    march_row<NT>(R, R == b0 ? b1 : b0, inv, r, a, rho);
 }
 
 // row_nl with the full-physics nonlinear block (Raman / self-steepening in
