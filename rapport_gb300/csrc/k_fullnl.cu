@@ -9,10 +9,18 @@ __global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
 k_nl_full(float2 *__restrict__ u, const float *__restrict__ rho, const float *__restrict__ rhos, float dz, NLParams p,
           const float4 *__restrict__ tab, FullTabs ft, const float2 *__restrict__ tw) {
     extern __shared__ float2 smf[];
+    // the constants the out-of-line right-hand side reads at every point: a shared copy
+    __shared__ NLParams s_nl;
+    __shared__ FullTabs s_ft;
+    if (threadIdx.x == 0) {
+        s_nl = p;
+        s_ft = ft;
+    }
     const FullRows m = full_rows<NT>(smf);
     const size_t base = (size_t)blockIdx.x * NT;
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.U[t] = u[base + t];
-    nl_block_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, dz, p, tab, ft, tw);
+    __syncthreads();
+    nl_block_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, dz, s_nl, tab, s_ft, tw);
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) u[base + t] = m.U[t];
 }
 
@@ -22,6 +30,13 @@ k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const 
              float2 *__restrict__ rhs, float *__restrict__ alpha, NLParams p, const float4 *__restrict__ tab,
              FullTabs ft, const float2 *__restrict__ tw) {
     extern __shared__ float2 smf[];
+    // the constants the out-of-line right-hand side reads at every point: a shared copy
+    __shared__ NLParams s_nl;
+    __shared__ FullTabs s_ft;
+    if (threadIdx.x == 0) {
+        s_nl = p;
+        s_ft = ft;
+    }
     const FullRows m = full_rows<NT>(smf);
     const size_t base = (size_t)blockIdx.x * NT;
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) {
@@ -33,7 +48,7 @@ k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const 
         }
     }
     __syncthreads();
-    const float2 *K = rhs_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, p, tab, ft, tw);
+    const float2 *K = rhs_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, s_nl, tab, s_ft, tw);
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) rhs[base + t] = K[pidx(t)];
 }
 

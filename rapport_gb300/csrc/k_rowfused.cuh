@@ -519,14 +519,23 @@ __device__ __forceinline__ void row_nl_full_body(const RowFusedArgs &a, int r, f
                                                  const float *__restrict__ rho, const float *__restrict__ rho_s,
                                                  int g) {
     extern __shared__ float2 sm2[];
+    // the block's constants, read at every point of every RK stage by the
+    // out-of-line right-hand side: a copy in shared memory (a reference into
+    // the kernel's parameters would reload them from there at each use)
+    __shared__ NLParams s_nl;
+    __shared__ FullTabs s_ft;
+    if (threadIdx.x == 0) {
+        s_nl = a.nl;
+        s_ft = a.ft;
+    }
     const FullRows m = full_rows<NT>(sm2);
     load_mw_row<NT>(m.B0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
     const float2 *R = fft_row<NT, true>(m.B0, m.B1, a.tw);
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.U[t] = R[pidx(t)];
     __syncthreads();
-    nl_block_full<NT>(m, rho + (size_t)r * NT, rho_s ? rho_s + (size_t)r * NT : nullptr, a.dz, a.nl, a.pchip,
-                      a.ft, a.tw);
+    nl_block_full<NT>(m, rho + (size_t)r * NT, rho_s ? rho_s + (size_t)r * NT : nullptr, a.dz, s_nl, a.pchip,
+                      s_ft, a.tw);
     for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.B0[pidx(t)] = m.U[t];
     __syncthreads();
     float2 *Y = fft_row<NT, false>(m.B0, m.B1, a.tw);
