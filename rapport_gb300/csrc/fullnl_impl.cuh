@@ -80,6 +80,13 @@ __host__ __device__ constexpr int full_min_blocks() {
     return (228 * 1024) / (int)(full_smem_bytes<NT>() + 1024) >= 2 ? 2 : 1;
 }
 
+// The transforms of split() itself (the Raman convolution, F[X] and the
+// inverse of the filtered sum) take plain twiddle products: they produce k,
+// which reaches the field only as dz k, so the fixed rounding of the twiddle
+// table is scaled by the nonlinear phase of a step (<= ~0.05 rad) before it
+// can repeat from step to step -- below 1e-5 of the field over 2000 z-steps.
+// The row kernel's own transforms of the field keep the compensated products.
+//
 // k = split(S) for every point of the stage field S (shared, index t), left in
 // a free FFT buffer (padded index) whose pointer is returned; synced, and the
 // other buffers are free again.  All threads of the CTA call it.  Each thread
@@ -105,10 +112,10 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
             B0[pidx(t)] = make_float2(fmaf(v.x, v.x, v.y * v.y), 0.0f);
         }
         __syncthreads();
-        float2 *R = fft_row<NT, false>(B0, B1, tw);
+        float2 *R = fft_row<NT, false, NLSE_ROW_THREADS, false>(B0, B1, tw);
         for (int f = threadIdx.x; f < NT; f += TT) R[pidx(f)] = c_mul(R[pidx(f)], __ldg(&ft.Rf[f]));
         __syncthreads();
-        Q = fft_row<NT, true>(R, R == B0 ? B1 : B0, tw);
+        Q = fft_row<NT, true, NLSE_ROW_THREADS, false>(R, R == B0 ? B1 : B0, tw);
     }
     // the pointwise terms; X1 (and X2) into the transform buffers on the FFT
     // path (a point's Q value is read before the same thread overwrites it)
@@ -141,9 +148,9 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
     if (fft_path && !bad) {
         float2 *C;
         if (ft.T) {
-            float2 *P1 = fft_row<NT, false>(B0, B1, tw);
+            float2 *P1 = fft_row<NT, false, NLSE_ROW_THREADS, false>(B0, B1, tw);
             float2 *fr = P1 == B0 ? B1 : B0;
-            float2 *P2 = fft_row<NT, false>(B2, fr, tw);
+            float2 *P2 = fft_row<NT, false, NLSE_ROW_THREADS, false>(B2, fr, tw);
             float2 *fr2 = P2 == B2 ? fr : B2;  // the buffer neither P1 nor P2 occupies
             for (int f = threadIdx.x; f < NT; f += TT) {
                 const float T = __ldg(&ft.T[f]);
@@ -163,20 +170,20 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
                     }
                 }
                 __syncthreads();
-                float2 *P3 = fft_row<NT, false>(P2, fr2, tw);
+                float2 *P3 = fft_row<NT, false, NLSE_ROW_THREADS, false>(P2, fr2, tw);
                 for (int f = threadIdx.x; f < NT; f += TT)
                     C[pidx(f)] = c_scale(c_add(C[pidx(f)], P3[pidx(f)]), __ldg(&ft.invU[f]));
                 __syncthreads();
-                Y = fft_row<NT, true>(C, P3 == P2 ? fr2 : P2, tw);
+                Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, P3 == P2 ? fr2 : P2, tw);
             } else {
                 __syncthreads();
-                Y = fft_row<NT, true>(C, P2, tw);
+                Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, P2, tw);
             }
         } else {
-            C = fft_row<NT, false>(B0, B1, tw);
+            C = fft_row<NT, false, NLSE_ROW_THREADS, false>(B0, B1, tw);
             for (int f = threadIdx.x; f < NT; f += TT) C[pidx(f)] = c_scale(C[pidx(f)], __ldg(&ft.invU[f]));
             __syncthreads();
-            Y = fft_row<NT, true>(C, C == B0 ? B1 : B0, tw);
+            Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, C == B0 ? B1 : B0, tw);
         }
     }
     // k per point, written where the thread read its Y (or Q) value: the same
