@@ -139,8 +139,7 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl", device_id=dev)
     w = WORKLOAD
     Z = args.zsteps
-    stf = dict(enable_space_time_focusing=True) if args.space_time_focusing else {}
-    cfg = R.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], w["dz"], Z, **stf)
+    cfg = R.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], w["dz"], Z, **physics_over(args))
     g = R.build_grids(cfg)
     ctx = _lib.Context(cfg, g)
     u0 = R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"])(g["rr"], g["tt"], cfg, g)
@@ -219,9 +218,11 @@ def run_ours(args, rank, world, local_rank):
         bt.set_mode(modes[bmode])
         bu = [torch.from_numpy(e).to(dev) for e in envs]
         br = [torch.zeros(u0.shape, dtype=torch.float32, device=dev) for _ in range(B)]
-        bt.propagate(bu, br, None, w["dz"], 1)
+        # the exciton density, where the channel is on (the batch then requires it)
+        bs = [torch.zeros(u0.shape, dtype=torch.float32, device=dev) for _ in range(B)] if cfg.enable_ste else None
+        bt.propagate(bu, br, bs, w["dz"], 1)
         for _ in range(args.warmup):
-            bt.propagate(bu, br, None, w["dz"], Z)
+            bt.propagate(bu, br, bs, w["dz"], Z)
         torch.cuda.synchronize()
         K = args.steps
         bev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
@@ -231,7 +232,7 @@ def run_ours(args, rank, world, local_rank):
         for i in range(K):
             flush.fill_(float(i))
             bev[i][0].record()
-            bt.propagate(bu, br, None, w["dz"], Z)
+            bt.propagate(bu, br, bs, w["dz"], Z)
             bev[i][1].record()
         torch.cuda.synchronize()
         barrier()
@@ -247,7 +248,7 @@ def run_ours(args, rank, world, local_rank):
         pctx.profile_start(K * Z * 16 + 64)
         for i in range(K):
             flush.fill_(float(i))
-            bt.propagate(bu, br, None, w["dz"], Z)
+            bt.propagate(bu, br, bs, w["dz"], Z)
         prof = pctx.profile_read()
         assert bt.device_status() == 0 and all(bool(torch.isfinite(x).all().item()) for x in bu)
         # e2e through the C ABI with host buffers: every step copies each pulse's field in from
@@ -256,9 +257,11 @@ def run_ours(args, rank, world, local_rank):
         # and compute, as a caller streaming batches would run it; every copy of the K steps is
         # inside the one timed region.  The batch's working set (~0.6 GB) exceeds the L2.
         uh = [torch.from_numpy(e).pin_memory() for e in envs]
-        dsets = [(bu, br), ([torch.empty_like(x) for x in bu], [torch.empty_like(x) for x in br])]
+        dsets = [(bu, br, bs), ([torch.empty_like(x) for x in bu], [torch.empty_like(x) for x in br],
+                                [torch.zeros_like(x) for x in bs] if bs else None)]
+        nd = 2 if bs else 1  # densities read back per pulse: rho (and rho_s)
         hsets = [([torch.empty_like(x).pin_memory() for x in uh],
-                  [torch.empty(u0.shape, dtype=torch.float32).pin_memory() for _ in range(B)]) for _ in range(2)]
+                  [torch.empty(u0.shape, dtype=torch.float32).pin_memory() for _ in range(nd * B)]) for _ in range(2)]
         main = torch.cuda.current_stream()
         s_in, s_out = torch.cuda.Stream(), torch.cuda.Stream()
         ev_in = [torch.cuda.Event() for _ in range(2)]
@@ -267,7 +270,7 @@ def run_ours(args, rank, world, local_rank):
 
         def e2e_step(i):
             k = i % 2
-            du, dr = dsets[k]
+            du, dr, ds = dsets[k]
             ho, hr = hsets[k]
             with torch.cuda.stream(s_in):
                 if i >= 2:
@@ -276,13 +279,15 @@ def run_ours(args, rank, world, local_rank):
                     du[j].copy_(uh[j], non_blocking=True)
                 ev_in[k].record(s_in)
             main.wait_event(ev_in[k])
-            bt.propagate(du, dr, None, w["dz"], Z)
+            bt.propagate(du, dr, ds, w["dz"], Z)
             ev_done[k].record(main)
             with torch.cuda.stream(s_out):
                 s_out.wait_event(ev_done[k])
                 for j in range(B):
                     ho[j].copy_(du[j], non_blocking=True)
                     hr[j].copy_(dr[j], non_blocking=True)
+                    if ds:
+                        hr[B + j].copy_(ds[j], non_blocking=True)
                 ev_out[k].record(s_out)
 
         for i in range(2):                     # untimed: both buffer sets once
@@ -306,14 +311,14 @@ def run_ours(args, rank, world, local_rank):
         # the other tensor-core form on the same batch, for the forms table
         for oname in [m for m in ("split_bf16", "split_f16") if m != bmode and args.mode == "auto"]:
             bt.set_mode(modes[oname])
-            bt.propagate(bu, br, None, w["dz"], Z)
+            bt.propagate(bu, br, bs, w["dz"], Z)
             K2 = max(2, K // 2)
             oev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K2)]
             torch.cuda.synchronize()
             for i in range(K2):
                 flush.fill_(float(i))
                 oev[i][0].record()
-                bt.propagate(bu, br, None, w["dz"], Z)
+                bt.propagate(bu, br, bs, w["dz"], Z)
                 oev[i][1].record()
             torch.cuda.synchronize()
             assert bt.device_status() == 0
@@ -381,7 +386,8 @@ def run_ours(args, rank, world, local_rank):
         "dtype": {"split_bf16": "bf16x3-split + f32", "split_f16": "f16x2-split + f32"}.get(bmode, "f32"),
         "data": "synthetic (seeded lens-focused Gaussian pulses with 1% noise)",
         "config": dict(CONFIG, form=form, pulses=max(B, 1), z_steps_per_step=Z, parallelism=f"replicas{world}",
-                       space_time_focusing=bool(args.space_time_focusing),
+                       space_time_focusing=bool(args.space_time_focusing or args.all_physics),
+                       physics=physics_name(args),
                        l2="256 MB flush before each timed step (outside its events); per pulse 24 MB",
                        kernel_times="second identical pass of K steps with per-launch events"),
         "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
@@ -496,6 +502,23 @@ def run_config4(args, rank, world, local_rank):
         print(json.dumps(line), flush=True)
 
 
+def physics_over(args):
+    """Config overrides of the physics options: none (the measured workload),
+    space-time focusing, or every term the reference's Config enables by default."""
+    if getattr(args, "all_physics", False):
+        return dict(f_R=0.18, enable_kerr_raman=True, enable_self_steepening=True,
+                    enable_space_time_focusing=True, enable_ste=True, enable_ste_index=True)
+    if args.space_time_focusing:
+        return dict(enable_space_time_focusing=True)
+    return {}
+
+
+def physics_name(args):
+    if getattr(args, "all_physics", False):
+        return "Raman + self-steepening + space-time focusing + exciton channel (the reference's defaults)"
+    return "space-time focusing" if args.space_time_focusing else "Kerr, MPI + avalanche + recombination"
+
+
 # ------------------------------------------------------------------ CPU (oracle) arm
 def _oracle_setup():
     sys.path.insert(0, os.path.join(HERE, "oracle"))
@@ -519,7 +542,7 @@ def cpu_baseline(nz):
     cores, blas = host_cores()
     return {"value": nz / dt, "unit": "z-steps/s", "cores": cores, "blas_threads": blas, "kind": "port",
             "sample": f"{nz} z-steps of the 1024x2048 workload (FP64 numpy/OpenBLAS + C carrier march, "
-                      f"OpenMP over r)",
+                      f"OpenMP over r; Kerr, MPI + avalanche + recombination whatever physics the GPU arm ran)",
             "what": "the oracle: an FP64 restatement of the reference path, pinned to the reference's own "
                     "outputs bit for bit or to 1e-12 (the reference itself needs CuPy and a GPU)"}
 
@@ -767,6 +790,10 @@ def main():
     ap.add_argument("--space-time-focusing", action="store_true",
                     help="the single / batched workload with space-time focusing on (the reference's default): "
                          "the tensor-core forms run the correction Y (P - 1) Y")
+    ap.add_argument("--all-physics", action="store_true",
+                    help="the single / batched workload with every term the reference's Config turns on by "
+                         "default: Raman (f_R 0.18), self-steepening, space-time focusing, the exciton channel "
+                         "and its index term (the measured workload's rate table and grid otherwise)")
     ap.add_argument("--workload", default="single", choices=["single", "config4", "config5", "tour"],
                     help="tour: every kernel once at 1024 x 2048 (for ncu launch lists)")
     ap.add_argument("--record-traffic", metavar="CSV",

@@ -119,7 +119,7 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
     }
     // the pointwise terms; X1 (and X2) into the transform buffers on the FFT
     // path (a point's Q value is read before the same thread overwrites it)
-    int bad = 0;
+    int bad = 0, any_x2 = 0, any_x3 = 0;
 #pragma unroll
     for (int q = 0; q < PP; ++q) {
         const int t = (int)threadIdx.x + q * TT;
@@ -128,6 +128,8 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
             const float a2 = fmaf(s.x, s.x, s.y * s.y);
             const float r = __ldg(&rho[t]), rs = rhos ? __ldg(&rhos[t]) : 0.0f;
             const float ph = photo_term(a2, r, p, tab);
+            any_x2 |= ph != 0.0f;
+            any_x3 |= r != 0.0f || rs != 0.0f;
             m.PH[t] = ph;
             const float kr = Q ? Q[pidx(t)].x * inv_n : 0.0f;
             const float K = fmaf(p.kp, a2, p.kp_raman * kr);  // kerr_pref * kerr_I
@@ -144,22 +146,36 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
         }
     }
     bad = __syncthreads_or(bad);  // also orders the buffer writes before the transforms
+    // On the self-steepening path X2 and X3 have transforms of their own: a
+    // row where the photo-ionisation term (X2) or the carrier densities (X3)
+    // are zero at every point has an exactly zero transform of that term, and
+    // it is left out (the results are the same but for the sign of zeros).
+    if (ft.T) {
+        any_x2 = __syncthreads_or(any_x2);
+        any_x3 = __syncthreads_or(any_x3);
+    }
     float2 *Y = nullptr;          // the spectral part of k (inverse-transformed, unnormalised)
     if (fft_path && !bad) {
         float2 *C;
         if (ft.T) {
             float2 *P1 = fft_row<NT, false, NLSE_ROW_THREADS, false>(B0, B1, tw);
             float2 *fr = P1 == B0 ? B1 : B0;
-            float2 *P2 = fft_row<NT, false, NLSE_ROW_THREADS, false>(B2, fr, tw);
+            float2 *P2 = B2;   // F[X2], or (no X2 transform) the unused X2 buffer
+            if (any_x2) P2 = fft_row<NT, false, NLSE_ROW_THREADS, false>(B2, fr, tw);
             float2 *fr2 = P2 == B2 ? fr : B2;  // the buffer neither P1 nor P2 occupies
             for (int f = threadIdx.x; f < NT; f += TT) {
                 const float T = __ldg(&ft.T[f]);
-                const float2 a = P1[pidx(f)], b = P2[pidx(f)];
+                const float2 a = P1[pidx(f)], b = any_x2 ? P2[pidx(f)] : make_float2(0.0f, 0.0f);
                 // T^2 F[X1] - T F[X2] = T (T F[X1] - F[X2])
                 P1[pidx(f)] = c_scale(make_float2(fmaf(T, a.x, -b.x), fmaf(T, a.y, -b.y)), T);
             }
             C = P1;
-            if (ft.invU) {
+            if (ft.invU && !any_x3) {
+                // F[X3] = 0: only the U^-1 factor
+                for (int f = threadIdx.x; f < NT; f += TT) C[pidx(f)] = c_scale(C[pidx(f)], __ldg(&ft.invU[f]));
+                __syncthreads();
+                Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, P2, tw);
+            } else if (ft.invU) {
                 // F[X3] through the two free buffers, then the U^-1 factor
 #pragma unroll
                 for (int q = 0; q < PP; ++q) {

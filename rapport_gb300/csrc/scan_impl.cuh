@@ -579,14 +579,21 @@ static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *
     const int T = Nt - 1;
     const ScanLayout L = scan_layout(Nt);
     const int C = L.C;
+    int need = 0;
     for (int t = threadIdx.x; t < Nt; t += blockDim.x) {
         const int q = scan_slot(t, L);
         sW[q] = lut_rate_dt(sI[q], lut, p.I_w0, p);
         sWs[q] = lut_rate_dt(sI[q], lut_s, p.I_w0s, p);
         se[q] = t == 0 ? x0e : 0.0f;
         ss[q] = t == 0 ? x0s : 0.0f;
+        need |= march_needed(sW[q], sI[q], Nt, p) || sWs[q] != 0.0f;
     }
-    __syncthreads();
+    // As for one population: with both rates zero along the row and both
+    // densities starting at zero, every step maps (0, 0) to exactly (0, 0)
+    // (the re-ionisation and the exciton source vanish with the densities),
+    // the affine offsets stay +0 and the maps' products finite: the row stays
+    // at zero and skips the sweeps.
+    if (!__syncthreads_or(need) && x0e == 0.0f && x0s == 0.0f) return;
     const int n0 = min((int)threadIdx.x * C, T), n1 = min(n0 + C, T);
     const int q_last = (int)threadIdx.x + 1;
     int converged = 0, clamp_any = 0;
