@@ -137,7 +137,7 @@ def run_ours(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    w = WORKLOAD
+    w = dict(WORKLOAD, Nt=args.nt) if args.nt else WORKLOAD
     Z = args.zsteps
     cfg = R.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], w["dz"], Z, **physics_over(args))
     g = R.build_grids(cfg)
@@ -385,7 +385,8 @@ def run_ours(args, rank, world, local_rank):
         "vs_baseline": None,
         "dtype": {"split_bf16": "bf16x3-split + f32", "split_f16": "f16x2-split + f32"}.get(bmode, "f32"),
         "data": "synthetic (seeded lens-focused Gaussian pulses with 1% noise)",
-        "config": dict(CONFIG, form=form, pulses=max(B, 1), z_steps_per_step=Z, parallelism=f"replicas{world}",
+        "config": dict(CONFIG, Nt=w["Nt"], workload=CONFIG["workload"].replace("N_t=2048", f"N_t={w['Nt']}"),
+                       form=form, pulses=max(B, 1), z_steps_per_step=Z, parallelism=f"replicas{world}",
                        space_time_focusing=bool(args.space_time_focusing or args.all_physics),
                        physics=physics_name(args),
                        l2="256 MB flush before each timed step (outside its events); per pulse 24 MB",
@@ -787,6 +788,9 @@ def main():
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=8, help="pulses of the batched (headline) form; 0 = single pulse")
+    ap.add_argument("--nt", type=int, default=0,
+                    help="time points of the single / batched workload instead of 2048 (same +-800 fs window); "
+                         "4096 is the reference Config's default")
     ap.add_argument("--space-time-focusing", action="store_true",
                     help="the single / batched workload with space-time focusing on (the reference's default): "
                          "the tensor-core forms run the correction Y (P - 1) Y")

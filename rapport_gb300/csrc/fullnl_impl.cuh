@@ -72,6 +72,14 @@ __device__ __forceinline__ float alpha_from(float photo, float rho, const NLPara
 
 __device__ __forceinline__ bool c_finite(float2 v) { return isfinite(v.x) && isfinite(v.y); }
 
+// Threads of a full-physics CTA: 256, and 512 at N_t = 4096, where the row's
+// buffers leave room for one CTA per SM and 512 threads give every radix-8 pass
+// exactly one butterfly a thread (16 warps instead of 8 to hide the latency).
+template <int NT>
+__host__ __device__ constexpr int full_threads() {
+    return NT >= 4096 ? 512 : NLSE_ROW_THREADS;
+}
+
 // CTAs per SM the full-physics kernels are compiled for: what their shared
 // memory admits, at most 2 (<= 128 registers a thread at 256 threads; with
 // the whole block inlined ptxas otherwise spends ~180 and fits one CTA).
@@ -98,7 +106,7 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
                                          const float *__restrict__ rhos, const NLParams &p,
                                          const float4 *__restrict__ tab, const FullTabs &ft,
                                          const float2 *__restrict__ tw) {
-    constexpr int TT = NLSE_ROW_THREADS;
+    constexpr int TT = full_threads<NT>();
     constexpr int PP = (NT + TT - 1) / TT;  // points per thread
     constexpr float inv_n = 1.0f / (float)NT;
     const bool fft_path = ft.T != nullptr || ft.invU != nullptr;
@@ -112,10 +120,10 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
             B0[pidx(t)] = make_float2(fmaf(v.x, v.x, v.y * v.y), 0.0f);
         }
         __syncthreads();
-        float2 *R = fft_row<NT, false, NLSE_ROW_THREADS, false>(B0, B1, tw);
+        float2 *R = fft_row<NT, false, TT, false>(B0, B1, tw);
         for (int f = threadIdx.x; f < NT; f += TT) R[pidx(f)] = c_mul(R[pidx(f)], __ldg(&ft.Rf[f]));
         __syncthreads();
-        Q = fft_row<NT, true, NLSE_ROW_THREADS, false>(R, R == B0 ? B1 : B0, tw);
+        Q = fft_row<NT, true, TT, false>(R, R == B0 ? B1 : B0, tw);
     }
     // the pointwise terms; X1 (and X2) into the transform buffers on the FFT
     // path (a point's Q value is read before the same thread overwrites it)
@@ -158,10 +166,10 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
     if (fft_path && !bad) {
         float2 *C;
         if (ft.T) {
-            float2 *P1 = fft_row<NT, false, NLSE_ROW_THREADS, false>(B0, B1, tw);
+            float2 *P1 = fft_row<NT, false, TT, false>(B0, B1, tw);
             float2 *fr = P1 == B0 ? B1 : B0;
             float2 *P2 = B2;   // F[X2], or (no X2 transform) the unused X2 buffer
-            if (any_x2) P2 = fft_row<NT, false, NLSE_ROW_THREADS, false>(B2, fr, tw);
+            if (any_x2) P2 = fft_row<NT, false, TT, false>(B2, fr, tw);
             float2 *fr2 = P2 == B2 ? fr : B2;  // the buffer neither P1 nor P2 occupies
             for (int f = threadIdx.x; f < NT; f += TT) {
                 const float T = __ldg(&ft.T[f]);
@@ -174,7 +182,7 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
                 // F[X3] = 0: only the U^-1 factor
                 for (int f = threadIdx.x; f < NT; f += TT) C[pidx(f)] = c_scale(C[pidx(f)], __ldg(&ft.invU[f]));
                 __syncthreads();
-                Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, P2, tw);
+                Y = fft_row<NT, true, TT, false>(C, P2, tw);
             } else if (ft.invU) {
                 // F[X3] through the two free buffers, then the U^-1 factor
 #pragma unroll
@@ -186,20 +194,20 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
                     }
                 }
                 __syncthreads();
-                float2 *P3 = fft_row<NT, false, NLSE_ROW_THREADS, false>(P2, fr2, tw);
+                float2 *P3 = fft_row<NT, false, TT, false>(P2, fr2, tw);
                 for (int f = threadIdx.x; f < NT; f += TT)
                     C[pidx(f)] = c_scale(c_add(C[pidx(f)], P3[pidx(f)]), __ldg(&ft.invU[f]));
                 __syncthreads();
-                Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, P3 == P2 ? fr2 : P2, tw);
+                Y = fft_row<NT, true, TT, false>(C, P3 == P2 ? fr2 : P2, tw);
             } else {
                 __syncthreads();
-                Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, P2, tw);
+                Y = fft_row<NT, true, TT, false>(C, P2, tw);
             }
         } else {
-            C = fft_row<NT, false, NLSE_ROW_THREADS, false>(B0, B1, tw);
+            C = fft_row<NT, false, TT, false>(B0, B1, tw);
             for (int f = threadIdx.x; f < NT; f += TT) C[pidx(f)] = c_scale(C[pidx(f)], __ldg(&ft.invU[f]));
             __syncthreads();
-            Y = fft_row<NT, true, NLSE_ROW_THREADS, false>(C, C == B0 ? B1 : B0, tw);
+            Y = fft_row<NT, true, TT, false>(C, C == B0 ? B1 : B0, tw);
         }
     }
     // k per point, written where the thread read its Y (or Q) value: the same
@@ -242,7 +250,7 @@ __device__ __forceinline__ void nl_block_full(const FullRows &m, const float *__
                                               const float *__restrict__ rhos, float dz, const NLParams &p,
                                               const float4 *__restrict__ tab, const FullTabs &ft,
                                               const float2 *__restrict__ tw) {
-    constexpr int TT = NLSE_ROW_THREADS;
+    constexpr int TT = full_threads<NT>();
     const float hdz = 0.5f * dz;
     float2 *U = m.U, *KS = m.KS, *S = m.S;
     for (int t = threadIdx.x; t < NT; t += TT) {

@@ -5,7 +5,7 @@
 #include "fullnl_impl.cuh"
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
+__global__ void __launch_bounds__(full_threads<NT>(), full_min_blocks<NT>())
 k_nl_full(float2 *__restrict__ u, const float *__restrict__ rho, const float *__restrict__ rhos, float dz, NLParams p,
           const float4 *__restrict__ tab, FullTabs ft, const float2 *__restrict__ tw) {
     extern __shared__ float2 smf[];
@@ -18,14 +18,14 @@ k_nl_full(float2 *__restrict__ u, const float *__restrict__ rho, const float *__
     }
     const FullRows m = full_rows<NT>(smf);
     const size_t base = (size_t)blockIdx.x * NT;
-    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.U[t] = u[base + t];
+    for (int t = threadIdx.x; t < NT; t += full_threads<NT>()) m.U[t] = u[base + t];
     __syncthreads();
     nl_block_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, dz, s_nl, tab, s_ft, tw);
-    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) u[base + t] = m.U[t];
+    for (int t = threadIdx.x; t < NT; t += full_threads<NT>()) u[base + t] = m.U[t];
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
+__global__ void __launch_bounds__(full_threads<NT>(), full_min_blocks<NT>())
 k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const float *__restrict__ rhos,
              float2 *__restrict__ rhs, float *__restrict__ alpha, NLParams p, const float4 *__restrict__ tab,
              FullTabs ft, const float2 *__restrict__ tw) {
@@ -39,7 +39,7 @@ k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const 
     }
     const FullRows m = full_rows<NT>(smf);
     const size_t base = (size_t)blockIdx.x * NT;
-    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) {
+    for (int t = threadIdx.x; t < NT; t += full_threads<NT>()) {
         const float2 v = u[base + t];
         m.S[t] = v;
         if (alpha) {
@@ -49,7 +49,7 @@ k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const 
     }
     __syncthreads();
     const float2 *K = rhs_full<NT>(m, rho + base, rhos ? rhos + base : nullptr, s_nl, tab, s_ft, tw);
-    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) rhs[base + t] = K[pidx(t)];
+    for (int t = threadIdx.x; t < NT; t += full_threads<NT>()) rhs[base + t] = K[pidx(t)];
 }
 
 static FullTabs ctx_tabs(const nlse_ctx *c) { return FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf}; }
@@ -60,7 +60,7 @@ cudaError_t launch_nl_full(nlse_ctx *c, float2 *u, const float *rho, const float
         const size_t smem = full_smem_bytes<NT>();
         cudaError_t e = cudaFuncSetAttribute(k_nl_full<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_nl_full<NT><<<c->Nr, NLSE_ROW_THREADS, smem, st>>>(u, rho, rho_s, dz, c->nl, c->d_pchip, ctx_tabs(c),
+        k_nl_full<NT><<<c->Nr, full_threads<NT>(), smem, st>>>(u, rho, rho_s, dz, c->nl, c->d_pchip, ctx_tabs(c),
                                                             c->d_tw);
     });
     return cudaGetLastError();
@@ -73,7 +73,7 @@ cudaError_t launch_split_full(nlse_ctx *c, const float2 *u, const float *rho, co
         cudaError_t e =
             cudaFuncSetAttribute(k_split_full<NT>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
-        k_split_full<NT><<<c->Nr, NLSE_ROW_THREADS, smem, st>>>(u, rho, rho_s, rhs, alpha, c->nl, c->d_pchip,
+        k_split_full<NT><<<c->Nr, full_threads<NT>(), smem, st>>>(u, rho, rho_s, rhs, alpha, c->nl, c->d_pchip,
                                                                ctx_tabs(c), c->d_tw);
     });
     return cudaGetLastError();

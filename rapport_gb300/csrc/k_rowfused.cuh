@@ -531,19 +531,19 @@ __device__ __forceinline__ void row_nl_full_body(const RowFusedArgs &a, int r, f
     const FullRows m = full_rows<NT>(sm2);
     load_mw_row<NT>(m.B0, r, a, F32, D, 1.0f / (float)NT, g);
     __syncthreads();
-    const float2 *R = fft_row<NT, true>(m.B0, m.B1, a.tw);
-    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.U[t] = R[pidx(t)];
+    const float2 *R = fft_row<NT, true, full_threads<NT>()>(m.B0, m.B1, a.tw);
+    for (int t = threadIdx.x; t < NT; t += full_threads<NT>()) m.U[t] = R[pidx(t)];
     __syncthreads();
     nl_block_full<NT>(m, rho + (size_t)r * NT, rho_s ? rho_s + (size_t)r * NT : nullptr, a.dz, s_nl, a.pchip,
                       s_ft, a.tw);
-    for (int t = threadIdx.x; t < NT; t += NLSE_ROW_THREADS) m.B0[pidx(t)] = m.U[t];
+    for (int t = threadIdx.x; t < NT; t += full_threads<NT>()) m.B0[pidx(t)] = m.U[t];
     __syncthreads();
-    float2 *Y = fft_row<NT, false>(m.B0, m.B1, a.tw);
+    float2 *Y = fft_row<NT, false, full_threads<NT>()>(m.B0, m.B1, a.tw);
     store_state_row<NT>(Y, r, a, F32, Fb, g + 1);
 }
 
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
+__global__ void __launch_bounds__(full_threads<NT>(), full_min_blocks<NT>())
 k_row_nl_full(RowFusedArgs a, float *__restrict__ F32, __nv_bfloat16 *__restrict__ Fb, const float *__restrict__ D,
               const float *__restrict__ rho, int g) {
     row_nl_full_body<NT>(a, blockIdx.x, F32, Fb, D, rho, a.rho_s, g);
@@ -609,7 +609,7 @@ k_row_next_b(const __grid_constant__ PulseTable T, const BatchCall *__restrict__
 
 // Pulses with the full-physics terms (Raman / self-steepening; one time-grid class).
 template <int NT>
-__global__ void __launch_bounds__(NLSE_ROW_THREADS, full_min_blocks<NT>())
+__global__ void __launch_bounds__(full_threads<NT>(), full_min_blocks<NT>())
 k_row_nl_full_b(const __grid_constant__ PulseTable T, const BatchCall *__restrict__ C,
                 const int2 *__restrict__ work, int g) {
     const int2 w = work[blockIdx.x];
@@ -700,7 +700,7 @@ cudaError_t RowKernels<NT>::nl_full(const RowFusedArgs &a, float *F32, __nv_bflo
         const size_t smem = full_smem_bytes<NT>();
         cudaError_t e = set_smem(k_row_nl_full<NT>, smem);
         if (e != cudaSuccess) return e;
-        k_row_nl_full<NT><<<a.Nr, NLSE_ROW_THREADS, smem, st>>>(a, F32, Fb, D, rho, g);
+        k_row_nl_full<NT><<<a.Nr, full_threads<NT>(), smem, st>>>(a, F32, Fb, D, rho, g);
         return cudaGetLastError();
     }
 }
@@ -716,7 +716,7 @@ cudaError_t RowKernels<NT>::batch(int kind, const PulseTable &T, const BatchCall
             const size_t smem = full_smem_bytes<NT>();
             e = set_smem(k_row_nl_full_b<NT>, smem);
             if (e != cudaSuccess) return e;
-            k_row_nl_full_b<NT><<<nblocks, NLSE_ROW_THREADS, smem, st>>>(T, C, work, g);
+            k_row_nl_full_b<NT><<<nblocks, full_threads<NT>(), smem, st>>>(T, C, work, g);
             return cudaGetLastError();
         }
     }

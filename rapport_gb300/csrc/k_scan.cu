@@ -25,7 +25,12 @@
 // run out of shared memory.
 #include "scan_impl.cuh"
 
-__global__ void __launch_bounds__(NLSE_ROW_THREADS)
+// Threads a row: 256, 512 from N_t = 4096 and 1024 from 8192 -- 8 steps a
+// thread, so long rows keep short sequential chunks and 16-32 warps per CTA
+// (their scan arrays leave room for one CTA per SM).
+static int scan_threads(int Nt) { return Nt >= 8192 ? 1024 : (Nt >= 4096 ? 512 : NLSE_ROW_THREADS); }
+
+__global__ void __launch_bounds__(1024)
 k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__restrict__ rho_s, int Nt,
             ScanParams p, const float *__restrict__ lut, const float *__restrict__ lut_s, int zero_first,
             int *__restrict__ stats) {
@@ -87,10 +92,11 @@ k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__rest
 
 cudaError_t launch_rate_scan(nlse_ctx *c, const float2 *u, float *rho, float *rho_s, int zero_first,
                              cudaStream_t stream) {
-    size_t smem = (c->sc.ste ? 11 : 5) * (size_t)scan_span(c->Nt, NLSE_ROW_THREADS) * sizeof(float);
+    const int threads = scan_threads(c->Nt);
+    size_t smem = (c->sc.ste ? 11 : 5) * (size_t)scan_span(c->Nt, threads) * sizeof(float);
     cudaError_t e = cudaFuncSetAttribute(k_rate_scan, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (e != cudaSuccess) return e;
-    k_rate_scan<<<c->Nr, NLSE_ROW_THREADS, smem, stream>>>(u, rho, rho_s, c->Nt, c->sc, c->d_lut_dt, c->d_lut_s_dt,
+    k_rate_scan<<<c->Nr, threads, smem, stream>>>(u, rho, rho_s, c->Nt, c->sc, c->d_lut_dt, c->d_lut_s_dt,
                                                            zero_first, c->d_flag);
     return cudaGetLastError();
 }

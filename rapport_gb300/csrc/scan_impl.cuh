@@ -1,6 +1,8 @@
 // Newton-linearised parallel scan of the carrier-rate march, shared by the
 // standalone scan kernel and the fused row kernels.  (Derivation in k_scan.cu.)
 #pragma once
+#include <float.h>
+
 #include "nlse_internal.cuh"
 
 
@@ -637,7 +639,13 @@ static __device__ void scan_row2(const float *sI, float *sW, float *sWs, float *
         block_reduce(dmax, xmax, f, red);
         clamp_any |= f;
         if (clamp_any) break;
-        if (it > 0 && dmax <= SCAN_TOL * xmax) {
+        // converged: the sweep changed nothing by more than 1e-6 of the row's
+        // largest density, or by less than the smallest normal FP32 number --
+        // at the rim of the ionised region the densities can be ~1e-38 cm^-3,
+        // where the iterates settle into denormal rounding noise tens of ulps
+        // wide and never meet a relative test (the row would otherwise be
+        // re-marched sequentially by one thread)
+        if (it > 0 && (dmax <= SCAN_TOL * xmax || dmax <= FLT_MIN)) {
             converged = 1;
             break;
         }

@@ -149,10 +149,12 @@ def test_split_forms_every_term_match_reference_fixture(fc, full, mode):
 
 
 @pytest.mark.parametrize("over,shape", [(FULL_PHYSICS, (64, 256)), (SINGLE["stf"], (256, 512)),
-                                        (SINGLE["stf"], (100, 1024))])
+                                        (SINGLE["stf"], (100, 1024)), (FULL_PHYSICS, (32, 4096))])
 def test_split_space_time_focusing_vs_oracle(full, over, shape):
     """Space-time focusing in the tensor-core forms against the FP64 oracle:
-    with every term and alone, on a radial size that is padded (100 -> 128)."""
+    with every term and alone, on a radial size that is padded (100 -> 128),
+    and with every term at N_t = 4096 (the full-physics block and the exciton
+    march at 512 threads a row)."""
     from rapport_gb300 import _lib
     m = meta_case(full)
     Nr, Nt = shape
