@@ -211,6 +211,7 @@ def run_ours(args, rank, world, local_rank):
     B = args.batch if head in ("split_bf16", "split_f16") else 0
     bmode = args.batch_mode if args.mode == "auto" else head
     other_batched = {}
+    fallback = {"single_pulse": int(ctx.scan_fallback_rows())}
     if B > 0:
         envs = [np.ascontiguousarray(R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"] + i)(
             g["rr"], g["tt"], cfg, g).astype(np.complex64)) for i in range(B)]
@@ -308,6 +309,9 @@ def run_ours(args, rank, world, local_rank):
                                          sum(x.numel() * 4 for x in hsets[0][1])),
                "overlap": "double-buffered: step i's read-back overlaps step i+1's upload and compute"}
         del dsets[1]
+        # rows whose carrier march fell back to the one-thread sequential form (a
+        # diagnostic: the Newton scan should solve every row of these workloads)
+        fallback["batched"] = int(sum(bt.context(i).scan_fallback_rows() for i in range(B)))
         # the other tensor-core form on the same batch, for the forms table
         for oname in [m for m in ("split_bf16", "split_f16") if m != bmode and args.mode == "auto"]:
             bt.set_mode(modes[oname])
@@ -393,6 +397,7 @@ def run_ours(args, rank, world, local_rank):
                        kernel_times="second identical pass of K steps with per-launch events"),
         "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
+        "scan_fallback_rows": fallback,
         "autotuned": {"gemm_variant": ctx.gemm_variant(),
                       "row_plans": dict(zip(("row_nl", "row_next"), _lib.row_plans(Nt)))},
         "clocks": clocks,
