@@ -144,3 +144,43 @@ def test_space_time_focusing_half_cm_accuracy():
     for at, entry in report["checkpoints"].items():
         m = entry["split_stf_sandwich"]
         assert m["l2"] <= 1e-4 and m["peak_rho"] <= 1e-3, (at, m)
+
+
+def test_all_physics_accuracy():
+    """Every split() term on (Raman, self-steepening, space-time focusing, the
+    exciton channel with a 1 ps decay), a 1 uJ pulse focused by a 1 mm lens on
+    256 x 1024: 400 z-steps of 2.5 um (0.1 cm, through the focus) in the split-
+    BF16 and split-FP16 forms against the FP64 numpy oracle (the reference's
+    arithmetic), checkpoints every 100 steps.  Writes
+    accuracy_all_physics_256x1024.json to NLSE_REPORT_DIR; asserts relative L2
+    <= 1e-4 and peak-rho / peak-rho_s <= 1e-3 at every checkpoint."""
+    from conftest import FULL_PHYSICS
+    from rapport_gb300 import _lib
+    dz, chunk, nchunk = 2.5e-6, 100, 4
+    c = Case(256, 1024, 5e-4, 50e-6, 400e-15, 100e-15, 1.0, 1e-3, dz, chunk * nchunk, 0, **FULL_PHYSICS)
+    og = c.og
+    uo, ro, so = c.u0.copy(), np.zeros(c.u0.shape), np.zeros(c.u0.shape)
+    ref = []
+    for _ in range(nchunk):
+        uo, ro, so = og.propagate(uo, chunk, dz, ro, so)
+        ref.append((uo.copy(), ro.copy(), so.copy()))
+    report = {"workload": "256x1024, 1 uJ, w0 50 um, f 1 mm, dz 2.5 um, every split() term, 1% noise seed 0",
+              "commit": os.environ.get("NLSE_COMMIT", ""), "reference": "FP64 numpy oracle (oracle/nlse_oracle.py)",
+              "checkpoints": {}}
+    for name, mode in (("split_bf16", _lib.MODE_SPLIT_BF16), ("split_f16", _lib.MODE_SPLIT_F16)):
+        u, rho, rs = dev(c.u0), dev(np.zeros(c.u0.shape)), dev(np.zeros(c.u0.shape))
+        for j in range(nchunk):
+            c.ctx.propagate(u, rho, rs, dz, chunk, mode)
+            ur, rr, sr = ref[j]
+            m = _metrics(host(u), host(rho), ur, rr, 1.0, 1.0)  # the fluence ratio needs no units
+            m["peak_rho_s"] = abs(host(rs).max() / max(sr.max(), 1e-300) - 1) if sr.max() > 0 else 0.0
+            report["checkpoints"].setdefault(f"{(j + 1) * chunk * dz * 100:.3f} cm", {})[name] = m
+        assert c.ctx.device_status() == 0
+    out = os.environ.get("NLSE_REPORT_DIR")
+    if out:
+        os.makedirs(out, exist_ok=True)
+        with open(os.path.join(out, "accuracy_all_physics_256x1024.json"), "w") as f:
+            json.dump(report, f, indent=1)
+    for cp, forms in report["checkpoints"].items():
+        for name, m in forms.items():
+            assert m["l2"] <= 1e-4 and m["peak_rho"] <= 1e-3 and m["peak_rho_s"] <= 1e-3, (cp, name, m)
