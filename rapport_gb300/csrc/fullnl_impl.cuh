@@ -17,7 +17,8 @@
 // zero; the block reproduces that with a row-wide flag (__syncthreads_or), so
 // the rule holds whichever transforms run.
 //
-// Thread t of the CTA owns the points t, t + T, t + 2T, ... (T = 256).  Shared
+// Thread t of the CTA owns the points t, t + T, t + 2T, ... (T = full_threads:
+// 256, 512 at N_t = 4096).  Shared
 // memory holds three padded complex rows (the FFT ping-pong buffers) and three
 // plain complex rows: the post-alpha field U, the RK accumulator and the stage
 // field S, each read and written only by the thread owning the point.
@@ -81,8 +82,9 @@ __host__ __device__ constexpr int full_threads() {
 }
 
 // CTAs per SM the full-physics kernels are compiled for: what their shared
-// memory admits, at most 2 (<= 128 registers a thread at 256 threads; with
-// the whole block inlined ptxas otherwise spends ~180 and fits one CTA).
+// memory admits, at most 2 (two CTAs of 256 threads, or one of 512 at N_t =
+// 4096: <= 128 registers a thread either way; with the whole block inlined
+// ptxas otherwise spends ~180).
 template <int NT>
 __host__ __device__ constexpr int full_min_blocks() {
     return (228 * 1024) / (int)(full_smem_bytes<NT>() + 1024) >= 2 ? 2 : 1;

@@ -367,7 +367,7 @@ __host__ __device__ constexpr int nl_threads() {
 
 // CTAs per SM a kernel of T threads and the given dynamic shared memory is
 // compiled for: what the shared memory and the 2048 threads per SM admit, at
-// no fewer than 48 registers a thread (64 from 512 threads on).
+// no fewer than 40 registers a thread (64 from 512 threads on).
 template <int T>
 __host__ __device__ constexpr int row_min_blocks_t(size_t smem) {
     const int by_smem = (228 * 1024) / (int)(smem + 1024);
