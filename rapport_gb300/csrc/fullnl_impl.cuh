@@ -81,6 +81,102 @@ __host__ __device__ constexpr int full_threads() {
     return NT >= 4096 ? 512 : NLSE_ROW_THREADS;
 }
 
+// Complex affine map x -> a x + b, and its composition (f first, then g).
+struct CAff {
+    float2 a, b;
+};
+
+__device__ __forceinline__ CAff caff_then(const CAff &f, const CAff &g) {
+    return CAff{c_mul(g.a, f.a), c_add(c_mul(g.a, f.b), g.b)};
+}
+
+// Block-wide exclusive scan of one complex affine map per thread (thread
+// order) and the composition of all of them; TT threads, wsum = 32 maps of
+// shared scratch.  All threads call it.
+template <int TT>
+__device__ __forceinline__ void block_scan_caff(const CAff &v, CAff *wsum, CAff *pre, CAff *tot) {
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    constexpr int NW = TT / 32;
+    const CAff id{make_float2(1.0f, 0.0f), make_float2(0.0f, 0.0f)};
+    CAff inc = v;
+#pragma unroll
+    for (int off = 1; off < 32; off <<= 1) {
+        CAff o;
+        o.a.x = __shfl_up_sync(0xffffffffu, inc.a.x, off);
+        o.a.y = __shfl_up_sync(0xffffffffu, inc.a.y, off);
+        o.b.x = __shfl_up_sync(0xffffffffu, inc.b.x, off);
+        o.b.y = __shfl_up_sync(0xffffffffu, inc.b.y, off);
+        if (lane >= off) inc = caff_then(o, inc);
+    }
+    if (lane == 31) wsum[wid] = inc;
+    __syncthreads();
+    if (wid == 0) {
+        CAff w = lane < NW ? wsum[lane] : id;
+#pragma unroll
+        for (int off = 1; off < 32; off <<= 1) {
+            CAff o;
+            o.a.x = __shfl_up_sync(0xffffffffu, w.a.x, off);
+            o.a.y = __shfl_up_sync(0xffffffffu, w.a.y, off);
+            o.b.x = __shfl_up_sync(0xffffffffu, w.b.x, off);
+            o.b.y = __shfl_up_sync(0xffffffffu, w.b.y, off);
+            if (lane >= off) w = caff_then(o, w);
+        }
+        if (lane < NW) wsum[lane] = w;
+    }
+    __syncthreads();
+    CAff lex;
+    lex.a.x = __shfl_up_sync(0xffffffffu, inc.a.x, 1);
+    lex.a.y = __shfl_up_sync(0xffffffffu, inc.a.y, 1);
+    lex.b.x = __shfl_up_sync(0xffffffffu, inc.b.x, 1);
+    lex.b.y = __shfl_up_sync(0xffffffffu, inc.b.y, 1);
+    if (lane == 0) lex = id;
+    *pre = wid > 0 ? caff_then(wsum[wid - 1], lex) : lex;
+    *tot = wsum[NW - 1];
+    __syncthreads();  // wsum is free again
+}
+
+// The Raman convolution kerr_I's second term needs, Re F^-1[F[|S|^2] R_f], as
+// the periodic solution of G[n] = z (G[n - 1] + I[n - 1]) (FullTabs::rz), with
+// I = |S|^2: each thread composes the step maps of its chunk of C points, a
+// block scan composes the chunks, G[-1] = G[N - 1] closes the period
+// (G[-1] = b / (1 - a) for the whole row's map a x + b), and each thread walks
+// its chunk again writing ramp Im G[n] -- times NT, as the FFT path leaves it
+// unnormalised -- to Q[pidx(n)].  O(N) work instead of two row FFTs; the same
+// circular convolution to ~1e-10 in exact arithmetic (raman_fit).
+template <int NT, int TT>
+__device__ __forceinline__ void raman_recurrence(const float2 *S, float2 *Q, float2 z, float ramp) {
+    constexpr int C = NT >= TT ? NT / TT : 1;
+    __shared__ CAff wsum[32];
+    const int n0 = (int)threadIdx.x * C;
+    CAff m{make_float2(1.0f, 0.0f), make_float2(0.0f, 0.0f)};
+    __syncthreads();  // the chunks read points of S other threads wrote
+    if (n0 < NT) {
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+            const float2 sp = S[(n0 + j - 1 + NT) & (NT - 1)];
+            const float ip = fmaf(sp.x, sp.x, sp.y * sp.y);
+            m = CAff{c_mul(z, m.a), c_mul(z, make_float2(m.b.x + ip, m.b.y))};
+        }
+    }
+    CAff pre, tot;
+    block_scan_caff<TT>(m, wsum, &pre, &tot);
+    if (n0 < NT) {
+        // G[-1] = tot.b / (1 - tot.a)
+        const float2 d = make_float2(1.0f - tot.a.x, -tot.a.y);
+        const float dd = fmaf(d.x, d.x, d.y * d.y);
+        const float2 g0 = make_float2(fmaf(tot.b.x, d.x, tot.b.y * d.y) / dd, fmaf(tot.b.y, d.x, -tot.b.x * d.y) / dd);
+        float2 G = c_add(c_mul(pre.a, g0), pre.b);  // G[n0 - 1]
+#pragma unroll
+        for (int j = 0; j < C; ++j) {
+            const float2 sp = S[(n0 + j - 1 + NT) & (NT - 1)];
+            const float ip = fmaf(sp.x, sp.x, sp.y * sp.y);
+            G = c_mul(z, make_float2(G.x + ip, G.y));
+            Q[pidx(n0 + j)] = make_float2(ramp * G.y * (float)NT, 0.0f);
+        }
+    }
+    __syncthreads();
+}
+
 // CTAs per SM the full-physics kernels are compiled for: what their shared
 // memory admits, at most 2 (two CTAs of 256 threads, or one of 512 at N_t =
 // 4096: <= 128 registers a thread either way; with the whole block inlined
@@ -116,7 +212,10 @@ __device__ __noinline__ float2 *rhs_full(const FullRows m, const float *__restri
     const float2 *S = m.S;
     // Raman: kerr_I's convolution term Re F^-1[F[|S|^2] R_f], left in Q
     const float2 *Q = nullptr;
-    if (ft.Rf) {
+    if (ft.Rf && ft.riir) {
+        raman_recurrence<NT, TT>(S, B0, ft.rz, ft.ramp);
+        Q = B0;
+    } else if (ft.Rf) {
         for (int t = threadIdx.x; t < NT; t += TT) {
             const float2 v = S[t];
             B0[pidx(t)] = make_float2(fmaf(v.x, v.x, v.y * v.y), 0.0f);

@@ -52,7 +52,9 @@ k_split_full(const float2 *__restrict__ u, const float *__restrict__ rho, const 
     for (int t = threadIdx.x; t < NT; t += full_threads<NT>()) rhs[base + t] = K[pidx(t)];
 }
 
-static FullTabs ctx_tabs(const nlse_ctx *c) { return FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf}; }
+static FullTabs ctx_tabs(const nlse_ctx *c) {
+    return FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf, c->raman_z, c->raman_amp, c->raman_iir};
+}
 
 cudaError_t launch_nl_full(nlse_ctx *c, float2 *u, const float *rho, const float *rho_s, float dz,
                            cudaStream_t st) {

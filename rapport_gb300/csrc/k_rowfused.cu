@@ -197,7 +197,7 @@ cudaError_t row_plan_tune(int logNt, int Nr, const float2 *tw, const float *lut,
     a.dz = 2.5e-6f;
     a.stats = stats;
     a.rho_s = nullptr;
-    a.ft = FullTabs{nullptr, nullptr, nullptr};
+    a.ft = FullTabs{nullptr, nullptr, nullptr, make_float2(0.0f, 0.0f), 0.0f, 0};
     a.f16 = 0;
     a.scale = scale;
     for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {

@@ -6,6 +6,7 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <algorithm>
 #include <vector>
 
 #include "nlse_internal.cuh"
@@ -160,6 +161,77 @@ static int check_desc(const nlse_grid_desc *d, nlse_error_slot *err) {
         }
     }
     return NLSE_OK;
+}
+
+// In-place radix-2 FFT of n complex values (re, im interleaved), sign -1 forward,
+// +1 inverse (unnormalised); FP64, host.
+static void fft64(std::vector<double> &a, int n, int sign) {
+    for (int i = 1, j = 0; i < n; ++i) {
+        int bit = n >> 1;
+        for (; j & bit; bit >>= 1) j ^= bit;
+        j ^= bit;
+        if (i < j) {
+            std::swap(a[2 * i], a[2 * j]);
+            std::swap(a[2 * i + 1], a[2 * j + 1]);
+        }
+    }
+    for (int len = 2; len <= n; len <<= 1) {
+        const double ang = sign * 2.0 * M_PI / len;
+        for (int i = 0; i < n; i += len)
+            for (int k = 0; k < len / 2; ++k) {
+                const double wr = cos(ang * k), wi = sin(ang * k);
+                const int u = i + k, v = i + k + len / 2;
+                const double xr = a[2 * v] * wr - a[2 * v + 1] * wi, xi = a[2 * v] * wi + a[2 * v + 1] * wr;
+                a[2 * v] = a[2 * u] - xr;
+                a[2 * v + 1] = a[2 * u + 1] - xi;
+                a[2 * u] += xr;
+                a[2 * u + 1] += xi;
+            }
+    }
+}
+
+// Whether the Raman response spectrum Rf (n complex values, the reference's
+// R_f = fft(ifftshift(resp)) dt, grids.py) is a sampled damped sine, so that
+// the row's circular convolution is the periodic solution of a first-order
+// complex recurrence.  The kernel k = ifft(Rf) (= dt h) has k[m + 1] =
+// p k[m] - q k[m - 1] with p = 2 r cos(theta), q = r^2 for such a response;
+// p, q come from k[1..3] (k[0] = 0), and the recurrence's own kernel -- with
+// the periodic wrap, dt h_eff[m] = Im(A z^m / (1 - z^n)), z = r e^{i theta} --
+// must reproduce every k[m] to 1e-9 of its largest value (the reference's
+// kernel is zero for negative times; there the recurrence's terms are below
+// |z|^{n/2}).  Then *zr + i *zi = z and *amp = A.
+static bool raman_fit(const double *Rf, int n, double *zr, double *zi, double *amp) {
+    if (n < 8 || (n & (n - 1))) return false;
+    std::vector<double> k(Rf, Rf + 2 * (size_t)n);
+    fft64(k, n, +1);
+    double kmax = 0.0;
+    for (int m = 0; m < n; ++m) {
+        k[2 * m] /= n;
+        kmax = fmax(kmax, fabs(k[2 * m]));
+    }
+    const double k1 = k[2], k2 = k[4], k3 = k[6];
+    if (!(kmax > 0.0) || !(fabs(k1) > 1e-6 * kmax)) return false;
+    const double p = k2 / k1, q = (p * k2 - k3) / k1;
+    if (!(q > 0.0 && q < 1.0)) return false;
+    const double r = sqrt(q), c = p / (2.0 * r);
+    if (!(fabs(c) < 1.0)) return false;
+    const double th = acos(c), A = k1 / (r * sin(th));
+    // z^n and the wrap factor 1 / (1 - z^n)
+    const double rn = pow(r, (double)n), tn = th * n;
+    const double wr = 1.0 - rn * cos(tn), wi = -rn * sin(tn), wd = wr * wr + wi * wi;
+    double err = 0.0;
+    for (int m = 0; m < n; ++m) {
+        // Im(A z^m' / (1 - z^n)) with m' = m, or n for m = 0
+        const int mm = m == 0 ? n : m;
+        const double zm = pow(r, (double)mm), ar = A * zm * cos(th * mm), ai = A * zm * sin(th * mm);
+        const double model = (ai * wr - ar * wi) / wd;
+        err = fmax(err, fabs(model - k[2 * m]));
+    }
+    if (!(err <= 1e-9 * kmax)) return false;
+    *zr = r * cos(th);
+    *zi = r * sin(th);
+    *amp = A;
+    return true;
 }
 
 // Intensity below which lut_rate_dt's interpolation reads two zero entries of
@@ -336,6 +408,10 @@ extern "C" int nlse_create(const nlse_grid_desc *d, nlse_ctx **out) {
         std::vector<float2> rf(Nt);
         for (int k = 0; k < Nt; ++k) rf[k] = make_float2((float)d->R_f[2 * k], (float)d->R_f[2 * k + 1]);
         NLSE_TRY(dev_upload(err, &c->d_Rf, rf.data(), Nt));
+        double zr = 0, zi = 0, amp = 0;
+        c->raman_iir = raman_fit(d->R_f, Nt, &zr, &zi, &amp) ? 1 : 0;
+        c->raman_z = make_float2((float)zr, (float)zi);
+        c->raman_amp = (float)amp;
     }
     if (d->flags & NLSE_F_SELF_STEEP) {
         std::vector<float> t(Nt);
@@ -627,7 +703,7 @@ static RowFusedArgs row_args(nlse_ctx *c, double dz) {
     a.dz = (float)dz;
     a.stats = c->d_flag;
     a.rho_s = nullptr;
-    a.ft = FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf};
+    a.ft = FullTabs{c->d_Tss, c->d_invUnl, c->d_Rf, c->raman_z, c->raman_amp, c->raman_iir};
     a.f16 = c->op_f16;
     a.scale = c->d_scale;
     a.stf = c->stf;

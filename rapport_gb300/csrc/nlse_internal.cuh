@@ -54,6 +54,13 @@ struct FullTabs {
     const float *T;       // T-hat(Omega) (self-steepening)
     const float *invU;    // U^-1(Omega) of split() (space-time focusing)
     const float2 *Rf;     // Raman response spectrum R_f
+    // The Raman convolution as a recurrence (riir = 1): the response R_f stands
+    // for, sampled, is dt h[m] = Im(ramp z^m) for m >= 1 (a damped sine), so
+    // the circular convolution dt (h * I)[n] = Im(ramp G[n]) with
+    // G[n] = z (G[n - 1] + I[n - 1]), periodic (see raman_fit)
+    float2 rz;
+    float ramp;
+    int riir;
 };
 
 // Carrier-rate scan constants.
@@ -164,6 +171,9 @@ struct nlse_ctx {
     int device;
     int Nr, Nt, logNt, flags;
     double dt, komega, Rk_iRk;
+    float2 raman_z;        // the Raman convolution as a recurrence (FullTabs::rz, ramp, riir)
+    float raman_amp;
+    int raman_iir;
     NLParams nl;
     ScanParams sc;
     // device tables

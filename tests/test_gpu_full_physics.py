@@ -181,3 +181,46 @@ def test_full_physics_limits():
     cfg = R.workload_config(16, 8192, 1e-4, 1e-5, 3e-13, 5e-6, 1, enable_self_steepening=True)
     with pytest.raises(_lib.NLSEError, match="4096"):
         _lib.Context(cfg, R.build_grids(cfg))
+
+
+def _raman_fit_error(Rf):
+    """Relative error of the damped-sine model of the Raman kernel ifft(R_f)
+    (the check the library makes before it takes the recurrence)."""
+    n = len(Rf)
+    k = np.fft.ifft(Rf).real
+    k1, k2, k3 = k[1], k[2], k[3]
+    p = k2 / k1
+    q = (p * k2 - k3) / k1
+    r = np.sqrt(q)
+    th = np.arccos(p / (2 * r))
+    a = k1 / (r * np.sin(th))
+    m = np.arange(n)
+    z = r * np.exp(1j * th)
+    model = (a * z ** np.where(m == 0, n, m) / (1 - z ** n)).imag
+    return np.abs(model - k).max() / np.abs(k).max()
+
+
+@pytest.mark.parametrize("Nt", [1024, 2048])
+def test_raman_recurrence_vs_oracle(Nt):
+    """On a +-800 fs window the Raman response has decayed to ~e^-25 at the
+    window's half width, so the library takes the Raman convolution as the
+    periodic solution of a first-order recurrence (a block scan) instead of
+    two row FFTs: split() and 6 z-steps with every term on, in the plain and
+    split-BF16 forms, against the FP64 oracle (which convolves by FFTs as the
+    reference does)."""
+    from rapport_gb300 import _lib
+    c = Case(64, Nt, 2e-4, 2e-5, 800e-15, 100e-15, 2.0, 1e-2, 5e-6, 6, 0, **FULL_PHYSICS)
+    assert _raman_fit_error(c.g["R_f"]) <= 1e-9  # the library's acceptance test
+    z0 = np.zeros(c.u0.shape)
+    rhs_o, al_o = c.og.split(c.u0, z0, z0)
+    rhs, al = c.nl.split(dev(c.u0), dev(z0), dev(z0))
+    assert rel_l2(host(rhs), rhs_o) < 2e-5
+    uo, ro, so = c.og.propagate(c.u0.copy(), 6, c.dz)
+    for mode in (_lib.MODE_PLAIN_F32, _lib.MODE_SPLIT_BF16):
+        u, rho, rs = dev(c.u0), dev(z0), dev(z0)
+        c.ctx.propagate(u, rho, rs, c.dz, 6, mode)
+        assert rel_l2(host(u), uo) < 5e-5, mode
+        assert np.abs(host(rho) - ro).max() <= 1e-3 * max(ro.max(), 1e-30), mode
+        if so.max() > 0:
+            assert np.abs(host(rs) - so).max() <= 1e-3 * so.max(), mode
+    assert c.ctx.device_status() == 0
