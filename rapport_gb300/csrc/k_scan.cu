@@ -25,10 +25,10 @@
 // run out of shared memory.
 #include "scan_impl.cuh"
 
-// Threads a row: 256, 512 from N_t = 4096 and 1024 from 8192 -- 8 steps a
-// thread, so long rows keep short sequential chunks and 16-32 warps per CTA
-// (their scan arrays leave room for one CTA per SM).
-static int scan_threads(int Nt) { return Nt >= 8192 ? 1024 : (Nt >= 4096 ? 512 : NLSE_ROW_THREADS); }
+// Threads a row: 256, 512 from N_t = 2048 and 1024 from 8192 -- at most 8
+// steps a thread, so long rows keep short sequential chunks, and 16-32 warps
+// per CTA where the scan arrays leave room for only one or two CTAs per SM.
+static int scan_threads(int Nt) { return Nt >= 8192 ? 1024 : (Nt >= 2048 ? 512 : NLSE_ROW_THREADS); }
 
 __global__ void __launch_bounds__(1024)
 k_rate_scan(const float2 *__restrict__ u, float *__restrict__ rho, float *__restrict__ rho_s, int Nt,
