@@ -15,9 +15,10 @@
 // the correction passes through FP16: carrying the whole field through four
 // FP16 roundings per z-step left its values far below the peak near FP16's
 // exponent floor (~17 bits), rounded the same way step after step -- a
-// systematic drift of ~1e-5 per step.  Y is carried in 3 scaled FP16 terms
-// (~33 bits; its rounding is applied twice per half step), the field and v'
-// in 2 (~22 bits).  P2 - 1 is built in FP64 per dz (cos - 1 as -2 sin^2 of the
+// systematic drift of ~1e-5 per step.  Y is split into 3 scaled FP16 terms
+// (~33 bits), of which the products read the first two (~22 bits: as accurate
+// over 0.5 cm as three, since only the correction passes through them), the
+// field and v' in 2 (~22 bits).  P2 - 1 is built in FP64 per dz (cos - 1 as -2 sin^2 of the
 // half angle) and applied with its FP32 rounding remainder folded in.  The
 // FP16 scale of v' follows its measured maxima.
 #include "nlse_internal.cuh"

@@ -11,6 +11,12 @@
 
 #include "nlse_internal.cuh"
 
+// FP16 terms of diag(Y, Y) the space-time-focusing products read (k_stf.cu
+// writes three): two carry Y to ~22 bits, and the 0.5 cm error with space-time
+// focusing is the same with two as with three (1.50e-5 against 1.52e-5
+// relative L2), at 3 MMAs a k-slice instead of 4.
+constexpr int NLSE_STF_Y_TERMS = 2;
+
 static thread_local nlse_error_slot g_create_err;
 
 // cuTensorMapEncodeTiled, resolved through the runtime so that the library
@@ -720,7 +726,7 @@ static cudaError_t tc_gemm_raw(nlse_ctx *c, int variant, cudaStream_t st) {
     const int K2 = 2 * c->Nrp;
     const CUtensorMap *a = variant ? &c->tmA32 : &c->tmA, *b = variant ? &c->tmB32 : &c->tmB;
     // operator terms: 3 FP16 (space-time focusing: Y), 2 FP16 (merged E, split-FP16), or a_terms BF16
-    const int terms = c->stf ? 3 : (c->op_f16 ? 2 : c->a_terms);
+    const int terms = c->stf ? NLSE_STF_Y_TERMS : (c->op_f16 ? 2 : c->a_terms);
     return launch_gemm_tc(a, b, c->d_D, K2, c->Nt, K2, terms, variant, c->op_f16, c->stf, c->d_flag, st);
 }
 
@@ -1297,7 +1303,7 @@ static cudaError_t batch_products(nlse_batch *b, int g, int lane, cudaStream_t s
     const int s0 = b->nmain + (lane == 1 ? b->stf_lane : 0);
     const int sn = lane < 0 ? nst : (lane == 0 ? b->stf_lane : nst - b->stf_lane);
     if (sn <= 0 || e != cudaSuccess) return e;
-    e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + s0, sn, 3, c->gemm_variant, 1, b->d_flag, st);
+    e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + s0, sn, NLSE_STF_Y_TERMS, c->gemm_variant, 1, b->d_flag, st);
     for (int j = 0; j < b->nstf && e == cudaSuccess; ++j) {
         const int i = b->stf_idx[j];
         if (lane >= 0 && (i < b->lane_pulse) != (lane == 0)) continue;
@@ -1305,7 +1311,7 @@ static cudaError_t batch_products(nlse_batch *b, int g, int lane, cudaStream_t s
         e = launch_stf_phase(q->d_D, q->d_P2s, q->d_Fb, q->Nr, q->Nrp, q->Nt, q->cY, g, q->d_scale, st);
     }
     if (e == cudaSuccess)
-        e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + s0, sn, 3, c->gemm_variant, 1, b->d_flag,
+        e = launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles + s0, sn, NLSE_STF_Y_TERMS, c->gemm_variant, 1, b->d_flag,
                                    st);
     return e;
 }
