@@ -408,7 +408,7 @@ def run_ours(args, rank, world, local_rank):
         if "zsteps_per_s" in results.get("plain", {}) else None,
     }
     if world == 1 and rank == 0 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(args.cpu_zsteps)
+        line["cpu_baseline"] = cpu_baseline(args.cpu_zsteps, args)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
@@ -416,8 +416,8 @@ def run_ours(args, rank, world, local_rank):
         dist.destroy_process_group()
 
 
-# ------------------------------------------------------------------ config 4: 64 mixed pulses
-def config4_pulses(n=64, seed=1):
+# ------------------------------------------------------------------ 64 pulses on mixed grids
+def mixed_pulses(n=64, seed=1):
     """The batch workload: rng = default_rng(seed); per-parameter draws in this
     order -- N_r in {512, 768, 1024}, N_t in {1024, 2048, 4096} (uniform),
     energy log-uniform 1-20 uJ, FWHM uniform 50-200 fs, w0 uniform 80-200 um,
@@ -435,7 +435,7 @@ def config4_pulses(n=64, seed=1):
             for i in range(n)]
 
 
-def run_config4(args, rank, world, local_rank):
+def run_mixed(args, rank, world, local_rank):
     import torch
     import rapport_gb300 as R
     from rapport_gb300 import _lib
@@ -445,7 +445,7 @@ def run_config4(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl", device_id=dev)
-    pulses = config4_pulses()
+    pulses = mixed_pulses()
     mine = shard_pulses([pulse_cost(p["Nr"], p["Nt"]) for p in pulses], world, rank)
     cfgs, grids, us, rhos = [], [], [], []
     for i in mine:
@@ -468,12 +468,14 @@ def run_config4(args, rank, world, local_rank):
         import torch.distributed as dist
         dist.barrier()
     torch.cuda.synchronize()
+    clk = ClockSampler(local_rank) if rank == 0 else None
     for i in range(args.steps):
         flush.fill_(float(i))
         ev[i][0].record()
         bt.propagate(us, rhos, None, 5e-6, Z)
         ev[i][1].record()
     torch.cuda.synchronize()
+    clocks = clk.stop() if clk else None
     t_ms = sum(a.elapsed_time(b) for a, b in ev)
     if world > 1:
         import torch.distributed as dist
@@ -491,7 +493,7 @@ def run_config4(args, rank, world, local_rank):
         "metric": "pulse-z-steps/s (1 GB300), split-BF16 batched, 64 mixed pulses", "value":
             len(pulses) * args.steps * Z / (t_ms * 1e-3), "unit": "pulse-z-steps/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True,
-        "scaling": "weak", "dtype": "bf16x3-split + f32", "data": "synthetic (config-4 draws, default_rng(1))",
+        "scaling": "weak", "dtype": "bf16x3-split + f32", "data": "synthetic (the 64-pulse draws, default_rng(1))",
         "config": {"workload": "64 pulses, N_r in {512,768,1024} x N_t in {1024,2048,4096}, 1-20 uJ, 50-200 fs, "
                                "w0 80-200 um, f 5-20 cm, dz 5 um", "z_steps_per_step": Z,
                    "grids": sorted({(p["Nr"], p["Nt"]) for p in pulses}), "parallelism": f"replicas{world}"},
@@ -503,6 +505,7 @@ def run_config4(args, rank, world, local_rank):
                       for nt in sorted({pulses[i]["Nt"] for i in mine})},
         "gemm_variant": bt.context(0).gemm_variant(),
         "launches_per_z_step": "2 grouped products + 2 row launches per N_t class (one per half step)",
+        "clocks": clocks,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -526,17 +529,18 @@ def physics_name(args):
 
 
 # ------------------------------------------------------------------ CPU (oracle) arm
-def _oracle_setup():
+def _oracle_setup(args):
+    """The oracle on the GPU arm's workload: the same grid (N_t from --nt), pulse and physics terms."""
     sys.path.insert(0, os.path.join(HERE, "oracle"))
     import nlse_oracle as O
-    w = WORKLOAD
-    og = O.OracleGrid(O.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"]))
+    w = dict(WORKLOAD, Nt=args.nt) if args.nt else WORKLOAD
+    og = O.OracleGrid(O.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], **physics_over(args)))
     u = O.lens_gaussian(og, w["w0"], w["fwhm"], w["E"], w["f"], w["seed"])
-    return og, u
+    return og, u, w
 
 
-def cpu_baseline(nz):
-    og, u = _oracle_setup()
+def cpu_baseline(nz, args):
+    og, u, w = _oracle_setup(args)
     rho = np.zeros(u.shape)
     rs = np.zeros(u.shape)
     og.update_plasma(u, rho, rs)
@@ -547,8 +551,8 @@ def cpu_baseline(nz):
     dt = time.perf_counter() - t
     cores, blas = host_cores()
     return {"value": nz / dt, "unit": "z-steps/s", "cores": cores, "blas_threads": blas, "kind": "port",
-            "sample": f"{nz} z-steps of the 1024x2048 workload (FP64 numpy/OpenBLAS + C carrier march, "
-                      f"OpenMP over r; Kerr, MPI + avalanche + recombination whatever physics the GPU arm ran)",
+            "sample": f"{nz} z-steps of the {w['Nr']}x{w['Nt']} workload (FP64 numpy/OpenBLAS + C carrier march, "
+                      f"OpenMP over r; physics: {physics_name(args)})",
             "what": "the oracle: an FP64 restatement of the reference path, pinned to the reference's own "
                     "outputs bit for bit or to 1e-12 (the reference itself needs CuPy and a GPU)"}
 
@@ -556,7 +560,7 @@ def cpu_baseline(nz):
 def run_reference(args, rank):
     if rank != 0:
         return
-    og, u = _oracle_setup()
+    og, u, w = _oracle_setup(args)
     rho = np.zeros(u.shape)
     rs = np.zeros(u.shape)
     for _ in range(args.warmup):
@@ -573,23 +577,24 @@ def run_reference(args, rank):
         "metric": METRIC, "value": v, "unit": "z-steps/s", "n_gpus": 0, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dt / args.steps * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64 (complex128)", "data": "synthetic",
-        "config": dict(CONFIG, form="reference CPU path (FP64 restatement)", z_steps_per_step=1),
+        "config": dict(CONFIG, Nt=w["Nt"], workload=CONFIG["workload"].replace("N_t=2048", f"N_t={w['Nt']}"),
+                       physics=physics_name(args), form="reference CPU path (FP64 restatement)", z_steps_per_step=1),
         "impl": "reference",
         "cpu_baseline": {"value": v, "unit": "z-steps/s", "cores": cores, "blas_threads": blas, "kind": "port",
-                         "sample": f"{args.steps} z-steps of the 1024x2048 workload"},
+                         "sample": f"{args.steps} z-steps of the {w['Nr']}x{w['Nt']} workload ({physics_name(args)})"},
         "e2e": {"value": v, "unit": "z-steps/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 
 
-# ------------------------------------------------------------------ config 5: one large pulse
-CONFIG5 = dict(Nr=2048, Nt=8192, R_max=3e-3, w0=200e-6, T_half=1.5e-12, fwhm=80e-15, E=20.0, f=0.15, dz=1.25e-6,
+# ------------------------------------------------------------------ one large pulse (2048 x 8192)
+LARGE_PULSE = dict(Nr=2048, Nt=8192, R_max=3e-3, w0=200e-6, T_half=1.5e-12, fwhm=80e-15, E=20.0, f=0.15, dz=1.25e-6,
                seed=0)
 # algorithmic bytes per point of the row / elementwise kernels, FLOPs per launch of the products
 ROW_BYTES = {"k_row_nl": 36.0, "k_row_next": 36.0, "k_row_entry": 28.0, "k_fft_phase_ifft": 16.0,
              "k_nonlinear_step": 20.0, "k_rate_scan": 12.0, "k_split": 24.0}
 
 
-def run_config5(args, rank, world, local_rank):
+def run_large(args, rank, world, local_rank):
     """One 2048 x 8192 pulse (20 uJ, 80 fs, w0 200 um, f 15 cm, dz 1.25 um): z-steps/s of each
     arithmetic and the roofline fraction of every kernel (per-launch CUDA events)."""
     import torch
@@ -597,15 +602,15 @@ def run_config5(args, rank, world, local_rank):
     from rapport_gb300 import _lib
     torch.cuda.set_device(local_rank)
     dev = torch.device("cuda", local_rank)
-    c5 = CONFIG5
+    lp = LARGE_PULSE
     Z = args.zsteps
-    cfg = R.workload_config(c5["Nr"], c5["Nt"], c5["R_max"], c5["w0"], c5["T_half"], c5["dz"], Z)
+    cfg = R.workload_config(lp["Nr"], lp["Nt"], lp["R_max"], lp["w0"], lp["T_half"], lp["dz"], Z)
     g = R.build_grids(cfg)
     ctx = _lib.Context(cfg, g)
-    u0 = R.envelope_lens(c5["w0"], c5["fwhm"], c5["E"], c5["f"], c5["seed"])(g["rr"], g["tt"], cfg, g)
+    u0 = R.envelope_lens(lp["w0"], lp["fwhm"], lp["E"], lp["f"], lp["seed"])(g["rr"], g["tt"], cfg, g)
     u0 = np.ascontiguousarray(u0.astype(np.complex64))
     hbm, bf16, bf16_s, src = peaks()
-    Nr, Nt = c5["Nr"], c5["Nt"]
+    Nr, Nt = lp["Nr"], lp["Nt"]
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
     modes = [("split_bf16", _lib.MODE_SPLIT_BF16), ("split_f16", _lib.MODE_SPLIT_F16), ("plain", _lib.MODE_PLAIN_F32)]
     forms, kernels, clocks = {}, {}, None
@@ -615,14 +620,14 @@ def run_config5(args, rank, world, local_rank):
         rs = torch.zeros_like(rho)
         K = args.steps if name != "plain" else max(2, args.steps // 3)
         for _ in range(args.warmup):
-            ctx.propagate(u, rho, rs, c5["dz"], Z, mode)
+            ctx.propagate(u, rho, rs, lp["dz"], Z, mode)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(K)]
         clk = ClockSampler(local_rank) if name == "split_bf16" else None
         for i in range(K):
             flush.fill_(float(i))
             ev[i][0].record()
-            ctx.propagate(u, rho, rs, c5["dz"], Z, mode)
+            ctx.propagate(u, rho, rs, lp["dz"], Z, mode)
             ev[i][1].record()
         torch.cuda.synchronize()
         if clk:
@@ -632,7 +637,7 @@ def run_config5(args, rank, world, local_rank):
         ctx.profile_start(K * Z * 16 + 64)
         for i in range(K):
             flush.fill_(float(i))
-            ctx.propagate(u, rho, rs, c5["dz"], Z, mode)
+            ctx.propagate(u, rho, rs, lp["dz"], Z, mode)
         prof = ctx.profile_read()
         assert ctx.device_status() == 0 and bool(torch.isfinite(u).all().item())
         per = {}
@@ -653,7 +658,7 @@ def run_config5(args, rank, world, local_rank):
         kernels[name] = per
         del u, rho, rs
     line = {
-        "metric": "z-steps/s (1 GB300), config 5: one 2048x8192 pulse", "value": forms["split_bf16"],
+        "metric": "z-steps/s (1 GB300), one 2048x8192 pulse", "value": forms["split_bf16"],
         "unit": "z-steps/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup, "higher_is_better": True,
         "scaling": "weak", "dtype": "bf16x3-split + f32", "data": "synthetic (seeded lens-focused Gaussian, 1% noise)",
         "config": {"workload": "single pulse, N_r=2048 (R_max 3 mm) x N_t=8192 (+-1.5 ps), 20 uJ, 80 fs, w0 200 um, "
@@ -803,8 +808,10 @@ def main():
                     help="the single / batched workload with every term the reference's Config turns on by "
                          "default: Raman (f_R 0.18), self-steepening, space-time focusing, the exciton channel "
                          "and its index term (the measured workload's rate table and grid otherwise)")
-    ap.add_argument("--workload", default="single", choices=["single", "config4", "config5", "tour"],
-                    help="tour: every kernel once at 1024 x 2048 (for ncu launch lists)")
+    ap.add_argument("--workload", default="single", choices=["single", "mixed64", "large", "tour"],
+                    help="mixed64: 64 pulses on mixed grids (N_r 512-1024, N_t 1024-4096) in one batch; "
+                         "large: one 2048 x 8192 pulse, every kernel's roofline; "
+                         "tour: every kernel once at 1024 x 2048 (for ncu launch lists)")
     ap.add_argument("--record-traffic", metavar="CSV",
                     help="write profiles/traffic_per_launch.json from an ncu CSV and exit")
     args = ap.parse_args()
@@ -817,11 +824,11 @@ def main():
     if args.impl == "reference":
         run_reference(args, rank)
         return
-    if args.workload == "config4":
-        run_config4(args, rank, world, local_rank)
+    if args.workload == "mixed64":
+        run_mixed(args, rank, world, local_rank)
         return
-    if args.workload == "config5":
-        run_config5(args, rank, world, local_rank)
+    if args.workload == "large":
+        run_large(args, rank, world, local_rank)
         return
     if args.workload == "tour":
         run_tour(args, rank, world, local_rank)

@@ -246,7 +246,7 @@ def main():
     for k in ("u_steps", "rho_steps", "steps_kept"):
         del hot[k]
     np.savez_compressed(os.path.join(HERE, "tiny_hot.npz"), **hot)
-    # BASELINE config 1 (256 x 512, 1 uJ, w0 100 um, R_max 1 mm, +-400 fs, f 10 cm),
+    # the CPU-runnable case (256 x 512, 1 uJ, w0 100 um, R_max 1 mm, +-400 fs, f 10 cm),
     # first 3 of its 2000 steps; every 8th radial row is kept to bound the fixture size.
     c1 = run_case(Nr=256, Nt=512, R_max=1e-3, w0=100e-6, T_half=400e-15, fwhm=100e-15,
                   energy_uJ=1.0, f=0.1, dz=5e-6, nsteps=3, seed=0,

@@ -23,7 +23,7 @@ def host(x):
 
 
 class Case:
-    """Product context + oracle grid for one workload (tiny / config-1 / ...)."""
+    """Product context + oracle grid for one workload (tiny / 256 x 512 / ...)."""
 
     def __init__(self, Nr, Nt, R_max, w0, T_half, fwhm, E, f, dz, nsteps=1, seed=0, **over):
         self.cfg = R.workload_config(Nr, Nt, R_max, w0, T_half, dz, max(nsteps, 1), **over)
@@ -57,6 +57,6 @@ class Case:
         return u * np.exp(-0.5 * dz * a)
 
 
-# config 2 of the measured workloads: 1024 x 2048, R_max 2 mm, +-800 fs, 5 uJ, w0 150 um, f 10 cm
+# the measured single-pulse workload: 1024 x 2048, R_max 2 mm, +-800 fs, 5 uJ, w0 150 um, f 10 cm
 CONFIG2 = dict(Nr=1024, Nt=2048, R_max=2e-3, w0=150e-6, T_half=800e-15, fwhm=100e-15, E=5.0, f=0.1,
                dz=2.5e-6)

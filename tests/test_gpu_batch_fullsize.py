@@ -5,7 +5,7 @@
   forms.  Every pulse must equal its own single-context run bit for bit, and
   the split-BF16 result must lie within 2e-5 (relative L2) of the FP64
   reference for the same input, densities within 1e-3 of the peak.
-* Mixed grids of the 64-pulse batch workload (bench.config4_pulses, seed 1):
+* Mixed grids of the 64-pulse batch workload (bench.mixed_pulses, seed 1):
   pulses 2, 3, 9 and 31 -- 1024 x 2048, 1024 x 4096, 512 x 1024 and
   768 x 4096, i.e. three N_t classes and three operator sizes in one grouped
   product -- with the same two checks.
@@ -73,10 +73,10 @@ def test_bench_batch_8x1024x2048(mode):
 
 
 @pytest.mark.parametrize("mode", [1, 2])
-def test_mixed_config4_grids(mode):
+def test_mixed_64_pulse_grids(mode):
     import bench
     import rapport_gb300 as R
-    P = bench.config4_pulses()
+    P = bench.mixed_pulses()
     picks = [P[i] for i in (2, 3, 9, 31)]
     assert sorted((p["Nr"], p["Nt"]) for p in picks) == [(512, 1024), (768, 4096), (1024, 2048), (1024, 4096)]
     dz = picks[0]["dz"]

@@ -1,4 +1,4 @@
-"""Parity at the measured grid (N_r = 1024, N_t = 2048, config 2) and
+"""Parity at the measured grid (N_r = 1024, N_t = 2048, the bench's single-pulse workload) and
 size-independent properties of the operators."""
 import numpy as np
 import pytest

@@ -1,4 +1,4 @@
-"""Config 5 grid (N_r = 2048, R_max 3 mm; N_t = 8192, +-1.5 ps; 20 uJ, 80 fs,
+"""The large single-pulse grid (N_r = 2048, R_max 3 mm; N_t = 8192, +-1.5 ps; 20 uJ, 80 fs,
 w0 200 um, f 15 cm, dz 1.25 um): both arithmetics against the FP64 GPU
 reference (pinned to the numpy oracle in test_gpu_accuracy.py) for two
 z-steps -- the largest single-GPU grid of the measured workloads (134 MB field,
@@ -15,7 +15,7 @@ CONFIG5 = dict(Nr=2048, Nt=8192, R_max=3e-3, w0=200e-6, T_half=1.5e-12, fwhm=80e
                dz=1.25e-6)
 
 
-def test_config5_two_z_steps_both_forms():
+def test_large_pulse_two_z_steps_both_forms():
     import torch
     import fp64_gpu
     from rapport_gb300._lib import MODE_PLAIN_F32, MODE_SPLIT_BF16

@@ -1,6 +1,6 @@
 """Replica sharding over pulses, on CPU with a world_size-2 gloo group.
 
-Each rank takes its share of a config-4-like batch (uneven grids), advances
+Each rank takes its share of a 64-pulse-like batch (uneven grids), advances
 its pulses with the FP64 oracle for two z-steps on a tiny grid (standing in
 for the GPU work the same code drives on a GB300), gathers the per-pulse
 results, and checks that every pulse was computed exactly once and equals a
