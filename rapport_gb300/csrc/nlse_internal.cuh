@@ -442,6 +442,21 @@ __device__ __forceinline__ void dft_small(float2 *v) {
 __host__ __device__ __forceinline__ constexpr int pidx(int i) { return i + (i >> 4); }
 __host__ __device__ __forceinline__ constexpr int fft_slots(int n) { return n + (n >> 4); }
 
+// A Stockham pass's gathers and scatters as compile-time offsets from one
+// padded base.  Sources j + r nb with nb = N / R a multiple of 16:
+// pidx(j + r nb) = pidx(j) + r (nb + nb / 16).  Destinations d0 + r NS,
+// d0 = (j - k) R + k: for NS a multiple of 16 the same; for NS = 8, d0 % 16 = k
+// < 8 ((j - k) R is a multiple of 16), so d0 % 16 + 8 r crosses r / 2 extra
+// 16-blocks: + 8 r + r / 2; for NS = 1 (d0 = j R, R dividing 16),
+// d0 % 16 + r < 16: + r.  Other strides keep pidx per point.
+__host__ __device__ constexpr bool pass_src_linear(int nb) { return nb % 16 == 0; }
+__host__ __device__ constexpr bool pass_dst_linear(int NS, int R) {
+    return NS % 16 == 0 || NS == 8 || (NS == 1 && 16 % R == 0);
+}
+__host__ __device__ constexpr int pass_dst_step(int NS, int r) {
+    return NS % 16 == 0 ? r * (NS + NS / 16) : (NS == 8 ? 8 * r + (r >> 1) : r);
+}
+
 // Radix of the Stockham pass at NS (the product of the radices applied so far)
 // for an N-point row: 8 while it divides what remains, then 4 or 2.
 __host__ __device__ constexpr int fft_radix(int N, int NS) {
@@ -547,13 +562,25 @@ __device__ __forceinline__ void stockham_pass(const float2 *__restrict__ src, fl
         if (nb % T == 0 || j < nb) {
             const int k = j & (NS - 1);
             float2 v[R];
+            if constexpr (pass_src_linear(nb)) {
+                const float2 *s = src + pidx(j);
 #pragma unroll
-            for (int r = 0; r < R; ++r) v[r] = src[pidx(j + r * nb)];
+                for (int r = 0; r < R; ++r) v[r] = s[r * (nb + nb / 16)];
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) v[r] = src[pidx(j + r * nb)];
+            }
             if (NS > 1) apply_twiddles<R, INV, N, NS, COMP>(v, k, tw);
             dft_small<R, INV>(v);
             const int d0 = (j - k) * R + k;
+            if constexpr (pass_dst_linear(NS, R)) {
+                float2 *d = dst + pidx(d0);
 #pragma unroll
-            for (int r = 0; r < R; ++r) dst[pidx(d0 + r * NS)] = v[r];
+                for (int r = 0; r < R; ++r) d[pass_dst_step(NS, r)] = v[r];
+            } else {
+#pragma unroll
+                for (int r = 0; r < R; ++r) dst[pidx(d0 + r * NS)] = v[r];
+            }
         }
     }
 }
@@ -756,13 +783,26 @@ __device__ __forceinline__ float2 *fft_regs_pass(float2 (&v)[N / T], float2 *src
         const int j = (int)threadIdx.x + q * T;
         const int k = j & (NS - 1);
         float2 y[R];
+        if constexpr (first) {
 #pragma unroll
-        for (int r = 0; r < R; ++r) y[r] = first ? v[q + r * Q] : src[pidx(j + r * nb)];
+            for (int r = 0; r < R; ++r) y[r] = v[q + r * Q];
+        } else if constexpr (pass_src_linear(nb)) {
+            const float2 *s = src + pidx(j);
+#pragma unroll
+            for (int r = 0; r < R; ++r) y[r] = s[r * (nb + nb / 16)];
+        } else {
+#pragma unroll
+            for (int r = 0; r < R; ++r) y[r] = src[pidx(j + r * nb)];
+        }
         if (NS > 1) apply_twiddles<R, INV, N, NS, COMP>(y, k, tw);
         dft_small<R, INV>(y);
         if constexpr (last) {
 #pragma unroll
             for (int r = 0; r < R; ++r) v[q + r * Q] = y[r];
+        } else if constexpr (pass_dst_linear(NS, R)) {
+            float2 *d = dst + pidx((j - k) * R + k);
+#pragma unroll
+            for (int r = 0; r < R; ++r) d[pass_dst_step(NS, r)] = y[r];
         } else {
             const int d0 = (j - k) * R + k;
 #pragma unroll
