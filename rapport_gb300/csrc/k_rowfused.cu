@@ -200,27 +200,34 @@ cudaError_t row_plan_tune(int logNt, int Nr, const float2 *tw, const float *lut,
     a.ft = FullTabs{nullptr, nullptr, nullptr, make_float2(0.0f, 0.0f), 0.0f, 0};
     a.f16 = 0;
     a.scale = scale;
+    // Every plan runs once untimed (module load, instruction cache, the clock
+    // leaving idle), then the plans are timed in turn over several rounds and
+    // each keeps its fastest round: a plan timed while the clock still ramps
+    // up, or in a disturbed round, is not chosen for that.
+    auto run = [&](int kind, int plan) {
+        return kind == 0 ? launch_row_nl(a, F32, Fb, D, rho, 0, plan, 0)
+                         : launch_row_next(a, F32, Fb, D, rho, nullptr, 1, 1, 1, 1, plan, 0);
+    };
     for (int kind = 0; kind < 2 && e == cudaSuccess; ++kind) {
         if (!want[kind]) continue;
-        float best = 1e30f;
-        int pick = 0;
-        for (int plan = 0; plan < 3 && e == cudaSuccess; ++plan) {
-            if (!(mask[kind] & (1 << plan))) continue;
-            for (int rep = 0; rep < 4 && e == cudaSuccess; ++rep) {
-                if (rep == 1) e = cudaEventRecord(e0, 0);
-                if (e != cudaSuccess) break;
-                e = kind == 0 ? launch_row_nl(a, F32, Fb, D, rho, 0, plan, 0)
-                              : launch_row_next(a, F32, Fb, D, rho, nullptr, 1, 1, 1, 1, plan, 0);
-            }
-            if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
-            if (e == cudaSuccess) e = cudaEventSynchronize(e1);
-            float ms = 1e30f;
-            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
-            if (e == cudaSuccess && ms < best) {
-                best = ms;
-                pick = plan;
+        float best[3] = {1e30f, 1e30f, 1e30f};
+        for (int plan = 0; plan < 3 && e == cudaSuccess; ++plan)
+            if (mask[kind] & (1 << plan)) e = run(kind, plan);
+        for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
+            for (int plan = 0; plan < 3 && e == cudaSuccess; ++plan) {
+                if (!(mask[kind] & (1 << plan))) continue;
+                e = cudaEventRecord(e0, 0);
+                for (int rep = 0; rep < 3 && e == cudaSuccess; ++rep) e = run(kind, plan);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, 0);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 1e30f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e == cudaSuccess && ms < best[plan]) best[plan] = ms;
             }
         }
+        int pick = 0;
+        for (int plan = 1; plan < 3; ++plan)
+            if (best[plan] < best[pick]) pick = plan;
         if (e == cudaSuccess) g_row_plan[dev][logNt][kind].store(pick + 1);
     }
     if (e0) cudaEventDestroy(e0);
