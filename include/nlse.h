@@ -239,7 +239,9 @@ void nlse_batch_destroy(nlse_batch *b);
  * (2 and 3 leave shared memory for other kernels' blocks on the same SM),
  * -1 = autotune (default: the first split-mode call times 0 and 1 on the
  * live operands and keeps the faster; that call synchronises its stream, so
- * make it before any stream capture).  A batch uses its first pulse's. */
+ * make it before any stream capture).  A batch times both variants on its own
+ * grouped launch at its first call in each form (also synchronising) and uses
+ * its pick, unless a variant was pinned on its first pulse's context. */
 int nlse_set_gemm_variant(nlse_ctx *ctx, int variant);
 int nlse_get_gemm_variant(const nlse_ctx *ctx);
 

@@ -1053,6 +1053,7 @@ extern "C" int nlse_set_gemm_variant(nlse_ctx *c, int variant) {
     if (variant < -1 || variant > 3) return bad(c, NLSE_ERR_INVALID_ARG, "variant must be -1 (autotune) or 0..3");
     c->gemm_variant = variant < 0 ? 0 : variant;
     c->tuned = variant >= 0;
+    c->pinned = variant >= 0;
     return NLSE_OK;
 }
 
@@ -1196,7 +1197,9 @@ struct nlse_batch {
     int ntiles;              // all tiles
     int nmain;               // tiles of the pulses without space-time focusing (the batch's form)
     int main_lane, stf_lane; // of those / of the rest: the tiles of lane 0's pulses
-    int *stf_idx, nstf;      // pulses with space-time focusing (products Y P Y in 3 FP16 terms)
+    int *stf_idx, nstf;      // pulses with space-time focusing (products Y P Y in FP16 terms)
+    int variant_of[2];       // the grouped product's pipeline variant per form (split-BF16, split-FP16),
+                             // tuned on the batch's own launch; -1 until then
     struct Class {
         int logNt, nblocks;
         int full;            // its pulses have the full-physics terms (row_nl kind 3)
@@ -1313,6 +1316,52 @@ static cudaError_t batch_products(nlse_batch *b, int g, int lane, cudaStream_t s
     return e;
 }
 
+// The grouped product's pipeline variant for the batch's form.  The grouped
+// launch over every pulse's tiles (8 x 1024 x 2048: 1024 tiles on 152 SMs) is
+// another load than the first pulse's own product (128 tiles), for which its
+// context was tuned, and can prefer the other variant; so the batch times both
+// on its own operands, once per form, as autotune_gemm does (each once
+// untimed, three interleaved rounds, each keeping its fastest).  The grouped
+// launch writes only the pulses' D, which the first z-step's product rewrites
+// before anything reads it.  A variant pinned on the first context stands.
+static int batch_tune(nlse_batch *b, cudaStream_t st) {
+    nlse_ctx *c = b->ctx[0];
+    if (c->pinned) return NLSE_OK;
+    int &pick = b->variant_of[b->f16 ? 1 : 0];
+    if (pick < 0 && b->nmain > 0) {
+        const int terms = b->f16 ? 2 : b->a_terms;
+        auto run = [&](int v) {
+            return launch_gemm_tc_grouped(b->d_maps, b->d_pulses, b->d_tiles, b->nmain, terms, v, b->f16, b->d_flag,
+                                          st);
+        };
+        cudaEvent_t e0 = nullptr, e1 = nullptr;
+        cudaError_t e = cudaEventCreate(&e0);
+        if (e == cudaSuccess) e = cudaEventCreate(&e1);
+        float best[2] = {1e30f, 1e30f};
+        for (int v = 0; v < 2 && e == cudaSuccess; ++v) e = run(v);
+        for (int round = 0; round < 3 && e == cudaSuccess; ++round) {
+            for (int v = 0; v < 2 && e == cudaSuccess; ++v) {
+                e = cudaEventRecord(e0, st);
+                if (e == cudaSuccess) e = run(v);
+                if (e == cudaSuccess) e = cudaEventRecord(e1, st);
+                if (e == cudaSuccess) e = cudaEventSynchronize(e1);
+                float ms = 1e30f;
+                if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, e0, e1);
+                if (e == cudaSuccess && ms < best[v]) best[v] = ms;
+            }
+        }
+        if (e0) cudaEventDestroy(e0);
+        if (e1) cudaEventDestroy(e1);
+        if (e != cudaSuccess) {
+            nlse_set_error(&b->err, NLSE_ERR_CUDA, "batch gemm autotune: %s", cudaGetErrorString(e));
+            return NLSE_ERR_CUDA;
+        }
+        pick = best[1] < best[0] ? 1 : 0;
+    }
+    if (pick >= 0) c->gemm_variant = pick;
+    return NLSE_OK;
+}
+
 // One z-step of one lane (0 or 1; -1: all pulses) on stream st: GEMM, row_nl
 // (consumes input g), GEMM, row_next (consumes g + 1; writes input g + 2 and
 // marches the carriers unless last).
@@ -1393,6 +1442,7 @@ extern "C" int nlse_batch_create(const nlse_grid_desc *descs, int n, nlse_batch 
     if (!b) return NLSE_ERR_INVALID_ARG;
     b->n = n;
     b->a_terms = 3;
+    b->variant_of[0] = b->variant_of[1] = -1;
     b->last_dz = NAN;
     b->ctx = (nlse_ctx **)calloc(n, sizeof(nlse_ctx *));
 #define BATCH_FAIL(st, ...)                       \
@@ -1679,6 +1729,10 @@ extern "C" int nlse_batch_propagate(nlse_batch *b, void *const *u, float *const 
              launch_row_batch(0, b->cls[k].logNt, *b->cls[k].tab, b->d_calls + b->cls[k].call0, b->cls[k].d_work,
                               b->cls[k].nblocks, 1, -1, 0, st),
              "batch row entry");
+    {
+        const int s = batch_tune(b, st);
+        if (s) return s;
+    }
     int it = 0;
     // the bulk of the non-final steps as graph launches of three steps each
     // (not while per-launch profiling records the individual kernels)

@@ -224,6 +224,7 @@ struct nlse_ctx {
     CUtensorMap tmB32;     // B operand, box 64 x 32
     int gemm_variant;      // 0 = BK 64 x 2 stages, 1 = BK 32 x 4 stages (autotuned)
     int tuned;
+    int pinned;            // gemm_variant set by nlse_set_gemm_variant (no tuner overrides it)
     // per-launch event profiling (off unless nlse_profile_start was called)
     int prof_on, prof_cap, prof_n;
     cudaEvent_t *prof_ev;  // 2 * prof_cap events

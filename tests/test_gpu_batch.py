@@ -265,3 +265,33 @@ def test_batch_with_space_time_focusing_pulses(mode):
         uo, rho_o, _ = og.propagate(O.lens_gaussian(og, 1.5e-5, 100e-15, 1.0 + 0.2 * i, 1e-2, 30 + i), 8, DZ)
         assert rel_l2(host(us[i]), uo) < 5e-5, i
         assert np.abs(host(rhos[i]) - rho_o).max() <= 1e-3 * max(rho_o.max(), 1e-30), i
+
+
+def test_batch_tunes_its_own_product_and_keeps_a_pinned_variant():
+    """The batch times the product's pipeline variants on its own grouped
+    launch (nlse_api.cu batch_tune) and takes the faster, in each form; the
+    variants agree bit for bit, so every pulse still equals its single-context
+    run.  A variant pinned on the first pulse's context is kept."""
+    from rapport_gb300 import _lib
+    cfgs, grids, u0s, _ = _setup()
+    for mode in (_lib.MODE_SPLIT_BF16, _lib.MODE_SPLIT_F16):
+        b = _lib.Batch(cfgs, grids)
+        b.set_mode(mode)
+        us = [dev(u) for u in u0s]
+        rhos = [dev(np.zeros(u.shape)) for u in u0s]
+        b.propagate(us, rhos, None, DZ, STEPS)
+        assert b.device_status() == 0
+        assert b.context(0).gemm_variant() in (0, 1)
+        for i, (cfg, g, u0) in enumerate(zip(cfgs, grids, u0s)):
+            ctx = _lib.Context(cfg, g)
+            u, rho, rs = dev(u0), dev(np.zeros(u0.shape)), dev(np.zeros(u0.shape))
+            ctx.propagate(u, rho, rs, DZ, STEPS, mode)
+            assert np.array_equal(host(us[i]), host(u)), (mode, i)
+            assert np.array_equal(host(rhos[i]), host(rho)), (mode, i)
+    b = _lib.Batch(cfgs, grids)
+    b.context(0).set_gemm_variant(3)
+    us = [dev(u) for u in u0s]
+    rhos = [dev(np.zeros(u.shape)) for u in u0s]
+    b.propagate(us, rhos, None, DZ, STEPS)
+    assert b.device_status() == 0
+    assert b.context(0).gemm_variant() == 3
