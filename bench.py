@@ -212,6 +212,7 @@ def run_ours(args, rank, world, local_rank):
     bmode = args.batch_mode if args.mode == "auto" else head
     other_batched = {}
     fallback = {"single_pulse": int(ctx.scan_fallback_rows())}
+    batch_variant = None
     if B > 0:
         envs = [np.ascontiguousarray(R.envelope_lens(w["w0"], w["fwhm"], w["E"], w["f"], w["seed"] + i)(
             g["rr"], g["tt"], cfg, g).astype(np.complex64)) for i in range(B)]
@@ -252,6 +253,7 @@ def run_ours(args, rank, world, local_rank):
             bt.propagate(bu, br, bs, w["dz"], Z)
         prof = pctx.profile_read()
         assert bt.device_status() == 0 and all(bool(torch.isfinite(x).all().item()) for x in bu)
+        batch_variant = bt.context(0).gemm_variant()  # the batch's own tuner pick (grouped launch)
         # e2e through the C ABI with host buffers: every step copies each pulse's field in from
         # pinned memory and its field + densities back out.  Two device (and host) buffer sets
         # alternate, so step i's read-back (own stream) overlaps step i + 1's upload (own stream)
@@ -398,7 +400,7 @@ def run_ours(args, rank, world, local_rank):
         "roofline": roof, "e2e": e2e, "gpu_launches": int(sum(v[0] for v in prof.values())),
         "kernels": {k: {"launches": v[0], "ms": round(v[1], 3)} for k, v in prof.items()},
         "scan_fallback_rows": fallback,
-        "autotuned": {"gemm_variant": ctx.gemm_variant(),
+        "autotuned": {"gemm_variant": ctx.gemm_variant(), "batch_gemm_variant": batch_variant,
                       "row_plans": dict(zip(("row_nl", "row_next"), _lib.row_plans(Nt)))},
         "clocks": clocks,
         "forms": dict({k + "_single_pulse": (round(v["zsteps_per_s"], 1) if "zsteps_per_s" in v else v)
