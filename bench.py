@@ -50,12 +50,14 @@ def peaks():
     return 6800.0, 1900.0, 1700.0, "fallback"
 
 
-def measured_traffic(kernel):
+TRAFFIC_JSON = os.path.join(HERE, "profiles", "traffic_per_launch.json")
+
+
+def measured_traffic(kernel, path=TRAFFIC_JSON):
     """DRAM bytes (read + write) per launch of a kernel from the ncu capture in
     profiles/traffic_per_launch.json, if that capture was taken of the kernel
     sources being run (same kernel fingerprint); else (None, why)."""
     from rapport_gb300.build import kernel_fingerprint
-    path = os.path.join(HERE, "profiles", "traffic_per_launch.json")
     if not os.path.exists(path):
         return None, "no capture"
     with open(path) as f:
@@ -749,7 +751,7 @@ def run_tour(args, rank, world, local_rank):
     print("kernel tour done")
 
 
-def record_traffic(csv_path):
+def record_traffic(csv_path, out_path=TRAFFIC_JSON):
     """Write profiles/traffic_per_launch.json from an ncu CSV of
     gpu__time_duration.sum, dram__bytes_read.sum and dram__bytes_write.sum
     (one row per launch and metric), stamped with the kernel fingerprint of the
@@ -781,8 +783,7 @@ def record_traffic(csv_path):
            "kernels": {k: {"bytes_per_launch": int(sum(v) / len(v)), "launches": len(v), "kernel_fingerprint": fp,
                            "note": f"mean of {len(v)} launches, capture {os.path.basename(csv_path)}"}
                        for k, v in sorted(out.items())}}
-    path = os.path.join(HERE, "profiles", "traffic_per_launch.json")
-    with open(path, "w") as f:
+    with open(out_path, "w") as f:
         json.dump(rec, f, indent=1)
     print(json.dumps(rec, indent=1))
 
