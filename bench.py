@@ -141,6 +141,8 @@ def run_ours(args, rank, world, local_rank):
         dist.init_process_group("nccl", device_id=dev)
     w = dict(WORKLOAD, Nt=args.nt) if args.nt else WORKLOAD
     Z = args.zsteps
+    if args.row_plans:
+        _lib.set_row_plans(w["Nt"], *args.row_plans)
     cfg = R.workload_config(w["Nr"], w["Nt"], w["R_max"], w["w0"], w["T_half"], w["dz"], Z, **physics_over(args))
     g = R.build_grids(cfg)
     ctx = _lib.Context(cfg, g)
@@ -801,6 +803,9 @@ def main():
     ap.add_argument("--cpu-zsteps", type=int, default=2, help="z-steps timed for cpu_baseline")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--batch", type=int, default=8, help="pulses of the batched (headline) form; 0 = single pulse")
+    ap.add_argument("--row-plans", type=int, nargs=2, metavar=("NL", "NEXT"),
+                    help="pin the row kernels' plans for the single / batched workload's N_t instead of tuning "
+                         "them (for profiling: under ncu the tuner's timings are meaningless)")
     ap.add_argument("--nt", type=int, default=0,
                     help="time points of the single / batched workload instead of 2048 (same +-800 fs window); "
                          "4096 is the reference Config's default")
